@@ -1,0 +1,235 @@
+"""Host-side mirror of the reference's particle-path interface over the C ABI.
+
+``PicContext`` stands in for PICurv's ``UserCtx`` + DMSwarm on one GPU: it
+owns the device-resident grid, velocity field and swarm, and exposes the
+reference's operations (``PerformInitialSetup``, ``AdvanceStep`` = one
+iteration of ``AdvanceSimulation_TEST``) with the reference's error codes
+raised as ``PetscError``.  Arrays cross the boundary in the reference's own
+layouts (DMSwarm ``[n][bs]`` fields, DMDA ``[k][j][i]`` arrays).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import FdfStepInfo
+
+ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG", 63: "PETSC_ERR_ARG_OUTOFRANGE",
+             73: "PETSC_ERR_ARG_WRONGSTATE", 76: "PETSC_ERR_LIB", 83: "PETSC_ERR_USER", 85: "PETSC_ERR_ARG_NULL",
+             97: "PETSC_ERR_GPU"}
+NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
+
+
+class PetscError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERR_NAMES.get(code, code)} ({code}): {msg}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+@dataclass
+class SwarmArrays:
+    """DMSwarm fields in the reference's layout."""
+    position: np.ndarray   # [n][3] f64
+    velocity: np.ndarray   # [n][3] f64
+    weight: np.ndarray     # [n][3] f64
+    P: np.ndarray          # [n]    f64
+    cell: np.ndarray       # [n][3] i64  DMSwarm_CellID
+    pid: np.ndarray        # [n]    i64  DMSwarm_pid
+    status: np.ndarray     # [n]    i64  DMSwarm_location_status
+
+    @property
+    def n(self) -> int:
+        return len(self.pid)
+
+    @classmethod
+    def create(cls, position, cell=None, pid=None, P=101325.0, status=UNINITIALIZED) -> "SwarmArrays":
+        n = len(position)
+        return cls(position=np.ascontiguousarray(position, dtype=np.float64).reshape(n, 3).copy(),
+                   velocity=np.zeros((n, 3)), weight=np.zeros((n, 3)), P=np.full(n, P, dtype=np.float64),
+                   cell=(np.full((n, 3), -1, dtype=np.int64) if cell is None
+                         else np.ascontiguousarray(cell, dtype=np.int64).reshape(n, 3).copy()),
+                   pid=(np.arange(n, dtype=np.int64) if pid is None else np.asarray(pid, dtype=np.int64).copy()),
+                   status=np.full(n, status, dtype=np.int64))
+
+    @classmethod
+    def empty(cls, n: int) -> "SwarmArrays":
+        return cls(position=np.zeros((n, 3)), velocity=np.zeros((n, 3)), weight=np.zeros((n, 3)), P=np.zeros(n),
+                   cell=np.zeros((n, 3), dtype=np.int64), pid=np.zeros(n, dtype=np.int64),
+                   status=np.zeros(n, dtype=np.int64))
+
+    def truncated(self, n: int) -> "SwarmArrays":
+        return SwarmArrays(self.position[:n], self.velocity[:n], self.weight[:n], self.P[:n], self.cell[:n],
+                           self.pid[:n], self.status[:n])
+
+    def sorted_by_pid(self) -> "SwarmArrays":
+        o = np.argsort(self.pid, kind="stable")
+        return SwarmArrays(self.position[o], self.velocity[o], self.weight[o], self.P[o], self.cell[o], self.pid[o],
+                           self.status[o])
+
+
+class PicContext:
+    """Device-resident grid + swarm on one GPU (the C ABI's FdfContext)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.fdf_ContextCreate(ctypes.byref(h), int(device))
+        if rc:
+            raise PetscError(rc, "fdf_ContextCreate failed (no usable CUDA device?)")
+        self.h = h
+        self.dims = None
+        self._cap = 0
+
+    # -- lifetime
+    def close(self):
+        if self.h:
+            self.lib.fdf_ContextDestroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc:
+            msg = self.lib.fdf_GetLastError(self.h)
+            raise PetscError(rc, msg.decode() if msg else "")
+
+    # -- set-up
+    def set_grid(self, coor: np.ndarray):
+        coor = np.ascontiguousarray(coor, dtype=np.float64)
+        KM, JM, IM = (s - 1 for s in coor.shape[:3])
+        self._check(self.lib.fdf_SetGrid(self.h, IM, JM, KM, _ptr(coor)))
+        self.dims = (IM, JM, KM)
+
+    def set_ucat(self, ucat: np.ndarray):
+        ucat = np.ascontiguousarray(ucat, dtype=np.float64)
+        IM, JM, KM = self.dims
+        if ucat.shape[:3] == (KM + 1, JM + 1, IM + 1):
+            node_sized = 1
+        elif ucat.shape[:3] == (KM, JM, IM):
+            node_sized = 0
+        else:
+            raise ValueError(f"ucat shape {ucat.shape} matches neither the cell nor the node layout")
+        self._check(self.lib.fdf_SetUcat(self.h, _ptr(ucat), node_sized))
+
+    def set_dt(self, dt: float):
+        self._check(self.lib.fdf_SetTimeStep(self.h, float(dt)))
+
+    def set_volume(self, v: float):
+        self._check(self.lib.fdf_SetParticleVolume(self.h, float(v)))
+
+    def reserve(self, cap: int):
+        self._check(self.lib.fdf_ReserveParticles(self.h, int(cap)))
+        self._cap = max(self._cap, int(cap))
+
+    def set_swarm(self, s: SwarmArrays):
+        arrs = [np.ascontiguousarray(a) for a in (s.position, s.velocity, s.weight, s.P, s.cell, s.pid, s.status)]
+        assert arrs[0].dtype == np.float64 and arrs[4].dtype == np.int64
+        self._check(self.lib.fdf_SetSwarm(self.h, s.n, *[_ptr(a) for a in arrs]))
+        self._cap = max(self._cap, s.n)
+
+    def load_workload(self, wl, P: float = 101325.0):
+        self.set_grid(wl.coor)
+        self.set_ucat(wl.ucat)
+        self.set_dt(wl.dt)
+        self.set_volume(wl.volume)
+        self.set_swarm(SwarmArrays.create(wl.pos, cell=wl.cell0, P=P))
+
+    # -- read back
+    def size(self) -> int:
+        n = ctypes.c_int64()
+        self._check(self.lib.fdf_GetSwarmSize(self.h, ctypes.byref(n)))
+        return n.value
+
+    def get_swarm(self) -> SwarmArrays:
+        n = self.size()
+        out = SwarmArrays.empty(n)
+        got = ctypes.c_int64()
+        self._check(self.lib.fdf_GetSwarm(self.h, n, ctypes.byref(got), _ptr(out.position), _ptr(out.velocity),
+                                          _ptr(out.weight), _ptr(out.P), _ptr(out.cell), _ptr(out.pid),
+                                          _ptr(out.status)))
+        return out.truncated(got.value)
+
+    def get_scattered(self):
+        IM, JM, KM = self.dims
+        count = np.zeros((KM + 1, JM + 1, IM + 1))
+        avg = np.zeros_like(count)
+        self._check(self.lib.fdf_GetScatteredFields(self.h, _ptr(count), _ptr(avg)))
+        return count, avg
+
+    def get_corner(self):
+        IM, JM, KM = self.dims
+        c = np.zeros((KM + 1, JM + 1, IM + 1, 3))
+        self._check(self.lib.fdf_GetCornerField(self.h, _ptr(c)))
+        return c
+
+    def get_faces(self):
+        IM, JM, KM = self.dims
+        fi = np.zeros((KM, JM, IM + 1)); fj = np.zeros((KM, JM + 1, IM)); fk = np.zeros((KM + 1, JM, IM))
+        self._check(self.lib.fdf_GetFaceDeposits(self.h, _ptr(fi), _ptr(fj), _ptr(fk)))
+        return fi, fj, fk
+
+    # -- the hot path
+    def initial_setup(self) -> FdfStepInfo:
+        info = FdfStepInfo()
+        self._check(self.lib.fdf_PerformInitialSetup(self.h, ctypes.byref(info)))
+        return info
+
+    def step(self, info: bool = True) -> FdfStepInfo | None:
+        if info:
+            inf = FdfStepInfo()
+            self._check(self.lib.fdf_AdvanceStep(self.h, ctypes.byref(inf)))
+            return inf
+        self._check(self.lib.fdf_AdvanceStep(self.h, None))
+        return None
+
+    def steps(self, n: int):
+        self._check(self.lib.fdf_AdvanceSteps(self.h, int(n)))
+
+    def synchronize(self):
+        self._check(self.lib.fdf_Synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.fdf_GetStream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.fdf_GetLaunchCount(self.h))
+
+    STAGES = ("center_to_corner", "advect_locate", "sort_by_cell", "cell_bounds", "gather_interpolate",
+              "deposit")
+
+    def counters(self) -> tuple[int, int]:
+        """(particle-steps advanced, walk evaluations) since the swarm was set."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.fdf_GetCounters(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.fdf_SetProfiling(self.h, 1 if on else 0))
+
+    def stage_times(self) -> dict:
+        """{stage: (total ms, runs)} since profiling was enabled (CUDA events on the context stream)."""
+        ms = np.zeros(len(self.STAGES))
+        runs = np.zeros(len(self.STAGES), dtype=np.int64)
+        self._check(self.lib.fdf_GetStageTimes(self.h, _ptr(ms), _ptr(runs), len(self.STAGES)))
+        return {name: (float(ms[i]), int(runs[i])) for i, name in enumerate(self.STAGES)}

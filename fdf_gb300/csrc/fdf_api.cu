@@ -1,0 +1,517 @@
+// fdf_api.cu -- the C ABI (include/fdf_gb300.h): device context, transfers, and
+// the step pipeline on the context's stream.
+//
+// Step pipeline (no host round trip):
+//   center->corner (ucat -> node field)
+//   locate  (advect, walk from the previous cell, weights; removed particles get key Nc)
+//   radix sort by cell key (stable)   ->  cell_start[Nc+1] boundary fill
+//   gather + interpolate into the alternate buffer (sorted order)
+//   deposit (cell count / P average, face volumes) from the sorted segments
+#include "fdf_internal.cuh"
+#include "../../include/fdf_gb300.h"
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+struct FdfContext {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  GridDims g{0, 0, 0, 0, 0};
+  bool has_grid = false, has_ucat = false;
+  double *coor = nullptr, *planes = nullptr, *ucat = nullptr, *corner = nullptr, *bbox = nullptr;
+  double *count = nullptr, *avg = nullptr, *fi = nullptr, *fj = nullptr, *fk = nullptr;
+  double bbox_h[6] = {0, 0, 0, 0, 0, 0};
+  double dt = 0.0, volume = 1.0;
+  int cap = 0;
+  SwarmBuf buf[2];
+  int cur = 0;
+  void *swarm_mem = nullptr;
+  unsigned int *keys = nullptr, *vals = nullptr;   // point into keyval_mem or radix_mem (swapped by the sort)
+  void *keyval_mem = nullptr;
+  void *radix_mem = nullptr;
+  RadixScratch rs{};
+  int *cell_start = nullptr;
+  DevCounters *cnt = nullptr;
+  void *staging = nullptr;
+  size_t staging_bytes = 0;
+  unsigned int sentinel = 0;
+  int key_bits = 1;
+  bool swarm_set = false;
+  long long launches = 0;
+  // stage timing: events recorded on the context stream between pipeline stages
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, std::pair<size_t, size_t>>> ev_spans;   // (stage, (start ev, end ev))
+  std::string last_error;
+};
+
+namespace {
+
+int fail(FdfContext *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+#define CU(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? FDF_ERR_MEM : FDF_ERR_GPU,       \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+  } while (0)
+
+#define CHECK_LAUNCH()                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                  \
+    if (e_ != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+void cfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+size_t swarm_bytes_per_buf(int cap) {
+  return (size_t)cap * (10 * sizeof(double) + sizeof(long long) + sizeof(int) + 1) + 16 * 256;
+}
+
+void carve_swarm(char *p, int cap, SwarmBuf &b) {
+  auto take = [&](size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) / 256 * 256;
+    return r;
+  };
+  b.x = (double *)take(8ull * cap); b.y = (double *)take(8ull * cap); b.z = (double *)take(8ull * cap);
+  b.u = (double *)take(8ull * cap); b.v = (double *)take(8ull * cap); b.w = (double *)take(8ull * cap);
+  b.a1 = (double *)take(8ull * cap); b.a2 = (double *)take(8ull * cap); b.a3 = (double *)take(8ull * cap);
+  b.P = (double *)take(8ull * cap);
+  b.pid = (long long *)take(8ull * cap);
+  b.cell = (int *)take(4ull * cap);
+  b.status = (unsigned char *)take((size_t)cap);
+}
+
+constexpr long long FDF_MAX_PARTICLES = 512LL * 1024 * 1024;
+
+int bits_for(unsigned long long v) {
+  int b = 1;
+  while (b < 32 && (1ull << b) <= v) ++b;
+  return b;
+}
+
+// Stage ids reported by fdf_GetStageTimes.
+enum { STAGE_CORNER = 0, STAGE_LOCATE = 1, STAGE_SORT = 2, STAGE_BOUNDS = 3, STAGE_GATHER_INTERP = 4,
+       STAGE_DEPOSIT = 5, NUM_STAGES = 6 };
+
+size_t record_event(FdfContext *ctx) {
+  if (ctx->ev_used == ctx->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return (size_t)-1;
+    ctx->ev_pool.push_back(e);
+  }
+  size_t id = ctx->ev_used++;
+  cudaEventRecord(ctx->ev_pool[id], ctx->stream);
+  return id;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdf_ContextCreate(FdfContext **out, int device) {
+  FdfContext *ctx = nullptr;
+  if (!out) return FDF_ERR_ARG_NULL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return FDF_ERR_GPU;
+  if (device < 0 || device >= ndev) return FDF_ERR_ARG_OUTOFRANGE;
+  ctx = new FdfContext();
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->cnt, sizeof(DevCounters));
+  if (e == cudaSuccess) e = cudaMemset(ctx->cnt, 0, sizeof(DevCounters));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->bbox, 6 * sizeof(double));
+  if (e != cudaSuccess) {
+    fdf_ContextDestroy(ctx);
+    return FDF_ERR_GPU;
+  }
+  *out = ctx;
+  return FDF_SUCCESS;
+}
+
+int fdf_ContextDestroy(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner); cfree(ctx->bbox);
+  cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk);
+  cfree(ctx->swarm_mem); cfree(ctx->keyval_mem); cfree(ctx->radix_mem);
+  cfree(ctx->cell_start); cfree(ctx->cnt); cfree(ctx->staging);
+  for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const double *coor) {
+  if (!ctx || !coor) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_SetGrid: null argument");
+  if (IM <= 0 || JM <= 0 || KM <= 0)   // grid.c:41-44
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetGrid: grid dimensions (IM, JM, KM) must be positive");
+  long long Nc = IM * JM * KM;
+  long long Nn = (IM + 1) * (JM + 1) * (KM + 1);
+  if (Nc >= 0x7fffffffLL || Nn >= 0x7fffffffLL)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetGrid: more than 2^31-1 cells or nodes");
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaStreamSynchronize(ctx->stream));
+  cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner);
+  cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk); cfree(ctx->cell_start);
+  GridDims g{(int)IM, (int)JM, (int)KM, Nc, Nn};
+  ctx->g = g;
+  long long nfi = (IM + 1) * JM * KM, nfj = IM * (JM + 1) * KM, nfk = IM * JM * (KM + 1);
+  CU(cudaMalloc((void **)&ctx->coor, 24ull * Nn));
+  CU(cudaMalloc((void **)&ctx->planes, 8ull * FDF_ROW * Nc));
+  CU(cudaMalloc((void **)&ctx->ucat, 24ull * Nc));
+  CU(cudaMalloc((void **)&ctx->corner, 24ull * Nn));
+  CU(cudaMalloc((void **)&ctx->count, 8ull * Nn));
+  CU(cudaMalloc((void **)&ctx->avg, 8ull * Nn));
+  CU(cudaMalloc((void **)&ctx->fi, 8ull * nfi));
+  CU(cudaMalloc((void **)&ctx->fj, 8ull * nfj));
+  CU(cudaMalloc((void **)&ctx->fk, 8ull * nfk));
+  CU(cudaMalloc((void **)&ctx->cell_start, 4ull * (Nc + 1)));
+  CU(cudaMemsetAsync(ctx->ucat, 0, 24ull * Nc, ctx->stream));
+  CU(cudaMemsetAsync(ctx->corner, 0, 24ull * Nn, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->coor, coor, 24ull * Nn, cudaMemcpyHostToDevice, ctx->stream));
+  unsigned int *err = nullptr;
+  launch_build_planes(ctx->coor, g, ctx->planes, err, ctx->stream);
+  CHECK_LAUNCH();
+  double init[6] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308,
+                    -1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};
+  CU(cudaMemcpyAsync(ctx->bbox, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+  launch_bbox(ctx->coor, Nn, ctx->bbox, ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 2;
+  double bb[6];
+  CU(cudaMemcpyAsync(bb, ctx->bbox, sizeof(bb), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < 3; ++c) { bb[c] = bb[c] - FDF_BBOX_TOL; bb[3 + c] = bb[3 + c] + FDF_BBOX_TOL; }
+  memcpy(ctx->bbox_h, bb, sizeof(bb));
+  CU(cudaMemcpy(ctx->bbox, bb, sizeof(bb), cudaMemcpyHostToDevice));
+  ctx->sentinel = (unsigned int)Nc;
+  ctx->key_bits = bits_for((unsigned long long)Nc);
+  ctx->has_grid = true;
+  ctx->has_ucat = false;
+  ctx->swarm_set = false;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized) {
+  if (!ctx || !ucat) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_SetUcat: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_SetUcat: call fdf_SetGrid first");
+  const GridDims &g = ctx->g;
+  // Host-side transpose to the device SoA layout [3][Nc].
+  std::vector<double> soa(3 * (size_t)g.Nc);
+  const long long mx = node_sized ? g.IM + 1 : g.IM, my = node_sized ? g.JM + 1 : g.JM;
+  for (long long k = 0; k < g.KM; ++k)
+    for (long long j = 0; j < g.JM; ++j)
+      for (long long i = 0; i < g.IM; ++i) {
+        long long c = (k * g.JM + j) * g.IM + i;
+        const double *v = ucat + 3 * ((k * my + j) * mx + i);
+        soa[c] = v[0]; soa[g.Nc + c] = v[1]; soa[2 * g.Nc + c] = v[2];
+      }
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemcpyAsync(ctx->ucat, soa.data(), 24ull * g.Nc, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->has_ucat = true;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetTimeStep(FdfContext *ctx, double dt) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  ctx->dt = dt;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetParticleVolume(FdfContext *ctx, double volume) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  ctx->volume = volume;
+  return FDF_SUCCESS;
+}
+
+int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  // The sort's scan of per-tile digit counts handles up to 2^17 tiles of 4096 keys.
+  if (capacity < 0 || capacity > FDF_MAX_PARTICLES)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_ReserveParticles: capacity out of range (max 512M)");
+  if (capacity <= ctx->cap && ctx->swarm_mem) return FDF_SUCCESS;
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaStreamSynchronize(ctx->stream));
+  cfree(ctx->swarm_mem); cfree(ctx->keyval_mem); cfree(ctx->radix_mem); cfree(ctx->staging);
+  int cap = (int)(capacity < 256 ? 256 : capacity);   // never zero: the sort always has scratch
+  size_t per = swarm_bytes_per_buf(cap);
+  CU(cudaMalloc(&ctx->swarm_mem, 2 * per));
+  carve_swarm((char *)ctx->swarm_mem, cap, ctx->buf[0]);
+  carve_swarm((char *)ctx->swarm_mem + per, cap, ctx->buf[1]);
+  size_t kv = (4ull * cap + 255) / 256 * 256;
+  CU(cudaMalloc(&ctx->keyval_mem, 2 * kv));
+  ctx->keys = (unsigned int *)ctx->keyval_mem;
+  ctx->vals = (unsigned int *)((char *)ctx->keyval_mem + kv);
+  CU(cudaMalloc(&ctx->radix_mem, radix_scratch_bytes(cap)));
+  radix_scratch_carve(ctx->radix_mem, cap, &ctx->rs);
+  ctx->staging_bytes = (size_t)cap * 120 + 1024;
+  CU(cudaMalloc(&ctx->staging, ctx->staging_bytes));
+  ctx->cap = cap;
+  ctx->swarm_set = false;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity, const double *weight,
+                 const double *P, const int64_t *cell_id, const int64_t *pid, const int64_t *status) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (n > 0 && (!position || !velocity || !weight || !P || !cell_id || !pid || !status))
+    return fail(ctx, FDF_ERR_ARG_NULL, "fdf_SetSwarm: null field pointer");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_SetSwarm: call fdf_SetGrid first");
+  if (n < 0) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetSwarm: negative particle count");
+  if (n > ctx->cap || !ctx->swarm_mem) {
+    int r = fdf_ReserveParticles(ctx, n);
+    if (r) return r;
+  }
+  CU(cudaSetDevice(ctx->device));
+  char *st = (char *)ctx->staging;
+  double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
+  long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
+  if (n > 0) {
+    CU(cudaMemcpyAsync(d_pos, position, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d_vel, velocity, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d_wgt, weight, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d_P, P, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d_cell, cell_id, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d_pid, pid, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaMemcpyAsync(d_st, status, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->cur = 0;
+    launch_swarm_from_aos(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
+    CHECK_LAUNCH();
+    ctx->launches += 1;
+  }
+  DevCounters c{};
+  c.n = (int)n;
+  c.n_sorted = (int)n;
+  CU(cudaMemcpyAsync(ctx->cnt, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->cur = 0;
+  ctx->swarm_set = true;
+  return FDF_SUCCESS;
+}
+
+int fdf_GetSwarmSize(FdfContext *ctx, int64_t *n) {
+  if (!ctx || !n) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetSwarmSize: null argument");
+  CU(cudaSetDevice(ctx->device));
+  int v = 0;
+  CU(cudaMemcpyAsync(&v, &ctx->cnt->n_sorted, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  *n = v;
+  return FDF_SUCCESS;
+}
+
+int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *position, double *velocity, double *weight,
+                 double *P, int64_t *cell_id, int64_t *pid, int64_t *status) {
+  if (!ctx || !n_out) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetSwarm: null argument");
+  int64_t n = 0;
+  int r = fdf_GetSwarmSize(ctx, &n);
+  if (r) return r;
+  *n_out = n;
+  if (n > n_max) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_GetSwarm: output arrays smaller than the swarm");
+  if (n == 0) return FDF_SUCCESS;
+  if (!position || !velocity || !weight || !P || !cell_id || !pid || !status)
+    return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetSwarm: null field pointer");
+  char *st = (char *)ctx->staging;
+  double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
+  long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
+  launch_swarm_to_aos(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
+                      ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  CU(cudaMemcpyAsync(position, d_pos, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(velocity, d_vel, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(weight, d_wgt, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(P, d_P, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(cell_id, d_cell, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(pid, d_pid, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(status, d_st, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FDF_SUCCESS;
+}
+
+int fdf_GetScatteredFields(FdfContext *ctx, double *count, double *P_avg) {
+  if (!ctx || !count || !P_avg) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetScatteredFields: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetScatteredFields: no grid");
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemcpyAsync(count, ctx->count, 8ull * ctx->g.Nn, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(P_avg, ctx->avg, 8ull * ctx->g.Nn, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FDF_SUCCESS;
+}
+
+int fdf_GetCornerField(FdfContext *ctx, double *corner) {
+  if (!ctx || !corner) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetCornerField: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetCornerField: no grid");
+  CU(cudaSetDevice(ctx->device));
+  std::vector<double> soa(3 * (size_t)ctx->g.Nn);
+  CU(cudaMemcpyAsync(soa.data(), ctx->corner, 24ull * ctx->g.Nn, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  const long long Nn = ctx->g.Nn;
+  for (long long q = 0; q < Nn; ++q) {
+    corner[3 * q] = soa[q]; corner[3 * q + 1] = soa[Nn + q]; corner[3 * q + 2] = soa[2 * Nn + q];
+  }
+  return FDF_SUCCESS;
+}
+
+int fdf_GetFaceDeposits(FdfContext *ctx, double *fi, double *fj, double *fk) {
+  if (!ctx || !fi || !fj || !fk) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetFaceDeposits: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetFaceDeposits: no grid");
+  const GridDims &g = ctx->g;
+  long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM, nfk = (long long)g.IM * g.JM * (g.KM + 1LL);
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemcpyAsync(fi, ctx->fi, 8ull * nfi, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(fj, ctx->fj, 8ull * nfj, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(fk, ctx->fk, 8ull * nfk, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FDF_SUCCESS;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The shared pipeline of the initial setup (advect=0, drop=0) and a step (1, 1).
+int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no grid: call fdf_SetGrid first");
+  if (!ctx->has_ucat) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no ucat: call fdf_SetUcat first");
+  if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
+  CU(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const GridDims &g = ctx->g;
+  int n_start = 0;
+  if (info) {
+    CU(cudaMemcpyAsync(&n_start, &ctx->cnt->n_sorted, sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
+  // zero the per-step counters; the error word stays set until the swarm is replaced
+  CU(cudaMemsetAsync(ctx->cnt, 0, offsetof(DevCounters, err), s));
+  const bool prof = ctx->profiling;
+  size_t e0 = prof ? record_event(ctx) : 0;
+  launch_center_to_corner(ctx->ucat, g, ctx->corner, s);
+  size_t e1 = prof ? record_event(ctx) : 0;
+  SwarmBuf &src = ctx->buf[ctx->cur];
+  SwarmBuf &dst = ctx->buf[1 - ctx->cur];
+  launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys, ctx->vals,
+                ctx->sentinel, s);
+  size_t e2 = prof ? record_event(ctx) : 0;
+  radix_sort_pairs(&ctx->keys, &ctx->vals, &ctx->cnt->n_sorted, ctx->key_bits, ctx->rs, s);
+  size_t e3 = prof ? record_event(ctx) : 0;
+  launch_cell_bounds(ctx->keys, ctx->cap, ctx->cnt, ctx->sentinel, ctx->cell_start, s);
+  launch_update_counts(ctx->cnt, ctx->cell_start, ctx->sentinel, drop, s);
+  size_t e4 = prof ? record_event(ctx) : 0;
+  launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->keys, ctx->vals, ctx->sentinel, ctx->cnt, s);
+  size_t e5 = prof ? record_event(ctx) : 0;
+  launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, s);
+  size_t e6 = prof ? record_event(ctx) : 0;
+  if (prof) {
+    size_t ids[7] = {e0, e1, e2, e3, e4, e5, e6};
+    for (int st = 0; st < NUM_STAGES; ++st) ctx->ev_spans.push_back({st, {ids[st], ids[st + 1]}});
+  }
+  CHECK_LAUNCH();
+  ctx->cur = 1 - ctx->cur;
+  int passes = (ctx->key_bits + 7) / 8;
+  ctx->launches += 2 + passes * 5 + 4;
+  if (info) {
+    DevCounters c{};
+    CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    info->n_start = n_start;
+    info->n_end = c.n_sorted;
+    info->removed_lost = (int64_t)c.removed_lost;
+    info->removed_oob = (int64_t)c.removed_oob;
+    info->walk_evals = (int64_t)c.evals;
+    if (c.err & ERRBIT_DEGENERATE)
+      return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
+  }
+  return FDF_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  FdfStepInfo local{};
+  return run_pipeline(ctx, 0, 0, info ? info : &local);
+}
+
+int fdf_AdvanceStep(FdfContext *ctx, FdfStepInfo *info) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  return run_pipeline(ctx, 1, 1, info);
+}
+
+int fdf_AdvanceSteps(FdfContext *ctx, int nsteps) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  for (int q = 0; q < nsteps; ++q) {
+    int r = run_pipeline(ctx, 1, 1, nullptr);
+    if (r) return r;
+  }
+  return FDF_SUCCESS;
+}
+
+int fdf_Synchronize(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaStreamSynchronize(ctx->stream));
+  unsigned int err = 0;
+  CU(cudaMemcpy(&err, &ctx->cnt->err, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err & ERRBIT_DEGENERATE) return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
+  return FDF_SUCCESS;
+}
+
+void *fdf_GetStream(FdfContext *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+const char *fdf_GetLastError(FdfContext *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int64_t fdf_GetLaunchCount(FdfContext *ctx) { return ctx ? ctx->launches : 0; }
+
+int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals) {
+  if (!ctx || !particle_steps || !walk_evals) return FDF_ERR_ARG_NULL;
+  CU(cudaSetDevice(ctx->device));
+  DevCounters c{};
+  CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  *particle_steps = (int64_t)c.psteps_total;
+  *walk_evals = (int64_t)c.evals_total;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetProfiling(FdfContext *ctx, int enable) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->profiling = enable != 0;
+  ctx->ev_used = 0;
+  ctx->ev_spans.clear();
+  return FDF_SUCCESS;
+}
+
+int fdf_GetStageTimes(FdfContext *ctx, double *ms_total, int64_t *launches, int nstages) {
+  if (!ctx || !ms_total || !launches) return FDF_ERR_ARG_NULL;
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaStreamSynchronize(ctx->stream));
+  for (int q = 0; q < nstages; ++q) { ms_total[q] = 0.0; launches[q] = 0; }
+  for (auto &sp : ctx->ev_spans) {
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, ctx->ev_pool[sp.second.first], ctx->ev_pool[sp.second.second]));
+    if (sp.first < nstages) { ms_total[sp.first] += ms; launches[sp.first] += 1; }
+  }
+  return FDF_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+// fdf_walk.cu -- fused advect + walking-search locate, one thread per particle.
+//
+// Restates, per particle, UpdateParticlePosition (ParticleMotion.c:19-29) and
+// LocateParticleOrFindMigrationTarget_TEST (walkingsearch.c:1094-1242) with
+// EvaluateParticlePosition (:811-859), DeterminePointPosition (:407-462),
+// UpdateCellIndicesBasedOnDistancesTEST (:882-959) and UpdateParticleWeights
+// (ParticleSwarm.c:1010-1047).  The per-cell plane table holds every
+// particle-independent value of ComputeSignedDistanceToPlane, computed with the
+// reference's own operation order, so each signed distance here is the
+// reference's bit for bit: d = (fc - p) . n, then |d| < thr -> 0.
+//
+// The stuck-cell tie-breaker (walkingsearch.c:1149-1185) cannot fire on one
+// rank: an evaluation either concludes (position >= 0) or reports some d < 0,
+// and UpdateCellIndices then changes at least one index, so the same cell is
+// never visited twice in a row.  It is therefore not restated here.
+//
+// Cycle cut-off.  The next cell of the walk is a function of (cell, position)
+// only, so once the walk returns to a cell it has already evaluated without
+// concluding, it repeats that cycle until MAX_TRAVERSAL and the particle is
+// LOST.  This happens for points in the thin gap between a cell's FRONT plane
+// and the next cell's BACK plane on curved grids (the two planes are built from
+// different corner vertices, walkingsearch.c:303-325).  The walk here detects
+// the revisit (Brent's method: compare with the cell saved at step 2^m) and
+// concludes LOST at once; the outcome, cell (-1,-1,-1), and the unchanged
+// weights are the reference's, and the evaluation count reported for parity is
+// the reference's (MAX_TRAVERSAL).
+#include "fdf_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
+                                                double dt, int advect, int reset_first, const double *__restrict__ bbox,
+                                                int drop_removed, DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                unsigned int *__restrict__ vals, unsigned int sentinel) {
+  const int n = cnt->n_sorted;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
+  unsigned long long my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0;
+  unsigned int my_err = 0;
+  if (s < n) {
+    double x = b.x[s], y = b.y[s], z = b.z[s];
+    if (advect) {
+      x = add(x, mul(b.u[s], dt));
+      y = add(y, mul(b.v[s], dt));
+      z = add(z, mul(b.w[s], dt));
+      b.x[s] = x; b.y[s] = y; b.z[s] = z;
+    }
+    unsigned char st = b.status[s];
+    if (reset_first && st == ST_ACTIVE_AND_LOCATED) st = ST_NEEDS_LOCATION;
+    int cell = b.cell[s];
+    bool lost = false;
+    if (st != ST_ACTIVE_AND_LOCATED) {
+      // InitializeTraversalParameters: previous cell if it is inside the grid, else (0,0,0)
+      int i = 0, j = 0, k = 0;
+      if (cell >= 0 && (long long)cell < g.Nc) {
+        i = cell % g.IM;
+        int t = cell / g.IM;
+        j = t % g.JM;
+        k = t / g.JM;
+      }
+      int steps = 0, evaluated = 0;
+      bool concluded = false, cycle = false;
+      long long saved = -1;
+      int power = 1, lam = 0;
+      double d[6];
+      while (!concluded && steps < FDF_MAX_TRAVERSAL) {
+        ++steps;
+        if (i < 0 || i >= g.IM || j < 0 || j >= g.JM || k < 0 || k >= g.KM) { lost = true; break; }
+        const long long cur = ((long long)k * g.JM + j) * g.IM + i;
+        if (cur == saved) { cycle = true; lost = true; break; }
+        if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
+        const double2 *row = reinterpret_cast<const double2 *>(planes + cur * FDF_ROW);
+        double2 tf = __ldg(row + 18);   // thr, degenerate flag
+        if (tf.y != 0.0) { my_err |= ERRBIT_DEGENERATE; lost = true; break; }
+        const double thr = tf.x;
+        ++evaluated;
+        bool neg = false, zero = false;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+          double2 p0 = __ldg(row + 3 * f), p1 = __ldg(row + 3 * f + 1), p2 = __ldg(row + 3 * f + 2);
+          // p0 = (fc.x, fc.y), p1 = (fc.z, n.x), p2 = (n.y, n.z)
+          double dd = add(add(mul(sub(p0.x, x), p1.y), mul(sub(p0.y, y), p2.x)), mul(sub(p1.x, z), p2.y));
+          if (fabs(dd) < thr) dd = 0.0;
+          d[f] = dd;
+          neg |= (dd < 0.0);
+          zero |= (dd == 0.0);
+        }
+        if (!neg || zero) {
+          concluded = true;   // position >= 0: inside, or on a face (accepted even if outside another)
+        } else {
+          if (d[F_FRONT] < 0.0) k += 1; else if (d[F_BACK] < 0.0) k -= 1;
+          if (d[F_LEFT] < 0.0) i -= 1; else if (d[F_RIGHT] < 0.0) i += 1;
+          if (d[F_BOTTOM] < 0.0) j -= 1; else if (d[F_TOP] < 0.0) j += 1;
+        }
+      }
+      my_evals = (unsigned long long)(cycle ? FDF_MAX_TRAVERSAL : steps);
+      my_done = (unsigned long long)evaluated;
+      if (lost || !concluded) {
+        lost = true;
+        cell = -1;
+        st = ST_LOST;
+      } else {
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+          if (d[f] <= FDF_INTERP_DIST_TOL) d[f] = FDF_INTERP_DIST_TOL;
+        b.a1[s] = __ddiv_rn(d[F_LEFT], add(d[F_LEFT], d[F_RIGHT]));
+        b.a2[s] = __ddiv_rn(d[F_BOTTOM], add(d[F_BOTTOM], d[F_TOP]));
+        b.a3[s] = __ddiv_rn(d[F_BACK], add(d[F_FRONT], d[F_BACK]));
+        cell = (int)(((long long)k * g.JM + j) * g.IM + i);
+        st = ST_ACTIVE_AND_LOCATED;
+      }
+      b.cell[s] = cell;
+      b.status[s] = st;
+    } else {
+      lost = (cell < 0);
+    }
+    unsigned int key = lost ? sentinel : (unsigned int)cell;
+    if (lost) my_lost_total = 1;
+    if (drop_removed) {
+      // CheckAndRemoveLostParticles, then CheckAndRemoveOutOfBoundsParticles on the rest.
+      if (lost) {
+        my_lost = 1;
+      } else {
+        bool inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
+        if (!inside) { my_oob = 1; key = sentinel; }
+      }
+    }
+    keys[s] = key;
+    vals[s] = (unsigned int)s;
+  }
+  my_lost = warp_sum_u64(my_lost);
+  my_oob = warp_sum_u64(my_oob);
+  my_evals = warp_sum_u64(my_evals);
+  my_done = warp_sum_u64(my_done);
+  my_lost_total = warp_sum_u64(my_lost_total);
+  my_err = __reduce_or_sync(0xffffffffu, my_err);
+  if ((threadIdx.x & 31) == 0) {
+    if (my_lost) atomicAdd(&cnt->removed_lost, my_lost);
+    if (my_oob) atomicAdd(&cnt->removed_oob, my_oob);
+    if (my_evals) atomicAdd(&cnt->evals, my_evals);
+    if (my_done) atomicAdd(&cnt->evals_total, my_done);
+    if (my_lost_total) atomicAdd(&cnt->lost_total, my_lost_total);
+    if (my_err) atomicOr(&cnt->err, my_err);
+  }
+}
+
+}  // namespace
+
+void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
+                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *vals,
+                   unsigned int sentinel, cudaStream_t s) {
+  // advect and drop_removed are both set by the fused step, which also resets statuses first.
+  int reset_first = drop_removed;
+  int th = 256;
+  int blocks = (n_cap + th - 1) / th;
+  if (blocks == 0) blocks = 1;
+  k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, vals,
+                                 sentinel);
+}

@@ -1,0 +1,129 @@
+/*
+ * fdf_gb300.h -- C ABI of the GB300-native particle hot path of PICurv
+ * (VishalKandala/fdf): walking-search cell location, trilinear interpolation of
+ * cell-centred ucat, explicit position update, and particle-to-grid deposits.
+ *
+ * The reference's hot path is a set of C functions on PETSc objects
+ * (UserCtx, DMSwarm, DMDA Vec) returning PetscErrorCode.  This library keeps
+ * their names, argument meaning and error behaviour, with the PETSc objects
+ * replaced by an opaque FdfContext that holds the grid and the swarm
+ * device-resident on one GPU (one rank owning the whole domain: no migration).
+ *
+ *   - Plain pointers and sizes only; host pointers are ordinary (or pinned)
+ *     host memory, laid out exactly as the reference's DMSwarm / DMDA arrays.
+ *   - Every function returns 0 or a PETSc error code (same numbering as
+ *     petscerror.h).  A particle that cannot be located is not an error: its
+ *     status becomes LOST and its cell (-1,-1,-1), as in the reference.
+ *   - PetscInt is 64-bit in the reference's own build (PETSc 3.19.2-64bit), so
+ *     cell indices and statuses cross this boundary as int64_t.
+ *   - Calls on one context are issued on that context's CUDA stream and return
+ *     once the work is queued; functions that return host data synchronise.
+ */
+#ifndef FDF_GB300_H
+#define FDF_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes (PETSc numbering). */
+#define FDF_SUCCESS 0
+#define FDF_ERR_MEM 55
+#define FDF_ERR_SUP 56
+#define FDF_ERR_ARG_WRONG 62
+#define FDF_ERR_ARG_OUTOFRANGE 63
+#define FDF_ERR_ARG_WRONGSTATE 73
+#define FDF_ERR_LIB 76
+#define FDF_ERR_USER 83          /* degenerate cell face met by the walk (walkingsearch.c:147-155) */
+#define FDF_ERR_ARG_NULL 85
+#define FDF_ERR_GPU 97
+
+/* ParticleLocationStatus (common.h:75-124). */
+#define FDF_NEEDS_LOCATION 0
+#define FDF_ACTIVE_AND_LOCATED 1
+#define FDF_MIGRATING_OUT 2
+#define FDF_LOST 3
+#define FDF_UNINITIALIZED 4
+
+/* BoundingBox (common.h:145-148). */
+typedef struct { double min_coords[3]; double max_coords[3]; } FdfBoundingBox;
+
+typedef struct FdfContext FdfContext;
+
+/* Per-step bookkeeping that the reference reports through its removal calls. */
+typedef struct {
+  int64_t n_start;         /* live particles when the step began            */
+  int64_t n_end;           /* live particles after removal                  */
+  int64_t removed_lost;    /* CheckAndRemoveLostParticles count             */
+  int64_t removed_oob;     /* CheckAndRemoveOutOfBoundsParticles count      */
+  int64_t walk_evals;      /* cell evaluations the reference's walk makes (a walk that cycles
+                              until MAX_TRAVERSAL counts 1000; the GPU walk stops at the cycle) */
+} FdfStepInfo;
+
+/* ---- context, grid and fields (replace UserCtx set-up: setup.c:197-290, grid.c:34-160) ---- */
+int fdf_ContextCreate(FdfContext **ctx, int device);
+int fdf_ContextDestroy(FdfContext *ctx);
+/* Node coordinates, DMDA coordinate layout [KM+1][JM+1][IM+1][3] (grid.c:356-383).
+ * Builds the per-cell face-plane table and the bounding box (grid.c:762-883). */
+int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const double *coor);
+/* Cell-centred Cartesian velocity.  node_sized=1: the reference's DMDA layout
+ * [KM+1][JM+1][IM+1][3] with cell (i,j,k) at [k][j][i]; node_sized=0: [KM][JM][IM][3]. */
+int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized);
+int fdf_SetTimeStep(FdfContext *ctx, double dt);                 /* user->dt            */
+int fdf_SetParticleVolume(FdfContext *ctx, double volume);       /* face deposit V_p    */
+
+/* ---- swarm transfer (DMSwarm fields, ParticleSwarm.c:64-96, [n][bs] layout) ---- */
+int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity);
+int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity,
+                 const double *weight, const double *P, const int64_t *cell_id, const int64_t *pid,
+                 const int64_t *status);
+int fdf_GetSwarmSize(FdfContext *ctx, int64_t *n);
+int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n, double *position, double *velocity,
+                 double *weight, double *P, int64_t *cell_id, int64_t *pid, int64_t *status);
+
+/* ---- Eulerian outputs ---- */
+/* ParticleCount and the P average, node-sized [KM+1][JM+1][IM+1] (interpolation.c:2063-2116). */
+int fdf_GetScatteredFields(FdfContext *ctx, double *count, double *P_avg);
+/* Corner (node) velocity of the last interpolation, [KM+1][JM+1][IM+1][3]. */
+int fdf_GetCornerField(FdfContext *ctx, double *corner);
+/* Face volume deposits: fi [KM][JM][IM+1], fj [KM][JM+1][IM], fk [KM+1][JM][IM].
+ * No counterpart in the reference (its only deposit is the cell average of P):
+ * a particle of volume V in cell (i,j,k) with weights (a1,a2,a3) gives (1-a)V/3
+ * to the lower and aV/3 to the upper face of each logical direction. */
+int fdf_GetFaceDeposits(FdfContext *ctx, double *fi, double *fj, double *fk);
+
+/* ---- the hot path ---- */
+/* PerformInitialSetup_TEST (simulation.c:129-175): locate every particle, interpolate,
+ * scatter and deposit.  LOST particles are kept (the reference removes them in step 1). */
+int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info);
+/* One step of AdvanceSimulation_TEST (simulation.c:240-297): ResetAllParticleStatuses,
+ * UpdateAllParticlePositions, LocateAllParticlesInGrid_TEST, CheckAndRemoveLostParticles,
+ * CheckAndRemoveOutOfBoundsParticles, InterpolateAllFieldsToSwarm,
+ * ScatterAllParticleFieldsToEulerFields, plus the face deposit; the particles are
+ * re-sorted by cell.  info may be NULL (then nothing is read back and the call does
+ * not synchronise). */
+int fdf_AdvanceStep(FdfContext *ctx, FdfStepInfo *info);
+int fdf_AdvanceSteps(FdfContext *ctx, int nsteps);
+
+/* ---- utilities ---- */
+int fdf_Synchronize(FdfContext *ctx);
+/* The context's cudaStream_t, for callers that time or order work around it. */
+void *fdf_GetStream(FdfContext *ctx);
+const char *fdf_GetLastError(FdfContext *ctx);
+/* Number of kernel launches the library has issued on this context. */
+int64_t fdf_GetLaunchCount(FdfContext *ctx);
+/* Stage timing with CUDA events on the context stream (enable resets the record).
+ * Stages: 0 center->corner, 1 advect+locate, 2 sort by cell, 3 cell bounds,
+ * 4 gather+interpolate, 5 deposits.  ms_total[s] sums the stage over all pipeline
+ * runs since enabling; launches[s] counts those runs. */
+int fdf_SetProfiling(FdfContext *ctx, int enable);
+/* Running totals since fdf_SetSwarm: particles advanced (sum over steps of the live
+ * particles at step start) and walking-search cell evaluations actually made. */
+int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals);
+int fdf_GetStageTimes(FdfContext *ctx, double *ms_total, int64_t *launches, int nstages);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
