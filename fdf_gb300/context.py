@@ -215,14 +215,14 @@ class PicContext:
     def launches(self) -> int:
         return int(self.lib.fdf_GetLaunchCount(self.h))
 
-    STAGES = ("center_to_corner", "advect_locate", "sort_by_cell", "cell_bounds", "gather_interpolate",
+    STAGES = ("center_to_corner", "advect_locate", "sort_by_cell", "wait_corner", "gather_interpolate",
               "deposit")
 
-    def counters(self) -> tuple[int, int]:
-        """(particle-steps advanced, walk evaluations) since the swarm was set."""
-        a, b = ctypes.c_int64(), ctypes.c_int64()
-        self._check(self.lib.fdf_GetCounters(self.h, ctypes.byref(a), ctypes.byref(b)))
-        return a.value, b.value
+    def counters(self) -> tuple[int, int, int]:
+        """(particle-steps advanced, walk evaluations made, corner nodes computed) since the swarm was set."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.fdf_GetCounters(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
 
     def set_profiling(self, on: bool):
         self._check(self.lib.fdf_SetProfiling(self.h, 1 if on else 0))

@@ -2,9 +2,12 @@
 // the step pipeline on the context's stream.
 //
 // Step pipeline (no host round trip):
-//   center->corner (ucat -> node field)
-//   locate  (advect, walk from the previous cell, weights; removed particles get key Nc)
-//   radix sort by cell key (stable)   ->  cell_start[Nc+1] boundary fill
+//   locate  (advect, walk from the previous cell, weights; histogram of the new cells;
+//            removed particles get key Nc and no slot)
+//   scan of the histogram -> cell_start[Nc+2]
+//   [side stream] center->corner for nodes next to occupied cells (FP64-bound, runs
+//                 concurrently with the integer-bound slot assignment)
+//   slot assignment (counting sort) + per-cell ordering by PID
 //   gather + interpolate into the alternate buffer (sorted order)
 //   deposit (cell count / P average, face volumes) from the sorted segments
 #include "fdf_internal.cuh"
@@ -17,8 +20,9 @@
 
 struct FdfContext {
   int device = 0;
-  cudaStream_t stream = nullptr;
-  GridDims g{0, 0, 0, 0, 0};
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t ev_scan = nullptr, ev_corner = nullptr;
+  GridDims g{};
   bool has_grid = false, has_ucat = false;
   double *coor = nullptr, *planes = nullptr, *ucat = nullptr, *corner = nullptr, *bbox = nullptr;
   double *count = nullptr, *avg = nullptr, *fi = nullptr, *fj = nullptr, *fk = nullptr;
@@ -28,16 +32,14 @@ struct FdfContext {
   SwarmBuf buf[2];
   int cur = 0;
   void *swarm_mem = nullptr;
-  unsigned int *keys = nullptr, *vals = nullptr;   // point into keyval_mem or radix_mem (swapped by the sort)
-  void *keyval_mem = nullptr;
-  void *radix_mem = nullptr;
-  RadixScratch rs{};
-  int *cell_start = nullptr;
+  unsigned int *keys = nullptr, *perm = nullptr;   // [cap]: cell key per slot, sorted slot -> previous slot
+  unsigned int *cell_start = nullptr;              // [Nc+2]: histogram, then its exclusive scan
+  unsigned int *cursor = nullptr;                  // [Nc+1]: per-cell slot cursors of the counting sort
+  unsigned int *scan_sums = nullptr;
   DevCounters *cnt = nullptr;
   void *staging = nullptr;
   size_t staging_bytes = 0;
   unsigned int sentinel = 0;
-  int key_bits = 1;
   bool swarm_set = false;
   long long launches = 0;
   // stage timing: events recorded on the context stream between pipeline stages
@@ -96,24 +98,19 @@ void carve_swarm(char *p, int cap, SwarmBuf &b) {
 
 constexpr long long FDF_MAX_PARTICLES = 512LL * 1024 * 1024;
 
-int bits_for(unsigned long long v) {
-  int b = 1;
-  while (b < 32 && (1ull << b) <= v) ++b;
-  return b;
-}
 
 // Stage ids reported by fdf_GetStageTimes.
-enum { STAGE_CORNER = 0, STAGE_LOCATE = 1, STAGE_SORT = 2, STAGE_BOUNDS = 3, STAGE_GATHER_INTERP = 4,
+enum { STAGE_CORNER = 0, STAGE_LOCATE = 1, STAGE_SORT = 2, STAGE_WAIT = 3, STAGE_GATHER_INTERP = 4,
        STAGE_DEPOSIT = 5, NUM_STAGES = 6 };
 
-size_t record_event(FdfContext *ctx) {
+size_t record_event(FdfContext *ctx, cudaStream_t stream) {
   if (ctx->ev_used == ctx->ev_pool.size()) {
     cudaEvent_t e;
     if (cudaEventCreate(&e) != cudaSuccess) return (size_t)-1;
     ctx->ev_pool.push_back(e);
   }
   size_t id = ctx->ev_used++;
-  cudaEventRecord(ctx->ev_pool[id], ctx->stream);
+  cudaEventRecord(ctx->ev_pool[id], stream);
   return id;
 }
 
@@ -131,6 +128,9 @@ int fdf_ContextCreate(FdfContext **out, int device) {
   ctx->device = device;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_scan, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_corner, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->cnt, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMemset(ctx->cnt, 0, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->bbox, 6 * sizeof(double));
@@ -148,9 +148,13 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner); cfree(ctx->bbox);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk);
-  cfree(ctx->swarm_mem); cfree(ctx->keyval_mem); cfree(ctx->radix_mem);
-  cfree(ctx->cell_start); cfree(ctx->cnt); cfree(ctx->staging);
+  if (ctx->side) cudaStreamSynchronize(ctx->side);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
+  cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->ev_scan) cudaEventDestroy(ctx->ev_scan);
+  if (ctx->ev_corner) cudaEventDestroy(ctx->ev_corner);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return FDF_SUCCESS;
@@ -162,13 +166,16 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
     return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetGrid: grid dimensions (IM, JM, KM) must be positive");
   long long Nc = IM * JM * KM;
   long long Nn = (IM + 1) * (JM + 1) * (KM + 1);
-  if (Nc >= 0x7fffffffLL || Nn >= 0x7fffffffLL)
-    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetGrid: more than 2^31-1 cells or nodes");
+  if (Nc + 2 > scan_max_count() || Nn >= 0x7fffffffLL)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetGrid: too many cells or nodes (max 134M cells)");
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk); cfree(ctx->cell_start);
-  GridDims g{(int)IM, (int)JM, (int)KM, Nc, Nn};
+  cfree(ctx->cursor); cfree(ctx->scan_sums);
+  GridDims g{};
+  g.IM = (int)IM; g.JM = (int)JM; g.KM = (int)KM; g.Nc = Nc; g.Nn = Nn;
+  g.fIM.init((unsigned)IM); g.fJM.init((unsigned)JM); g.fMX.init((unsigned)(IM + 1)); g.fMY.init((unsigned)(JM + 1));
   ctx->g = g;
   long long nfi = (IM + 1) * JM * KM, nfj = IM * (JM + 1) * KM, nfk = IM * JM * (KM + 1);
   CU(cudaMalloc((void **)&ctx->coor, 24ull * Nn));
@@ -180,27 +187,32 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   CU(cudaMalloc((void **)&ctx->fi, 8ull * nfi));
   CU(cudaMalloc((void **)&ctx->fj, 8ull * nfj));
   CU(cudaMalloc((void **)&ctx->fk, 8ull * nfk));
-  CU(cudaMalloc((void **)&ctx->cell_start, 4ull * (Nc + 1)));
+  CU(cudaMalloc((void **)&ctx->cell_start, 4ull * (Nc + 2)));
+  CU(cudaMalloc((void **)&ctx->cursor, 4ull * (Nc + 1)));
+  CU(cudaMalloc((void **)&ctx->scan_sums, 4ull * scan_scratch_words(Nc + 2)));
+  CU(cudaMemsetAsync(ctx->cell_start, 0, 4ull * (Nc + 2), ctx->stream));
   CU(cudaMemsetAsync(ctx->ucat, 0, 24ull * Nc, ctx->stream));
   CU(cudaMemsetAsync(ctx->corner, 0, 24ull * Nn, ctx->stream));
   CU(cudaMemcpyAsync(ctx->coor, coor, 24ull * Nn, cudaMemcpyHostToDevice, ctx->stream));
   unsigned int *err = nullptr;
   launch_build_planes(ctx->coor, g, ctx->planes, err, ctx->stream);
   CHECK_LAUNCH();
-  double init[6] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308,
-                    -1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};
-  CU(cudaMemcpyAsync(ctx->bbox, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
-  launch_bbox(ctx->coor, Nn, ctx->bbox, ctx->stream);
-  CHECK_LAUNCH();
-  ctx->launches += 2;
-  double bb[6];
-  CU(cudaMemcpyAsync(bb, ctx->bbox, sizeof(bb), cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->launches += 1;
+  // ComputeLocalBoundingBox (grid.c:762-883) on one rank: min/max over every node,
+  // widened by 1e-6 -- done on the host, which holds the coordinates.
+  double bb[6] = {1.7976931348623157e308, 1.7976931348623157e308, 1.7976931348623157e308,
+                  -1.7976931348623157e308, -1.7976931348623157e308, -1.7976931348623157e308};
+  for (long long q = 0; q < Nn; ++q)
+    for (int c = 0; c < 3; ++c) {
+      double v = coor[3 * q + c];
+      if (v < bb[c]) bb[c] = v;
+      if (v > bb[3 + c]) bb[3 + c] = v;
+    }
   for (int c = 0; c < 3; ++c) { bb[c] = bb[c] - FDF_BBOX_TOL; bb[3 + c] = bb[3 + c] + FDF_BBOX_TOL; }
   memcpy(ctx->bbox_h, bb, sizeof(bb));
-  CU(cudaMemcpy(ctx->bbox, bb, sizeof(bb), cudaMemcpyHostToDevice));
+  CU(cudaMemcpyAsync(ctx->bbox, bb, sizeof(bb), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
   ctx->sentinel = (unsigned int)Nc;
-  ctx->key_bits = bits_for((unsigned long long)Nc);
   ctx->has_grid = true;
   ctx->has_ucat = false;
   ctx->swarm_set = false;
@@ -248,18 +260,14 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   if (capacity <= ctx->cap && ctx->swarm_mem) return FDF_SUCCESS;
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
-  cfree(ctx->swarm_mem); cfree(ctx->keyval_mem); cfree(ctx->radix_mem); cfree(ctx->staging);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->staging);
   int cap = (int)(capacity < 256 ? 256 : capacity);   // never zero: the sort always has scratch
   size_t per = swarm_bytes_per_buf(cap);
   CU(cudaMalloc(&ctx->swarm_mem, 2 * per));
   carve_swarm((char *)ctx->swarm_mem, cap, ctx->buf[0]);
   carve_swarm((char *)ctx->swarm_mem + per, cap, ctx->buf[1]);
-  size_t kv = (4ull * cap + 255) / 256 * 256;
-  CU(cudaMalloc(&ctx->keyval_mem, 2 * kv));
-  ctx->keys = (unsigned int *)ctx->keyval_mem;
-  ctx->vals = (unsigned int *)((char *)ctx->keyval_mem + kv);
-  CU(cudaMalloc(&ctx->radix_mem, radix_scratch_bytes(cap)));
-  radix_scratch_carve(ctx->radix_mem, cap, &ctx->rs);
+  CU(cudaMalloc((void **)&ctx->keys, 4ull * cap));
+  CU(cudaMalloc((void **)&ctx->perm, 4ull * cap));
   ctx->staging_bytes = (size_t)cap * 120 + 1024;
   CU(cudaMalloc(&ctx->staging, ctx->staging_bytes));
   ctx->cap = cap;
@@ -357,7 +365,12 @@ int fdf_GetScatteredFields(FdfContext *ctx, double *count, double *P_avg) {
 int fdf_GetCornerField(FdfContext *ctx, double *corner) {
   if (!ctx || !corner) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetCornerField: null argument");
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetCornerField: no grid");
+  if (!ctx->has_ucat) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetCornerField: no ucat");
   CU(cudaSetDevice(ctx->device));
+  // the step computes only the nodes next to occupied cells; the full field is made here
+  launch_center_to_corner(ctx->ucat, ctx->g, ctx->corner, nullptr, nullptr, ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
   std::vector<double> soa(3 * (size_t)ctx->g.Nn);
   CU(cudaMemcpyAsync(soa.data(), ctx->corner, 24ull * ctx->g.Nn, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -399,32 +412,44 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   }
   // zero the per-step counters; the error word stays set until the swarm is replaced
   CU(cudaMemsetAsync(ctx->cnt, 0, offsetof(DevCounters, err), s));
+  CU(cudaMemsetAsync(ctx->cell_start, 0, 4ull * (g.Nc + 2), s));
+  CU(cudaMemsetAsync(ctx->cursor, 0, 4ull * (g.Nc + 1), s));
   const bool prof = ctx->profiling;
-  size_t e0 = prof ? record_event(ctx) : 0;
-  launch_center_to_corner(ctx->ucat, g, ctx->corner, s);
-  size_t e1 = prof ? record_event(ctx) : 0;
   SwarmBuf &src = ctx->buf[ctx->cur];
   SwarmBuf &dst = ctx->buf[1 - ctx->cur];
-  launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys, ctx->vals,
-                ctx->sentinel, s);
-  size_t e2 = prof ? record_event(ctx) : 0;
-  radix_sort_pairs(&ctx->keys, &ctx->vals, &ctx->cnt->n_sorted, ctx->key_bits, ctx->rs, s);
-  size_t e3 = prof ? record_event(ctx) : 0;
-  launch_cell_bounds(ctx->keys, ctx->cap, ctx->cnt, ctx->sentinel, ctx->cell_start, s);
-  launch_update_counts(ctx->cnt, ctx->cell_start, ctx->sentinel, drop, s);
-  size_t e4 = prof ? record_event(ctx) : 0;
-  launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->keys, ctx->vals, ctx->sentinel, ctx->cnt, s);
-  size_t e5 = prof ? record_event(ctx) : 0;
+  size_t e0 = prof ? record_event(ctx, s) : 0;
+  launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys,
+                ctx->cell_start, ctx->sentinel, s);
+  size_t e1 = prof ? record_event(ctx, s) : 0;
+  exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
+  // the corner field needs only cell_start: compute it beside the slot assignment
+  CU(cudaEventRecord(ctx->ev_scan, s));
+  CU(cudaStreamWaitEvent(ctx->side, ctx->ev_scan, 0));
+  size_t c0 = prof ? record_event(ctx, ctx->side) : 0;
+  launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->side);
+  size_t c1 = prof ? record_event(ctx, ctx->side) : 0;
+  CU(cudaEventRecord(ctx->ev_corner, ctx->side));
+  launch_scatter_slots(ctx->keys, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start, ctx->cursor,
+                       ctx->perm, s);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
+  size_t e2 = prof ? record_event(ctx, s) : 0;
+  CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
+  size_t e3 = prof ? record_event(ctx, s) : 0;
+  launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s);
+  size_t e4 = prof ? record_event(ctx, s) : 0;
   launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, s);
-  size_t e6 = prof ? record_event(ctx) : 0;
+  size_t e5 = prof ? record_event(ctx, s) : 0;
   if (prof) {
-    size_t ids[7] = {e0, e1, e2, e3, e4, e5, e6};
-    for (int st = 0; st < NUM_STAGES; ++st) ctx->ev_spans.push_back({st, {ids[st], ids[st + 1]}});
+    ctx->ev_spans.push_back({STAGE_LOCATE, {e0, e1}});
+    ctx->ev_spans.push_back({STAGE_SORT, {e1, e2}});
+    ctx->ev_spans.push_back({STAGE_CORNER, {c0, c1}});
+    ctx->ev_spans.push_back({STAGE_WAIT, {e2, e3}});
+    ctx->ev_spans.push_back({STAGE_GATHER_INTERP, {e3, e4}});
+    ctx->ev_spans.push_back({STAGE_DEPOSIT, {e4, e5}});
   }
   CHECK_LAUNCH();
   ctx->cur = 1 - ctx->cur;
-  int passes = (ctx->key_bits + 7) / 8;
-  ctx->launches += 2 + passes * 5 + 4;
+  ctx->launches += 9;   // locate, 3 scan kernels, corner, slots, order, gather, deposit
   if (info) {
     DevCounters c{};
     CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
@@ -480,15 +505,36 @@ const char *fdf_GetLastError(FdfContext *ctx) { return ctx ? ctx->last_error.c_s
 
 int64_t fdf_GetLaunchCount(FdfContext *ctx) { return ctx ? ctx->launches : 0; }
 
-int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals) {
-  if (!ctx || !particle_steps || !walk_evals) return FDF_ERR_ARG_NULL;
+int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals, int64_t *corner_nodes) {
+  if (!ctx || !particle_steps || !walk_evals || !corner_nodes) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));
   DevCounters c{};
   CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   *particle_steps = (int64_t)c.psteps_total;
   *walk_evals = (int64_t)c.evals_total;
+  *corner_nodes = (int64_t)c.nodes_total;
   return FDF_SUCCESS;
+}
+
+int fdf_SortByCell(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t *perm, uint32_t *cell_start,
+                   void *stream) {
+  if (n > 0 && (!cell_ids || !perm)) return FDF_ERR_ARG_NULL;
+  if (!cell_start) return FDF_ERR_ARG_NULL;
+  if (n < 0 || n > FDF_MAX_PARTICLES || ncells < 1 || ncells + 1 > scan_max_count()) return FDF_ERR_ARG_OUTOFRANGE;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *cursor = nullptr, *sums = nullptr;
+  const size_t nsums = scan_scratch_words(ncells + 1);
+  if (cudaMallocAsync((void **)&cursor, 4ull * ncells, s) != cudaSuccess) return FDF_ERR_MEM;
+  if (cudaMallocAsync((void **)&sums, 4ull * nsums, s) != cudaSuccess) {
+    cudaFreeAsync(cursor, s);
+    return FDF_ERR_MEM;
+  }
+  cell_sort_on_scratch(cell_ids, n, ncells, perm, cell_start, cursor, sums, s);
+  cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(sums, s);
+  cudaFreeAsync(cursor, s);
+  return e == cudaSuccess ? FDF_SUCCESS : FDF_ERR_GPU;
 }
 
 int fdf_SetProfiling(FdfContext *ctx, int enable) {
@@ -505,6 +551,7 @@ int fdf_GetStageTimes(FdfContext *ctx, double *ms_total, int64_t *launches, int 
   if (!ctx || !ms_total || !launches) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
+  CU(cudaStreamSynchronize(ctx->side));
   for (int q = 0; q < nstages; ++q) { ms_total[q] = 0.0; launches[q] = 0; }
   for (auto &sp : ctx->ev_spans) {
     float ms = 0.f;

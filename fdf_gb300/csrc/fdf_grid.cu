@@ -1,19 +1,20 @@
-// fdf_grid.cu -- grid-side kernels: per-cell face-plane table, center->corner
-// averaging of ucat, bounding box.
+// fdf_grid.cu -- grid-side kernels: per-cell face-plane table and center->corner
+// averaging of ucat.
 //
 // All FP64 arithmetic on the parity path uses the _rn intrinsics, which the
 // compiler never contracts into an FMA, so every value is rounded exactly as the
 // reference (compiled without FMA) rounds it.
 #include "fdf_internal.cuh"
+#include "fdf_exact.cuh"
 #include <cfloat>
 
 namespace {
 
 struct V3 { double x, y, z; };
 
-__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+using fdfx::add;
+using fdfx::sub;
+using fdfx::mul;
 
 __device__ __forceinline__ V3 node(const double *coor, GridDims g, long long i, long long j, long long k) {
   const double *q = coor + 3 * ((k * (g.JM + 1) + j) * (long long)(g.IM + 1) + i);
@@ -46,7 +47,8 @@ __global__ void k_build_planes(const double *__restrict__ coor, GridDims g, doub
                                unsigned int *err) {
   long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= g.Nc) return;
-  long long i = c % g.IM, t = c / g.IM, j = t % g.JM, k = t / g.JM;
+  int i, j, k;
+  cell_ijk(g, (unsigned int)c, i, j, k);
   // walkingsearch.c:521-549 vertex numbering
   V3 v[8];
   v[0] = node(coor, g, i, j, k);         v[1] = node(coor, g, i + 1, j, k);
@@ -85,13 +87,39 @@ __global__ void k_build_planes(const double *__restrict__ coor, GridDims g, doub
 }
 
 // InterpolateFieldFromCenterToCorner_Vector_Petsc, interpolation.c:598-679.
-// Each node averages its valid adjacent cells in (dk, dj, di) order; the count is
-// 1, 2, 4 or 8, so sum/count equals sum*(1/count) exactly.
-__global__ void k_center_to_corner(const double *__restrict__ ucat, GridDims g, double *__restrict__ corner) {
+// Each node averages its valid adjacent cells in (dk, dj, di) order.  The count is
+// a product of per-direction counts of 1 or 2, i.e. 1, 2, 4 or 8, so sum/count is
+// exactly sum*(1/count): both are the correctly rounded value of the same real.
+// The running sum starts at 0.0; "0.0 + first" is the first value except that a
+// -0.0 becomes +0.0 (add0).  With cell_start non-null, nodes none of whose
+// adjacent cells holds a particle are skipped: the corner field is an
+// intermediate of the interpolation and only those nodes are ever read.
+__global__ void k_center_to_corner(const double *__restrict__ ucat, GridDims g, double *__restrict__ corner,
+                                   const unsigned int *__restrict__ cell_start, unsigned long long *nodes_done) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= g.Nn) return;
-  const long long mx = g.IM + 1, my = g.JM + 1;
-  long long i = q % mx, t = q / mx, j = t % my, k = t / my;
+  bool work = q < g.Nn;
+  if (cell_start) {
+    // count the nodes this step computes (for the roofline bytes)
+    bool need = false;
+    if (work) {
+      int i0, j0, k0;
+      node_ijk(g, (unsigned int)q, i0, j0, k0);
+      for (int dk = -1; dk <= 0 && !need; ++dk)
+        for (int dj = -1; dj <= 0 && !need; ++dj)
+          for (int di = -1; di <= 0 && !need; ++di) {
+            int ck = k0 + dk, cj = j0 + dj, ci = i0 + di;
+            if (ci < 0 || ci >= g.IM || cj < 0 || cj >= g.JM || ck < 0 || ck >= g.KM) continue;
+            long long c = ((long long)ck * g.JM + cj) * g.IM + ci;
+            need = __ldg(cell_start + c + 1) > __ldg(cell_start + c);
+          }
+    }
+    unsigned int bal = __ballot_sync(0xffffffffu, need);
+    if (nodes_done && (threadIdx.x & 31) == 0 && bal) atomicAdd(nodes_done, (unsigned long long)__popc(bal));
+    if (!need) return;
+  }
+  if (!work) return;
+  int i, j, k;
+  node_ijk(g, (unsigned int)q, i, j, k);
   const double *ux = ucat, *uy = ucat + g.Nc, *uz = ucat + 2 * g.Nc;
   double sx = 0.0, sy = 0.0, sz = 0.0;
   int count = 0;
@@ -108,63 +136,22 @@ __global__ void k_center_to_corner(const double *__restrict__ ucat, GridDims g, 
         long long ci = i + di;
         if (ci < 0 || ci >= g.IM) continue;
         long long c = (ck * g.JM + cj) * g.IM + ci;
-        sx = add(sx, __ldg(ux + c)); sy = add(sy, __ldg(uy + c)); sz = add(sz, __ldg(uz + c));
+        double vx = __ldg(ux + c), vy = __ldg(uy + c), vz = __ldg(uz + c);
+        if (count == 0) {
+          sx = fdfx::add0(vx); sy = fdfx::add0(vy); sz = fdfx::add0(vz);
+        } else {
+          sx = add(sx, vx); sy = add(sy, vy); sz = add(sz, vz);
+        }
         ++count;
       }
     }
   }
   double ox = 0.0, oy = 0.0, oz = 0.0;
   if (count > 0) {
-    double dc = (double)count;
-    ox = __ddiv_rn(sx, dc); oy = __ddiv_rn(sy, dc); oz = __ddiv_rn(sz, dc);
+    const double r = count == 1 ? 1.0 : count == 2 ? 0.5 : count == 4 ? 0.25 : 0.125;
+    ox = mul(sx, r); oy = mul(sy, r); oz = mul(sz, r);
   }
   corner[q] = ox; corner[g.Nn + q] = oy; corner[2 * g.Nn + q] = oz;
-}
-
-__device__ __forceinline__ double atomic_min_d(double *addr, double val) {
-  unsigned long long *a = (unsigned long long *)addr;
-  unsigned long long old = *a, assumed;
-  do {
-    assumed = old;
-    if (__longlong_as_double(assumed) <= val) break;
-    old = atomicCAS(a, assumed, __double_as_longlong(val));
-  } while (assumed != old);
-  return __longlong_as_double(old);
-}
-__device__ __forceinline__ double atomic_max_d(double *addr, double val) {
-  unsigned long long *a = (unsigned long long *)addr;
-  unsigned long long old = *a, assumed;
-  do {
-    assumed = old;
-    if (__longlong_as_double(assumed) >= val) break;
-    old = atomicCAS(a, assumed, __double_as_longlong(val));
-  } while (assumed != old);
-  return __longlong_as_double(old);
-}
-
-// ComputeLocalBoundingBox, grid.c:762-883 (min/max over nodes; the widening by
-// 1e-6 is applied by the host). min/max are order-independent, so atomics are exact.
-__global__ void k_bbox(const double *__restrict__ coor, long long nn, double *bbox6) {
-  double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, mxv[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nn;
-       q += (long long)gridDim.x * blockDim.x) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      double v = coor[3 * q + c];
-      if (v < mn[c]) mn[c] = v;
-      if (v > mxv[c]) mxv[c] = v;
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    for (int o = 16; o > 0; o >>= 1) {
-      double a = __shfl_down_sync(0xffffffffu, mn[c], o);
-      double b = __shfl_down_sync(0xffffffffu, mxv[c], o);
-      if (a < mn[c]) mn[c] = a;
-      if (b > mxv[c]) mxv[c] = b;
-    }
-    if ((threadIdx.x & 31) == 0) { atomic_min_d(&bbox6[c], mn[c]); atomic_max_d(&bbox6[3 + c], mxv[c]); }
-  }
 }
 
 }  // namespace
@@ -175,12 +162,9 @@ void launch_build_planes(const double *coor, GridDims g, double *planes, unsigne
   k_build_planes<<<(unsigned)blocks, th, 0, s>>>(coor, g, planes, err);
 }
 
-void launch_center_to_corner(const double *ucat, GridDims g, double *corner, cudaStream_t s) {
+void launch_center_to_corner(const double *ucat, GridDims g, double *corner, const unsigned int *cell_start,
+                             unsigned long long *nodes_done, cudaStream_t s) {
   int th = 256;
   long long blocks = (g.Nn + th - 1) / th;
-  k_center_to_corner<<<(unsigned)blocks, th, 0, s>>>(ucat, g, corner);
-}
-
-void launch_bbox(const double *coor, long long nn, double *bbox6, cudaStream_t s) {
-  k_bbox<<<152 * 4, 256, 0, s>>>(coor, nn, bbox6);
+  k_center_to_corner<<<(unsigned)blocks, th, 0, s>>>(ucat, g, corner, cell_start, nodes_done);
 }

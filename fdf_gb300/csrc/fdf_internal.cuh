@@ -45,6 +45,7 @@ struct DevCounters {
   int n_sorted;     // particles held in the arrays (live + LOST kept by the initial setup)
   unsigned long long psteps_total;  // sum over steps of the particles at step start (never reset per step)
   unsigned long long evals_total;   // walk evaluations actually made, all pipeline runs (never reset per step)
+  unsigned long long nodes_total;   // corner nodes computed by the steps (never reset per step)
 };
 
 struct SwarmBuf {
@@ -54,40 +55,79 @@ struct SwarmBuf {
   unsigned char *status;
 };
 
+// Division by a fixed divisor d >= 1 for numerators n < 2^31 (cell and node
+// indices): floor(n/d) = (n * m) >> (31 + s) with s = ceil(log2 d) and
+// m = ceil(2^(31+s) / d) < 2^32.  Exact: m*n/2^(31+s) exceeds n/d by less than
+// 2^-s <= 1/d, which cannot carry past the next integer (equality only for
+// d = 2^s, where m is exact).
+struct FastDiv {
+  unsigned int d, m;
+  int sh;
+  __host__ void init(unsigned int div) {
+    d = div;
+    int s = 0;
+    while ((1ull << s) < (unsigned long long)div) ++s;
+    sh = 31 + s;
+    unsigned long long num = 1ull << sh;
+    m = (unsigned int)((num + div - 1) / div);
+  }
+  __device__ __forceinline__ unsigned int div(unsigned int n) const {
+    return (unsigned int)(((unsigned long long)n * m) >> sh);
+  }
+};
+
 struct GridDims {
   int IM, JM, KM;
   long long Nc, Nn;
+  FastDiv fIM, fJM, fMX, fMY;   // by IM, JM (cells) and IM+1, JM+1 (nodes)
 };
+
+// cell id -> (i, j, k)
+__device__ __forceinline__ void cell_ijk(const GridDims &g, unsigned int c, int &i, int &j, int &k) {
+  unsigned int t = g.fIM.div(c);
+  i = (int)(c - t * (unsigned)g.IM);
+  unsigned int kk = g.fJM.div(t);
+  j = (int)(t - kk * (unsigned)g.JM);
+  k = (int)kk;
+}
+// node id -> (i, j, k)
+__device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int &i, int &j, int &k) {
+  unsigned int t = g.fMX.div(q);
+  i = (int)(q - t * (unsigned)(g.IM + 1));
+  unsigned int kk = g.fMY.div(t);
+  j = (int)(t - kk * (unsigned)(g.JM + 1));
+  k = (int)kk;
+}
 
 // ---------------------------------------------------------------- kernels (launchers)
 void launch_build_planes(const double *coor_aos, GridDims g, double *planes, unsigned int *err, cudaStream_t s);
-void launch_center_to_corner(const double *ucat, GridDims g, double *corner, cudaStream_t s);
+// cell_start == nullptr: every node; else only nodes adjacent to an occupied cell.
+void launch_center_to_corner(const double *ucat, GridDims g, double *corner, const unsigned int *cell_start,
+                             unsigned long long *nodes_done, cudaStream_t s);
+// Advect + walk.  Writes the new cell (or -1) and status in place, keys[s] = cell
+// or sentinel (LOST / removed), and histograms the kept keys into count[] (bucket
+// Nc = LOST particles, counted only when keep_lost).
 void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
                    const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys,
-                   unsigned int *vals, unsigned int sentinel, cudaStream_t s);
+                   unsigned int *count, unsigned int sentinel, cudaStream_t s);
+// sorted slot s takes the particle perm[s]; n = cell_start[Nc+1] (read on the device)
 void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g,
-                          const double *corner, const unsigned int *keys, const unsigned int *vals,
-                          unsigned int sentinel, const DevCounters *cnt, cudaStream_t s);
-void launch_update_counts(DevCounters *cnt, const int *cell_start, unsigned int sentinel, int drop_removed,
-                          cudaStream_t s);
-void launch_cell_bounds(const unsigned int *keys, int n_cap, const DevCounters *cnt, unsigned int sentinel,
-                        int *cell_start, cudaStream_t s);
-void launch_deposit(const SwarmBuf &b, GridDims g, const int *cell_start, double volume, double *count,
+                          const double *corner, const unsigned int *perm, const unsigned int *cell_start,
+                          DevCounters *cnt, cudaStream_t s);
+void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,
                     double *avg, double *fi, double *fj, double *fk, cudaStream_t s);
-void launch_bbox(const double *coor_aos, long long nn, double *bbox6, cudaStream_t s);
 
-// Radix sort of (key, value) pairs, stable, ascending, on the low `bits` bits of the key.
-struct RadixScratch {
-  unsigned int *keys_alt, *vals_alt, *hist, *hist_scan_tmp;
-  int cap_items, cap_tiles;
-};
-size_t radix_scratch_bytes(int n_cap);
-void radix_scratch_carve(void *base, int n_cap, RadixScratch *rs);
-// Sorts (*keys, *vals); n is read from *n_dev on the device.  The passes ping-pong
-// with rs.keys_alt/vals_alt: on return *keys/*vals point at the sorted pairs and
-// rs.keys_alt/vals_alt at the other buffers.
-void radix_sort_pairs(unsigned int **keys, unsigned int **vals, const int *n_dev, int bits, RadixScratch &rs,
-                      cudaStream_t s);
+// Counting sort helpers (fdf_sort.cu).
+size_t scan_scratch_words(long long count);
+long long scan_max_count();
+void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums, cudaStream_t s);
+void launch_scatter_slots(const unsigned int *keys, int n_cap, const DevCounters *cnt, unsigned int sentinel,
+                          int keep_lost, const unsigned int *cell_start, unsigned int *cursor, unsigned int *perm,
+                          cudaStream_t s);
+void launch_order_segments(const unsigned int *cell_start, int nseg, const long long *pid, unsigned int *perm,
+                           cudaStream_t s);
+void cell_sort_on_scratch(const int *cell, long long n, long long ncells, unsigned int *perm,
+                          unsigned int *cell_start, unsigned int *cursor, unsigned int *sums, cudaStream_t s);
 
 // AoS <-> SoA marshalling of the DMSwarm fields.
 void launch_swarm_from_aos(const double *pos, const double *vel, const double *wgt, const double *P,

@@ -2,69 +2,79 @@
 // gather, the deterministic particle-to-grid deposits, and the DMSwarm AoS <->
 // device SoA marshalling.
 #include "fdf_internal.cuh"
+#include "fdf_exact.cuh"
 
 namespace {
 
-__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-// PETSc's PetscMin / PetscMax macros: a<b ? a : b and a<b ? b : a.
-__device__ __forceinline__ double pmin(double a, double b) { return (a < b) ? a : b; }
-__device__ __forceinline__ double pmax(double a, double b) { return (a < b) ? b : a; }
+using fdfx::add;
+using fdfx::sub;
+using fdfx::mul;
 
-// Sorted slot s takes the particle from slot vals[s] of the previous order, then
+// Sorted slot s takes the particle from slot perm[s] of the previous order, then
 // interpolates ucat to it: ComputeTrilinearWeights (interpolation.c:839-864) and
 // TrilinearInterpolation_Vector (:957-1042) from the node-averaged field, with
 // the stencil guard of InterpolateEulerFieldToSwarm (:1356-1372).
 __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf dst, GridDims g,
                                                        const double *__restrict__ corner,
-                                                       const unsigned int *__restrict__ keys,
-                                                       const unsigned int *__restrict__ vals, unsigned int sentinel,
-                                                       const DevCounters *cnt) {
-  const int n = cnt->n_sorted;
+                                                       const unsigned int *__restrict__ perm,
+                                                       const unsigned int *__restrict__ cell_start,
+                                                       DevCounters *cnt) {
+  const int n = (int)cell_start[g.Nc + 1];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {   // the new sizes, read by the next step
+    cnt->n = (int)cell_start[g.Nc];
+    cnt->n_sorted = n;
+  }
   if (s >= n) return;
-  const unsigned int key = keys[s];
-  const unsigned int p = vals[s];
+  const unsigned int p = perm[s];
+  const int cell = src.cell[p];
   double a1 = src.a1[p], a2 = src.a2[p], a3 = src.a3[p];
   dst.x[s] = src.x[p]; dst.y[s] = src.y[p]; dst.z[s] = src.z[p];
   dst.a1[s] = a1; dst.a2[s] = a2; dst.a3[s] = a3;
   dst.P[s] = src.P[p];
   dst.pid[s] = src.pid[p];
   double ux = 0.0, uy = 0.0, uz = 0.0;
-  if (key >= sentinel) {
+  if (cell < 0) {
     dst.cell[s] = -1;
     dst.status[s] = ST_LOST;
   } else {
-    dst.cell[s] = (int)key;
+    dst.cell[s] = cell;
     dst.status[s] = ST_ACTIVE_AND_LOCATED;
-    const int i = (int)(key % (unsigned)g.IM);
-    const unsigned int t = key / (unsigned)g.IM;
-    const int j = (int)(t % (unsigned)g.JM), k = (int)(t / (unsigned)g.JM);
-    a1 = pmax(0.0, pmin(1.0, a1));
-    a2 = pmax(0.0, pmin(1.0, a2));
-    a3 = pmax(0.0, pmin(1.0, a3));
+    int i, j, k;
+    cell_ijk(g, (unsigned int)cell, i, j, k);
+    a1 = fdfx::clamp01(a1);
+    a2 = fdfx::clamp01(a2);
+    a3 = fdfx::clamp01(a3);
     const double oa1 = sub(1.0, a1), oa2 = sub(1.0, a2), oa3 = sub(1.0, a3);
+    // w[c] = (x*y)*z as the reference evaluates it; the four (x*y) pair products are shared
+    const double p00 = mul(oa1, oa2), p10 = mul(a1, oa2), p01 = mul(oa1, a2), p11 = mul(a1, a2);
     double w[8];
-    w[0] = mul(mul(oa1, oa2), oa3); w[1] = mul(mul(a1, oa2), oa3);
-    w[2] = mul(mul(oa1, a2), oa3);  w[3] = mul(mul(a1, a2), oa3);
-    w[4] = mul(mul(oa1, oa2), a3);  w[5] = mul(mul(a1, oa2), a3);
-    w[6] = mul(mul(oa1, a2), a3);   w[7] = mul(mul(a1, a2), a3);
+    w[0] = mul(p00, oa3); w[1] = mul(p10, oa3); w[2] = mul(p01, oa3); w[3] = mul(p11, oa3);
+    w[4] = mul(p00, a3);  w[5] = mul(p10, a3);  w[6] = mul(p01, a3);  w[7] = mul(p11, a3);
     const long long mx = g.IM + 1, my = g.JM + 1;
     const long long q0 = ((long long)k * my + j) * mx + i;
     const long long off[8] = {0, 1, mx, mx + 1, mx * my, mx * my + 1, mx * my + mx, mx * my + mx + 1};
     const double *cx = corner, *cy = corner + g.Nn, *cz = corner + 2 * g.Nn;
-    double sw = 0.0, ax = 0.0, ay = 0.0, az = 0.0;
+    // accumulators start at 0.0: the first "0.0 + t" is t except that -0.0 becomes +0.0
+    double ax = fdfx::add0(mul(w[0], __ldg(cx + q0)));
+    double ay = fdfx::add0(mul(w[0], __ldg(cy + q0)));
+    double az = fdfx::add0(mul(w[0], __ldg(cz + q0)));
+    double sw = fdfx::add0(w[0]);
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int c = 1; c < 8; ++c) {
       const long long q = q0 + off[c];
       ax = add(ax, mul(w[c], __ldg(cx + q)));
       ay = add(ay, mul(w[c], __ldg(cy + q)));
       az = add(az, mul(w[c], __ldg(cz + q)));
       sw = add(sw, w[c]);
     }
-    if (sw > 1.0e-14) {
-      ux = __ddiv_rn(ax, sw); uy = __ddiv_rn(ay, sw); uz = __ddiv_rn(az, sw);
+    // sumW > 1e-14 (false for NaN); x / 1.0 == x exactly, so the common sumW == 1 skips the divides
+    if (!fdfx::is_nan(sw) && !fdfx::le_pos(sw, fdfx::ubits(1.0e-14))) {
+      if (fdfx::ubits(sw) == 0x3ff0000000000000ULL) {
+        ux = ax; uy = ay; uz = az;
+      } else {
+        ux = fdfx::div(ax, sw); uy = fdfx::div(ay, sw); uz = fdfx::div(az, sw);
+      }
     }
   }
   dst.u[s] = ux; dst.v[s] = uy; dst.w[s] = uz;
@@ -76,33 +86,37 @@ __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf ds
 // corner is this node: i-face (i,j,k) between cells i-1 and i, and likewise j, k.
 // A face sums its lower cell's particles (weight a) and then its upper cell's
 // (weight 1-a), each in sorted order: a fixed order, so the sum is deterministic.
-__global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const int *__restrict__ cs,
+__global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const unsigned int *__restrict__ cs,
                                                  double third, double *__restrict__ count,
                                                  double *__restrict__ avg, double *__restrict__ fi,
                                                  double *__restrict__ fj, double *__restrict__ fk) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nn) return;
   const int IM = g.IM, JM = g.JM, KM = g.KM;
-  const long long mx = IM + 1, my = JM + 1;
-  const int i = (int)(q % mx);
-  const long long t = q / mx;
-  const int j = (int)(t % my), k = (int)(t / my);
+  int i, j, k;
+  node_ijk(g, (unsigned int)q, i, j, k);
   const bool is_cell = i < IM && j < JM && k < KM;
   const long long c = ((long long)k * JM + j) * IM + i;
   int s0 = 0, s1 = 0;
-  if (is_cell) { s0 = __ldg(cs + c); s1 = __ldg(cs + c + 1); }
+  if (is_cell) { s0 = (int)__ldg(cs + c); s1 = (int)__ldg(cs + c + 1); }
   // AccumulateParticleField + CalculateParticleCountPerCell + NormalizeGridVectorByCount
   {
-    double sum = 0.0, cntv = 0.0;
-    for (int s = s0; s < s1; ++s) { sum = add(sum, __ldg(b.P + s)); cntv = add(cntv, 1.0); }
-    count[q] = cntv;
-    avg[q] = (cntv > 0.5) ? __ddiv_rn(sum, cntv) : 0.0;
+    double sum = 0.0;
+    if (s1 > s0) {
+      sum = fdfx::add0(__ldg(b.P + s0));
+      for (int s = s0 + 1; s < s1; ++s) sum = add(sum, __ldg(b.P + s));
+    }
+    const unsigned int ncell = (unsigned int)(s1 - s0);   // count += 1.0 per particle is exact in FP64
+    count[q] = fdfx::u32_to_double(ncell);
+    double a = 0.0;
+    if (ncell > 0) a = fdfx::div_count(sum, ncell);
+    avg[q] = a;
   }
   if (j < JM && k < KM) {   // i-face (i,j,k), i in [0, IM]
     double acc = 0.0;
     if (i > 0) {
       long long cl = c - 1;
-      int l0 = __ldg(cs + cl), l1 = __ldg(cs + cl + 1);
+      int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
       for (int s = l0; s < l1; ++s) acc = add(acc, mul(__ldg(b.a1 + s), third));
     }
     if (i < IM)
@@ -113,7 +127,7 @@ __global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const i
     double acc = 0.0;
     if (j > 0) {
       long long cl = ((long long)k * JM + (j - 1)) * IM + i;
-      int l0 = __ldg(cs + cl), l1 = __ldg(cs + cl + 1);
+      int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
       for (int s = l0; s < l1; ++s) acc = add(acc, mul(__ldg(b.a2 + s), third));
     }
     if (j < JM)
@@ -124,7 +138,7 @@ __global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const i
     double acc = 0.0;
     if (k > 0) {
       long long cl = ((long long)(k - 1) * JM + j) * IM + i;
-      int l0 = __ldg(cs + cl), l1 = __ldg(cs + cl + 1);
+      int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
       for (int s = l0; s < l1; ++s) acc = add(acc, mul(__ldg(b.a3 + s), third));
     }
     if (k < KM)
@@ -164,8 +178,9 @@ __global__ void k_to_aos(SwarmBuf b, int n, GridDims g, double *__restrict__ pos
   pid[p] = b.pid[p];
   int c = b.cell[p];
   if (c >= 0) {
-    long long i = c % g.IM, t = c / g.IM;
-    cell3[3 * p] = i; cell3[3 * p + 1] = t % g.JM; cell3[3 * p + 2] = t / g.JM;
+    int i, j, k;
+    cell_ijk(g, (unsigned int)c, i, j, k);
+    cell3[3 * p] = i; cell3[3 * p + 1] = j; cell3[3 * p + 2] = k;
   } else {
     cell3[3 * p] = -1; cell3[3 * p + 1] = -1; cell3[3 * p + 2] = -1;
   }
@@ -175,16 +190,16 @@ __global__ void k_to_aos(SwarmBuf b, int n, GridDims g, double *__restrict__ pos
 }  // namespace
 
 void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const double *corner,
-                              const unsigned int *keys, const unsigned int *vals, unsigned int sentinel,
-                              const DevCounters *cnt, cudaStream_t s) {
+                          const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
+                          cudaStream_t s) {
   int th = 256;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
-  k_gather_interp<<<blocks, th, 0, s>>>(src, dst, g, corner, keys, vals, sentinel, cnt);
+  k_gather_interp<<<blocks, th, 0, s>>>(src, dst, g, corner, perm, cell_start, cnt);
 }
 
-void launch_deposit(const SwarmBuf &b, GridDims g, const int *cell_start, double volume, double *count, double *avg,
-                    double *fi, double *fj, double *fk, cudaStream_t s) {
+void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,
+                    double *avg, double *fi, double *fj, double *fk, cudaStream_t s) {
   int th = 256;
   long long blocks = (g.Nn + th - 1) / th;
   double third = volume / 3.0;

@@ -1,48 +1,25 @@
-// fdf_sort.cu -- per-step re-sort of the particles by cell.
+// fdf_sort.cu -- per-step re-sort of the particles by cell (a counting sort).
 //
-// A stable LSD radix sort of (cell key, particle slot) pairs, 8 bits per pass,
-// followed by a boundary fill that turns the sorted keys into cell_start[Nc+1]
-// (the first sorted slot of every cell).  Removed particles carry the key Nc, so
-// they sort to the end and cell_start[Nc] is the number of survivors: the sort
-// is also the removal.  Stability makes the order -- and so every later sum --
-// a deterministic function of the previous order.
-//
-// Per pass: (1) per-tile digit histogram, (2) exclusive scan of the digit-major
-// histogram, (3) per-tile stable scatter.  In (3) each warp ranks its items in
-// order with __match_any_sync and a per-warp digit counter in shared memory;
-// the eight warps' counts are then scanned per digit.
+//   1. the locate kernel histograms the new cell keys (count[c], integer atomics,
+//      warp-aggregated: exact and order-independent);
+//   2. an exclusive scan turns count[0..Nc+1) into cell_start[0..Nc+1]: cell c
+//      owns sorted slots [cell_start[c], cell_start[c+1]); bucket Nc holds the LOST
+//      particles the initial setup keeps, and removed particles get no slot;
+//   3. each particle takes slot cell_start[key] + (atomic cursor of its cell);
+//   4. each cell's slots are then ordered by (PID, previous slot), so the final
+//      order -- and every later sum -- is the same on every run, whatever order
+//      the atomics took, and does not depend on the history of the swarm.
+// Sorted order is therefore (cell, PID): the order the oracle uses for the face
+// deposits, which makes those sums comparable bit for bit.
 #include "fdf_internal.cuh"
 
 namespace {
 
-constexpr int RADIX = 256;
-constexpr int SORT_THREADS = 256;
-constexpr int SORT_WARPS = SORT_THREADS / 32;
-constexpr int ITEMS = 16;
-constexpr int TILE = SORT_THREADS * ITEMS;   // 4096
-constexpr int WARP_CHUNK = TILE / SORT_WARPS;  // 512
-
-__global__ void __launch_bounds__(SORT_THREADS) k_hist(const unsigned int *__restrict__ keys, const int *n_dev,
-                                                      int shift, unsigned int *__restrict__ hist, int num_tiles) {
-  __shared__ unsigned int cnt[RADIX];
-  const int n = *n_dev;
-  const int tile = blockIdx.x;
-  for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) cnt[d] = 0;
-  __syncthreads();
-  const long long base = (long long)tile * TILE;
-#pragma unroll 4
-  for (int it = 0; it < ITEMS; ++it) {
-    long long idx = base + it * SORT_THREADS + threadIdx.x;
-    if (idx < n) atomicAdd(&cnt[(__ldg(keys + idx) >> shift) & (RADIX - 1)], 1u);
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) hist[(long long)d * num_tiles + tile] = cnt[d];
-}
-
-// ---- exclusive scan of a u32 array (reduce -> scan sums -> scan with offsets) ----
+// ---- exclusive scan of a u32 array (reduce -> scan of block sums -> scan with offsets) ----
 constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_ITEMS = 4;
-constexpr int SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;   // 8192 values per block
+constexpr int SUMS_PER_THREAD = 16;                      // up to 16384 blocks -> 134M values
 
 __device__ __forceinline__ unsigned int block_exclusive_scan(unsigned int v, unsigned int *total) {
   __shared__ unsigned int warp_tot[32];
@@ -73,7 +50,7 @@ __device__ __forceinline__ unsigned int block_exclusive_scan(unsigned int v, uns
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const unsigned int *__restrict__ in, long long count,
                                                              unsigned int *__restrict__ sums) {
-  long long base = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
+  long long base = (long long)blockIdx.x * SCAN_BLOCK + (long long)threadIdx.x * SCAN_ITEMS;
   unsigned int v = 0;
 #pragma unroll
   for (int q = 0; q < SCAN_ITEMS; ++q)
@@ -83,16 +60,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const unsigned int
   if (threadIdx.x == 0) sums[blockIdx.x] = tot;
 }
 
-// Single block: exclusive scan of up to SCAN_THREADS*8 block sums in place.
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(unsigned int *sums, int nsums) {
-  constexpr int PER = 8;
-  int base = threadIdx.x * PER;
-  unsigned int v[PER], t = 0;
+  int base = threadIdx.x * SUMS_PER_THREAD;
+  unsigned int v[SUMS_PER_THREAD], t = 0;
 #pragma unroll
-  for (int q = 0; q < PER; ++q) { v[q] = (base + q < nsums) ? sums[base + q] : 0u; t += v[q]; }
+  for (int q = 0; q < SUMS_PER_THREAD; ++q) { v[q] = (base + q < nsums) ? sums[base + q] : 0u; t += v[q]; }
   unsigned int ex = block_exclusive_scan(t, nullptr);
 #pragma unroll
-  for (int q = 0; q < PER; ++q) {
+  for (int q = 0; q < SUMS_PER_THREAD; ++q) {
     if (base + q < nsums) sums[base + q] = ex;
     ex += v[q];
   }
@@ -100,7 +75,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(unsigned int *sums, 
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(unsigned int *__restrict__ data, long long count,
                                                             const unsigned int *__restrict__ sums) {
-  long long base = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
+  long long base = (long long)blockIdx.x * SCAN_BLOCK + (long long)threadIdx.x * SCAN_ITEMS;
   unsigned int v[SCAN_ITEMS], t = 0;
 #pragma unroll
   for (int q = 0; q < SCAN_ITEMS; ++q) { v[q] = (base + q < count) ? data[base + q] : 0u; t += v[q]; }
@@ -112,141 +87,152 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(unsigned int *__res
   }
 }
 
-__global__ void __launch_bounds__(SORT_THREADS) k_scatter(const unsigned int *__restrict__ keys_in,
-                                                         const unsigned int *__restrict__ vals_in,
-                                                         unsigned int *__restrict__ keys_out,
-                                                         unsigned int *__restrict__ vals_out, const int *n_dev,
-                                                         int shift, const unsigned int *__restrict__ hist_scan,
-                                                         int num_tiles) {
-  __shared__ unsigned int wcnt[SORT_WARPS][RADIX];
-  const int n = *n_dev;
-  const int tile = blockIdx.x;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int q = threadIdx.x; q < SORT_WARPS * RADIX; q += SORT_THREADS) (&wcnt[0][0])[q] = 0;
-  __syncthreads();
-  const long long base = (long long)tile * TILE + (long long)w * WARP_CHUNK;
-  unsigned int key[ITEMS], val[ITEMS], rank[ITEMS];
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    long long idx = base + r * 32 + lane;
-    bool valid = idx < n;
-    key[r] = valid ? __ldg(keys_in + idx) : 0u;
-    val[r] = valid ? __ldg(vals_in + idx) : 0u;
-  }
-  const unsigned int lt_mask = (1u << lane) - 1u;
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    long long idx = base + r * 32 + lane;
-    bool valid = idx < n;
-    unsigned int d = valid ? ((key[r] >> shift) & (RADIX - 1)) : (unsigned int)RADIX;
-    unsigned int peers = __match_any_sync(0xffffffffu, d);
-    unsigned int before = __popc(peers & lt_mask);
-    unsigned int b0 = valid ? wcnt[w][d] : 0u;
-    __syncwarp();
-    if (valid && before == 0) wcnt[w][d] = b0 + __popc(peers);
-    __syncwarp();
-    rank[r] = b0 + before;
-  }
-  __syncthreads();
-  // per digit: exclusive scan over warps, plus the tile's global offset
-  for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) {
-    unsigned int run = hist_scan[(long long)d * num_tiles + tile];
-#pragma unroll
-    for (int ww = 0; ww < SORT_WARPS; ++ww) {
-      unsigned int c = wcnt[ww][d];
-      wcnt[ww][d] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < ITEMS; ++r) {
-    long long idx = base + r * 32 + lane;
-    if (idx < n) {
-      unsigned int d = (key[r] >> shift) & (RADIX - 1);
-      unsigned int pos = wcnt[w][d] + rank[r];
-      keys_out[pos] = key[r];
-      vals_out[pos] = val[r];
-    }
-  }
-}
-
-// cell_start[c] = first sorted slot whose key >= c, for c in [0, Nc] (Nc = sentinel).
-__global__ void k_cell_bounds(const unsigned int *__restrict__ keys, const DevCounters *cnt, unsigned int sentinel,
-                              int *__restrict__ cell_start) {
+// Slot of every kept particle: cell_start[key] + its rank among the particles of the
+// same cell that reached the cursor before it (warp-aggregated atomics).
+__global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__restrict__ keys, const DevCounters *cnt,
+                                                      unsigned int sentinel, int keep_lost,
+                                                      const unsigned int *__restrict__ cell_start,
+                                                      unsigned int *__restrict__ cursor,
+                                                      unsigned int *__restrict__ perm) {
   const int n = cnt->n_sorted;
-  long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (s > n) return;
-  long long prev = (s == 0) ? -1 : (long long)keys[s - 1];
-  long long cur = (s == n) ? (long long)sentinel : (long long)keys[s];
-  if (cur > (long long)sentinel) cur = sentinel;
-  for (long long c = prev + 1; c <= cur; ++c) cell_start[c] = (int)s;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned int key = 0xffffffffu;
+  if (s < n) {
+    key = keys[s];
+    if (key >= sentinel) key = keep_lost ? sentinel : 0xffffffffu;
+  }
+  const unsigned int peers = __match_any_sync(0xffffffffu, key);
+  if (key == 0xffffffffu) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  const unsigned int rank = __popc(peers & ((1u << lane) - 1u));
+  unsigned int base = 0;
+  if (lane == leader) base = atomicAdd(cursor + key, (unsigned int)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  perm[cell_start[key] + base + rank] = (unsigned int)s;
 }
 
-__global__ void k_update_counts(DevCounters *cnt, const int *cell_start, unsigned int sentinel, int drop_removed) {
-  int live = cell_start[sentinel];
-  cnt->n = live;
-  if (drop_removed) cnt->n_sorted = live;
+// Orders every cell's slots by (PID, previous slot) -- or by previous slot alone when
+// pid is null.  Segments are short (the mean occupancy is a few particles per cell);
+// up to 32 entries are sorted in registers and longer ones in place in global memory.
+constexpr int SEG_LOCAL = 32;
+__global__ void __launch_bounds__(256) k_order_segments(const unsigned int *__restrict__ cell_start, int nseg,
+                                                       const long long *__restrict__ pid,
+                                                       unsigned int *__restrict__ perm) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nseg) return;
+  const unsigned int s0 = cell_start[c], s1 = cell_start[c + 1];
+  const unsigned int L = s1 - s0;
+  if (L < 2) return;
+  if (L <= SEG_LOCAL) {
+    long long kp[SEG_LOCAL];
+    unsigned int ix[SEG_LOCAL];
+    for (unsigned int q = 0; q < L; ++q) {
+      unsigned int v = perm[s0 + q];
+      long long kv = pid ? pid[v] : (long long)v;
+      unsigned int r = q;
+      while (r > 0 && (kp[r - 1] > kv || (kp[r - 1] == kv && ix[r - 1] > v))) {
+        kp[r] = kp[r - 1];
+        ix[r] = ix[r - 1];
+        --r;
+      }
+      kp[r] = kv;
+      ix[r] = v;
+    }
+    for (unsigned int q = 0; q < L; ++q) perm[s0 + q] = ix[q];
+  } else {
+    for (unsigned int q = 1; q < L; ++q) {
+      unsigned int v = perm[s0 + q];
+      long long kv = pid ? pid[v] : (long long)v;
+      unsigned int r = q;
+      while (r > 0) {
+        unsigned int u = perm[s0 + r - 1];
+        long long ku = pid ? pid[u] : (long long)u;
+        if (ku < kv || (ku == kv && u < v)) break;
+        perm[s0 + r] = u;
+        --r;
+      }
+      perm[s0 + r] = v;
+    }
+  }
+}
+
+// count[cell[s]] += 1 for 0 <= cell[s] < ncells (warp-aggregated integer atomics)
+__global__ void __launch_bounds__(256) k_cell_histogram(const int *__restrict__ cell, long long n, long long ncells,
+                                                       unsigned int *__restrict__ count) {
+  const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int key = 0xffffffffu;
+  if (s < n) {
+    const int c = cell[s];
+    if (c >= 0 && (long long)c < ncells) key = (unsigned int)c;
+  }
+  const unsigned int peers = __match_any_sync(0xffffffffu, key);
+  if (key != 0xffffffffu && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+    atomicAdd(count + key, (unsigned int)__popc(peers));
+}
+
+// slot of every particle with a valid cell (warp-aggregated cursors)
+__global__ void __launch_bounds__(256) k_cell_slots(const int *__restrict__ cell, long long n, long long ncells,
+                                                   const unsigned int *__restrict__ cell_start,
+                                                   unsigned int *__restrict__ cursor, unsigned int *__restrict__ perm) {
+  const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  unsigned int key = 0xffffffffu;
+  if (s < n) {
+    const int c = cell[s];
+    if (c >= 0 && (long long)c < ncells) key = (unsigned int)c;
+  }
+  const unsigned int peers = __match_any_sync(0xffffffffu, key);
+  if (key == 0xffffffffu) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  const unsigned int rank = __popc(peers & ((1u << lane) - 1u));
+  unsigned int base = 0;
+  if (lane == leader) base = atomicAdd(cursor + key, (unsigned int)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  perm[cell_start[key] + base + rank] = (unsigned int)s;
 }
 
 }  // namespace
 
-size_t radix_scratch_bytes(int n_cap) {
-  long long tiles = ((long long)n_cap + TILE - 1) / TILE;
-  if (tiles < 1) tiles = 1;
-  long long hist = tiles * RADIX;
-  long long sums = (hist + SCAN_BLOCK - 1) / SCAN_BLOCK;
-  auto al = [](long long b) { return (size_t)((b + 255) / 256 * 256); };
-  return al(4LL * n_cap) * 2 + al(4 * hist) + al(4 * (sums + 1));
-}
+size_t scan_scratch_words(long long count) { return (size_t)((count + SCAN_BLOCK - 1) / SCAN_BLOCK) + 1; }
 
-void radix_scratch_carve(void *base, int n_cap, RadixScratch *rs) {
-  long long tiles = ((long long)n_cap + TILE - 1) / TILE;
-  if (tiles < 1) tiles = 1;
-  long long hist = tiles * RADIX;
-  auto al = [](long long b) { return (size_t)((b + 255) / 256 * 256); };
-  char *p = (char *)base;
-  rs->keys_alt = (unsigned int *)p; p += al(4LL * n_cap);
-  rs->vals_alt = (unsigned int *)p; p += al(4LL * n_cap);
-  rs->hist = (unsigned int *)p; p += al(4 * hist);
-  rs->hist_scan_tmp = (unsigned int *)p;
-  rs->cap_items = n_cap;
-  rs->cap_tiles = (int)tiles;
-}
+long long scan_max_count() { return (long long)SCAN_BLOCK * SCAN_THREADS * SUMS_PER_THREAD; }
 
-static void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums, cudaStream_t s) {
+void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums, cudaStream_t s) {
   long long blocks = (count + SCAN_BLOCK - 1) / SCAN_BLOCK;
+  if (blocks < 1) blocks = 1;
   k_scan_reduce<<<(unsigned)blocks, SCAN_THREADS, 0, s>>>(data, count, sums);
   k_scan_sums<<<1, SCAN_THREADS, 0, s>>>(sums, (int)blocks);
   k_scan_apply<<<(unsigned)blocks, SCAN_THREADS, 0, s>>>(data, count, sums);
 }
 
-void radix_sort_pairs(unsigned int **keys, unsigned int **vals, const int *n_dev, int bits, RadixScratch &rs,
-                      cudaStream_t s) {
-  int tiles = rs.cap_tiles;
-  unsigned int *kin = *keys, *vin = *vals, *kout = rs.keys_alt, *vout = rs.vals_alt;
-  int passes = (bits + 7) / 8;
-  for (int p = 0; p < passes; ++p) {
-    int shift = 8 * p;
-    k_hist<<<tiles, SORT_THREADS, 0, s>>>(kin, n_dev, shift, rs.hist, tiles);
-    exclusive_scan_u32(rs.hist, (long long)tiles * RADIX, rs.hist_scan_tmp, s);
-    k_scatter<<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n_dev, shift, rs.hist, tiles);
-    unsigned int *tk = kin, *tv = vin;
-    kin = kout; vin = vout; kout = tk; vout = tv;
-  }
-  // the sorted pairs are in (kin, vin); hand the other pair back as scratch
-  *keys = kin; *vals = vin;
-  rs.keys_alt = kout; rs.vals_alt = vout;
-}
-
-void launch_cell_bounds(const unsigned int *keys, int n_cap, const DevCounters *cnt, unsigned int sentinel,
-                        int *cell_start, cudaStream_t s) {
-  int th = 256;
-  long long blocks = ((long long)n_cap + 1 + th - 1) / th;
-  k_cell_bounds<<<(unsigned)blocks, th, 0, s>>>(keys, cnt, sentinel, cell_start);
-}
-
-void launch_update_counts(DevCounters *cnt, const int *cell_start, unsigned int sentinel, int drop_removed,
+void launch_scatter_slots(const unsigned int *keys, int n_cap, const DevCounters *cnt, unsigned int sentinel,
+                          int keep_lost, const unsigned int *cell_start, unsigned int *cursor, unsigned int *perm,
                           cudaStream_t s) {
-  k_update_counts<<<1, 1, 0, s>>>(cnt, cell_start, sentinel, drop_removed);
+  int th = 256;
+  int blocks = (n_cap + th - 1) / th;
+  if (blocks == 0) blocks = 1;
+  k_scatter_slots<<<blocks, th, 0, s>>>(keys, cnt, sentinel, keep_lost, cell_start, cursor, perm);
+}
+
+void launch_order_segments(const unsigned int *cell_start, int nseg, const long long *pid, unsigned int *perm,
+                           cudaStream_t s) {
+  int th = 256;
+  int blocks = (nseg + th - 1) / th;
+  k_order_segments<<<blocks, th, 0, s>>>(cell_start, nseg, pid, perm);
+}
+
+// Stable counting sort of particle slots by cell id, on caller-provided scratch:
+// cursor [ncells] and sums [scan_scratch_words(ncells + 1)].  cell_start [ncells + 1]
+// is both the histogram and (after the scan) the output.
+void cell_sort_on_scratch(const int *cell, long long n, long long ncells, unsigned int *perm,
+                          unsigned int *cell_start, unsigned int *cursor, unsigned int *sums, cudaStream_t s) {
+  cudaMemsetAsync(cell_start, 0, 4ull * (ncells + 1), s);
+  cudaMemsetAsync(cursor, 0, 4ull * ncells, s);
+  const int th = 256;
+  const unsigned int blocks = (unsigned int)((n + th - 1) / th > 0 ? (n + th - 1) / th : 1);
+  k_cell_histogram<<<blocks, th, 0, s>>>(cell, n, ncells, cell_start);
+  exclusive_scan_u32(cell_start, ncells + 1, sums, s);
+  k_cell_slots<<<blocks, th, 0, s>>>(cell, n, ncells, cell_start, cursor, perm);
+  launch_order_segments(cell_start, (int)ncells, nullptr, perm, s);
 }

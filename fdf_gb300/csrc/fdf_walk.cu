@@ -25,12 +25,13 @@
 // weights are the reference's, and the evaluation count reported for parity is
 // the reference's (MAX_TRAVERSAL).
 #include "fdf_internal.cuh"
+#include "fdf_exact.cuh"
 
 namespace {
 
-__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+using fdfx::add;
+using fdfx::sub;
+using fdfx::mul;
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -40,12 +41,13 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
                                                 double dt, int advect, int reset_first, const double *__restrict__ bbox,
                                                 int drop_removed, DevCounters *cnt, unsigned int *__restrict__ keys,
-                                                unsigned int *__restrict__ vals, unsigned int sentinel) {
+                                                unsigned int *__restrict__ count, unsigned int sentinel) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
   unsigned long long my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0;
   unsigned int my_err = 0;
+  unsigned int hkey = 0xffffffffu;   // histogram bucket of this particle (none = all ones)
   if (s < n) {
     double x = b.x[s], y = b.y[s], z = b.z[s];
     if (advect) {
@@ -61,12 +63,7 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
     if (st != ST_ACTIVE_AND_LOCATED) {
       // InitializeTraversalParameters: previous cell if it is inside the grid, else (0,0,0)
       int i = 0, j = 0, k = 0;
-      if (cell >= 0 && (long long)cell < g.Nc) {
-        i = cell % g.IM;
-        int t = cell / g.IM;
-        j = t % g.JM;
-        k = t / g.JM;
-      }
+      if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, i, j, k);
       int steps = 0, evaluated = 0;
       bool concluded = false, cycle = false;
       long long saved = -1;
@@ -80,26 +77,27 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
         if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
         const double2 *row = reinterpret_cast<const double2 *>(planes + cur * FDF_ROW);
         double2 tf = __ldg(row + 18);   // thr, degenerate flag
-        if (tf.y != 0.0) { my_err |= ERRBIT_DEGENERATE; lost = true; break; }
-        const double thr = tf.x;
+        if (fdfx::ubits(tf.y) != 0ULL) { my_err |= ERRBIT_DEGENERATE; lost = true; break; }
+        const unsigned long long thr_bits = fdfx::ubits(tf.x);
+        const bool thr_nan = fdfx::is_nan(tf.x);
         ++evaluated;
         bool neg = false, zero = false;
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
           double2 p0 = __ldg(row + 3 * f), p1 = __ldg(row + 3 * f + 1), p2 = __ldg(row + 3 * f + 2);
-          // p0 = (fc.x, fc.y), p1 = (fc.z, n.x), p2 = (n.y, n.z)
+          // p0 = (fc.x, fc.y), p1 = (fc.z, n.x), p2 = (n.y, n.z); d = (fc - p) . n
           double dd = add(add(mul(sub(p0.x, x), p1.y), mul(sub(p0.y, y), p2.x)), mul(sub(p1.x, z), p2.y));
-          if (fabs(dd) < thr) dd = 0.0;
+          if (fdfx::abs_lt_bits(dd, thr_bits, thr_nan)) dd = 0.0;
           d[f] = dd;
-          neg |= (dd < 0.0);
-          zero |= (dd == 0.0);
+          neg |= fdfx::lt0(dd);
+          zero |= fdfx::eq0(dd);
         }
         if (!neg || zero) {
           concluded = true;   // position >= 0: inside, or on a face (accepted even if outside another)
         } else {
-          if (d[F_FRONT] < 0.0) k += 1; else if (d[F_BACK] < 0.0) k -= 1;
-          if (d[F_LEFT] < 0.0) i -= 1; else if (d[F_RIGHT] < 0.0) i += 1;
-          if (d[F_BOTTOM] < 0.0) j -= 1; else if (d[F_TOP] < 0.0) j += 1;
+          if (fdfx::lt0(d[F_FRONT])) k += 1; else if (fdfx::lt0(d[F_BACK])) k -= 1;
+          if (fdfx::lt0(d[F_LEFT])) i -= 1; else if (fdfx::lt0(d[F_RIGHT])) i += 1;
+          if (fdfx::lt0(d[F_BOTTOM])) j -= 1; else if (fdfx::lt0(d[F_TOP])) j += 1;
         }
       }
       my_evals = (unsigned long long)(cycle ? FDF_MAX_TRAVERSAL : steps);
@@ -109,9 +107,10 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
         cell = -1;
         st = ST_LOST;
       } else {
+        const unsigned long long tol_bits = fdfx::ubits(FDF_INTERP_DIST_TOL);
 #pragma unroll
         for (int f = 0; f < 6; ++f)
-          if (d[f] <= FDF_INTERP_DIST_TOL) d[f] = FDF_INTERP_DIST_TOL;
+          if (fdfx::le_pos(d[f], tol_bits)) d[f] = FDF_INTERP_DIST_TOL;
         b.a1[s] = __ddiv_rn(d[F_LEFT], add(d[F_LEFT], d[F_RIGHT]));
         b.a2[s] = __ddiv_rn(d[F_BOTTOM], add(d[F_BOTTOM], d[F_TOP]));
         b.a3[s] = __ddiv_rn(d[F_BACK], add(d[F_FRONT], d[F_BACK]));
@@ -135,7 +134,14 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
       }
     }
     keys[s] = key;
-    vals[s] = (unsigned int)s;
+    if (key < sentinel) hkey = key;
+    else if (!drop_removed) hkey = sentinel;   // the initial setup keeps LOST particles, at the end
+  }
+  {
+    // histogram of the kept keys, one atomic per distinct key in the warp
+    const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
+    const int lane = threadIdx.x & 31;
+    if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
   }
   my_lost = warp_sum_u64(my_lost);
   my_oob = warp_sum_u64(my_oob);
@@ -156,13 +162,13 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
 }  // namespace
 
 void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
-                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *vals,
+                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *count,
                    unsigned int sentinel, cudaStream_t s) {
   // advect and drop_removed are both set by the fused step, which also resets statuses first.
   int reset_first = drop_removed;
   int th = 256;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
-  k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, vals,
+  k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, count,
                                  sentinel);
 }

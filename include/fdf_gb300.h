@@ -85,7 +85,8 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n, double *position, d
 /* ---- Eulerian outputs ---- */
 /* ParticleCount and the P average, node-sized [KM+1][JM+1][IM+1] (interpolation.c:2063-2116). */
 int fdf_GetScatteredFields(FdfContext *ctx, double *count, double *P_avg);
-/* Corner (node) velocity of the last interpolation, [KM+1][JM+1][IM+1][3]. */
+/* Corner (node) velocity that the interpolation averages from ucat (interpolation.c:598-679),
+ * every node, [KM+1][JM+1][IM+1][3]. */
 int fdf_GetCornerField(FdfContext *ctx, double *corner);
 /* Face volume deposits: fi [KM][JM][IM+1], fj [KM][JM+1][IM], fk [KM+1][JM][IM].
  * No counterpart in the reference (its only deposit is the cell average of P):
@@ -106,6 +107,17 @@ int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info);
 int fdf_AdvanceStep(FdfContext *ctx, FdfStepInfo *info);
 int fdf_AdvanceSteps(FdfContext *ctx, int nsteps);
 
+/* ---- sort by cell (the per-step re-sort of the hot path, as a standalone call) ---- */
+/* Stable counting sort of n particle slots by cell id, all pointers on the device.
+ * Slots whose id is negative or >= ncells get no place.  On return cell_start[c] is the
+ * first sorted slot of cell c (cell_start[ncells] = number of placed slots) and
+ * perm[cell_start[c] .. cell_start[c+1]) lists cell c's slot indices in ascending
+ * order.  Scratch is stream-ordered (cudaMallocAsync/cudaFreeAsync on `stream`).
+ * No counterpart call in the reference, which keeps DMSwarm in insertion order; it
+ * is the sort-by-cell step that makes the gathers of this library coalesced. */
+int fdf_SortByCell(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t *perm, uint32_t *cell_start,
+                   void *stream);
+
 /* ---- utilities ---- */
 int fdf_Synchronize(FdfContext *ctx);
 /* The context's cudaStream_t, for callers that time or order work around it. */
@@ -114,13 +126,15 @@ const char *fdf_GetLastError(FdfContext *ctx);
 /* Number of kernel launches the library has issued on this context. */
 int64_t fdf_GetLaunchCount(FdfContext *ctx);
 /* Stage timing with CUDA events on the context stream (enable resets the record).
- * Stages: 0 center->corner, 1 advect+locate, 2 sort by cell, 3 cell bounds,
+ * Stages: 0 center->corner (on a second stream, concurrent with 2), 1 advect+locate,
+ * 2 sort by cell (histogram scan, slots, per-cell PID order), 3 wait for stage 0,
  * 4 gather+interpolate, 5 deposits.  ms_total[s] sums the stage over all pipeline
  * runs since enabling; launches[s] counts those runs. */
 int fdf_SetProfiling(FdfContext *ctx, int enable);
 /* Running totals since fdf_SetSwarm: particles advanced (sum over steps of the live
- * particles at step start) and walking-search cell evaluations actually made. */
-int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals);
+ * particles at step start), walking-search cell evaluations actually made, and
+ * corner nodes computed (the steps compute only nodes next to occupied cells). */
+int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals, int64_t *corner_nodes);
 int fdf_GetStageTimes(FdfContext *ctx, double *ms_total, int64_t *launches, int nstages);
 
 #ifdef __cplusplus

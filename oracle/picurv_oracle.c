@@ -421,6 +421,20 @@ void o_ScatterParticleFieldToEulerField_P(const OGrid *g, const OSwarm *s, doubl
   free(sum);
 }
 
+typedef struct { int64_t cell, pid, idx; } OKey;
+
+static int o_key_cmp(const void *a, const void *b) {
+  const OKey *x = (const OKey *)a, *y = (const OKey *)b;
+  if (x->cell != y->cell) return x->cell < y->cell ? -1 : 1;
+  if (x->pid != y->pid) return x->pid < y->pid ? -1 : 1;
+  return (x->idx > y->idx) - (x->idx < y->idx);
+}
+
+/* The face deposit is defined with a fixed summation order: particles in
+ * ascending (linear cell id i + IM*(j + JM*k), PID) order, each face summing its
+ * contributions in that order from a starting 0.0.  A face's lower cell precedes
+ * its upper cell in that order, so every face adds its lower cell's particles
+ * (weight a) first and its upper cell's (weight 1-a) second. */
 void o_DepositParticlesToFaces(const OGrid *g, const OSwarm *s, double volume,
                                double *fi, double *fj, double *fk,
                                double *mom_i, double *mom_j, double *mom_k,
@@ -437,9 +451,17 @@ void o_DepositParticlesToFaces(const OGrid *g, const OSwarm *s, double volume,
   if (abs_j) memset(abs_j, 0, (size_t)nfj * sizeof(double));
   if (abs_k) memset(abs_k, 0, (size_t)nfk * sizeof(double));
   const double third = volume / 3.0;
+  OKey *order = (OKey *)malloc((size_t)(s->n > 0 ? s->n : 1) * sizeof(OKey));
+  int64_t m = 0;
   for (int64_t p = 0; p < s->n; p++) {
     int64_t i = s->cell[3 * p], j = s->cell[3 * p + 1], k = s->cell[3 * p + 2];
     if (i < 0 || i >= IM || j < 0 || j >= JM || k < 0 || k >= KM) continue;
+    order[m].cell = (k * JM + j) * IM + i; order[m].pid = s->pid[p]; order[m].idx = p; m++;
+  }
+  qsort(order, (size_t)m, sizeof(OKey), o_key_cmp);
+  for (int64_t q = 0; q < m; q++) {
+    const int64_t p = order[q].idx;
+    int64_t i = s->cell[3 * p], j = s->cell[3 * p + 1], k = s->cell[3 * p + 2];
     const double *a = &s->weight[3 * p];
     const double *u = &s->vel[3 * p];
     int64_t fidx[6];
@@ -464,6 +486,7 @@ void o_DepositParticlesToFaces(const OGrid *g, const OSwarm *s, double volume,
       }
     }
   }
+  free(order);
 }
 
 /* simulation.c:240-311 (one step, one rank, steady ucat). */

@@ -43,3 +43,12 @@ def assert_faces_close(gpu_faces, ref: dict, rel: float = 1e-12, what: str = "")
         err = np.abs(g - r)
         tol = rel * scale + 1e-300
         assert np.all(err <= tol), f"{what}: {key} max err {err.max()} (tol {rel} x |sum|)"
+
+
+def assert_faces_bitwise(gpu_faces, ref: dict, what: str = ""):
+    """Face sums bit-identical: both sides sum in (cell, PID) order from 0.0."""
+    for g, key in zip(gpu_faces, ("fi", "fj", "fk")):
+        r = ref[key]
+        bad = np.nonzero(g.view(np.int64) != r.view(np.int64))
+        assert len(bad[0]) == 0, (f"{what}: {key} differs at {len(bad[0])} faces, first {tuple(b[0] for b in bad)}: "
+                                  f"{g[tuple(b[0] for b in bad)]} vs {r[tuple(b[0] for b in bad)]}")

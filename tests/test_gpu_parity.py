@@ -1,9 +1,8 @@
 """GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
 
-Bar: bit-exact for cell indices, statuses, PIDs, positions, velocities, weights
-and the cell-averaged P (plain FP64 path, no FMA, same operation order);
-face deposits within 1e-12 x (sum of |contributions|) per face, because the
-GPU sums each face in sorted-by-cell order and the oracle in particle order.
+Bar: bit-exact for cell indices, statuses, PIDs, positions, velocities, weights,
+the cell count and P average, and the face deposits (plain FP64 path, no FMA,
+same operation order; the face sums run in (cell, PID) order on both sides).
 """
 import numpy as np
 import pytest
@@ -11,7 +10,8 @@ import pytest
 from fdf_gb300 import workloads as W
 from fdf_gb300.context import PicContext, SwarmArrays, PetscError, LOST, ACTIVE_AND_LOCATED
 from oracle import oracle as O
-from tests.parity_util import (assert_faces_close, assert_swarm_bitwise, from_oracle_swarm, to_oracle_swarm)
+from tests.parity_util import (assert_faces_bitwise, assert_faces_close, assert_swarm_bitwise, from_oracle_swarm,
+                               to_oracle_swarm)
 
 pytestmark = pytest.mark.gpu
 
@@ -54,6 +54,7 @@ def run_parity(ctx, wl, steps, check_every=1, faces=True):
             assert np.array_equal(avg, sim.avg), f"step {st} P average"
             if faces:
                 ref = O.deposit_faces(g, os_, volume=wl.volume)
+                assert_faces_bitwise(ctx.get_faces(), ref, what=f"step {st}")
                 assert_faces_close(ctx.get_faces(), ref, what=f"step {st}")
     return ctx.get_swarm()
 
@@ -150,6 +151,10 @@ def test_deterministic_repeat(ctx):
     (s1, f1, c1), (s2, f2, c2) = outs
     for name in ("position", "velocity", "weight", "cell", "pid"):
         assert np.array_equal(getattr(s1, name), getattr(s2, name)), name   # same order too
+    # the swarm is held sorted by (cell, PID)
+    lin = (s1.cell[:, 2] * 16 + s1.cell[:, 1]) * 16 + s1.cell[:, 0]
+    order = np.lexsort((s1.pid, lin))
+    assert np.array_equal(order, np.arange(s1.n))
     for a, b in zip(f1 + c1, f2 + c2):
         assert np.array_equal(a.view(np.int64), b.view(np.int64))
 
@@ -172,6 +177,7 @@ def test_full_size_properties_sinusoidal(ctx):
     cnt, avg = ctx.get_scattered()
     assert np.array_equal(cnt, sim.count) and np.array_equal(avg, sim.avg)
     fi, fj, fk = ctx.get_faces()
+    assert_faces_bitwise((fi, fj, fk), O.deposit_faces(g, os_, volume=wl.volume), "full-size step")
     tot = fi.sum() + fj.sum() + fk.sum()
     assert abs(tot - after.n * wl.volume) <= 1e-9 * after.n
     assert cnt.sum() == after.n
