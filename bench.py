@@ -333,6 +333,9 @@ def run_gpu(args, rank, ws, local, dist):
                 "config": {"workload": wl.name, "form": "plain_fp64", "grid": f"{IM}x{JM}x{KM}",
                            "particles": wl.n, "cfl": wl.meta.get("cfl"), "dt": wl.dt,
                            "parallelism": "replicas" if ws > 1 else "single",
+                           "initial_cell": ("corner cell (0,0,0), as the reference" if wl.meta.get("corner_start")
+                                            or wl.meta.get("family") == "uniform" else
+                                            "generating cell of each particle (harness choice)"),
                            "l2": "inputs larger than L2 (plane table %.2f GB, swarm %.0f MB)"
                                  % (38 * 8 * Nc / 1e9, 2 * 93 * wl.n / 1e6),
                            "walk_evals_per_particle_step": evals / max(psteps, 1)},
