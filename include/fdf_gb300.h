@@ -118,6 +118,19 @@ int fdf_AdvanceSteps(FdfContext *ctx, int nsteps);
 int fdf_SortByCell(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t *perm, uint32_t *cell_start,
                    void *stream);
 
+/* fdf_SortByCell for callers that cannot allocate device memory (e.g. a host code whose
+ * device memory is owned by another allocator, or a loop that must not enter one).
+ * No counterpart in the reference.  Same arguments, results and ordering as
+ * fdf_SortByCell; its scratch is a file-scope device array of ~4 MiB that every GPU
+ * loading this library keeps until exit, so ncells is limited to FDF_NOALLOC_MAX_CELLS
+ * (larger requests return FDF_ERR_ARG_OUTOFRANGE).  The first call on a device looks up
+ * that array's address on the current device: make it outside stream capture.  All
+ * calls share the array (each clears what must start at zero), so calls that overlap
+ * on the GPU race: serialise them.  Calls no cudaMalloc/cudaFree. */
+#define FDF_NOALLOC_MAX_CELLS 1048576
+int fdf_SortByCellNoAlloc(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t *perm, uint32_t *cell_start,
+                          void *stream);
+
 /* ---- utilities ---- */
 int fdf_Synchronize(FdfContext *ctx);
 /* The context's cudaStream_t, for callers that time or order work around it. */
