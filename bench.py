@@ -219,16 +219,39 @@ def run_reference(args, rank):
 
 # ----------------------------------------------------------------------------- GPU
 
-def run_gpu(args, rank, ws, local, dist):
-    from fdf_gb300.context import PicContext, SwarmArrays
-    import torch
+FORMS = {"plain_fp64": 0, "fp32": 1}
+FORM_DTYPE = {"plain_fp64": "f64", "fp32": "f32 (positions and walk decisions f64)"}
 
-    wl = workload(args.workload)
+
+def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_step: float, Nc: int, Nn: int,
+                      Nf: int) -> dict:
+    """Algorithmic bytes per launch of each stage (the accounting of the design doc 3.3)."""
+    if form == "fp32":
+        return {
+            "center_to_corner": 24 * nodes_per_step,
+            "advect_locate": 86 * n_avg + 176 * evals_per_step,
+            "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
+            "wait_corner": 0,
+            "gather_interpolate": 121 * n_avg + 12 * Nn,
+            "deposit": 4 * (Nc + 1) + 16 * n_avg + 8 * Nn + 4 * Nf,
+        }
+    return {
+        "center_to_corner": 48 * nodes_per_step,
+        "advect_locate": LOCATE_PER_PARTICLE * n_avg + ROW_BYTES * evals_per_step,
+        "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
+        "wait_corner": 0,
+        "gather_interpolate": GATHER_PER_PARTICLE * n_avg + 24 * Nn,
+        "deposit": 4 * (Nc + 1) + 32 * n_avg + 16 * Nn + 8 * Nf,
+    }
+
+
+def time_form(ctx, wl, form, args, dist, local, with_clocks):
+    """Warm-up, then the timed steps of one form; returns its measurements."""
+    import torch
     IM, JM, KM = wl.dims
     Nc, Nn = IM * JM * KM, (IM + 1) * (JM + 1) * (KM + 1)
     Nf = (IM + 1) * JM * KM + IM * (JM + 1) * KM + IM * JM * (KM + 1)
-    ctx = PicContext(local)
-    ctx.load_workload(wl)
+    ctx.load_workload(wl, form=FORMS[form])
     ctx.initial_setup()
     ctx.steps(args.warmup)
     ctx.synchronize()
@@ -237,42 +260,94 @@ def run_gpu(args, rank, ws, local, dist):
     ps0, e0, nd0 = ctx.counters()
     l0 = ctx.launches
     ctx.set_profiling(True)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local) if with_clocks else None
     barrier(dist)
     torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
     ev0.record(stream)
     ctx.steps(args.steps)
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
     barrier(dist)
-    clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    ms_max = reduce_max(dist, ms)
+    clk = clocks.stop() if clocks else None
+    ms_max = reduce_max(dist, ev0.elapsed_time(ev1))
     ps1, e1, nd1 = ctx.counters()
     launches = ctx.launches - l0
     stages = ctx.stage_times()
     ctx.set_profiling(False)
-    psteps = ps1 - ps0
-    evals = e1 - e0
-    n_avg = psteps / max(args.steps, 1)
-    total_psteps = psteps * ws            # replicas: every rank advanced its own copy
-    value = total_psteps / (ms_max / 1000.0)
-
-    # roofline of the dominant stage (algorithmic bytes / its average event-timed duration)
-    hbm, peak_kind = peaks()
-    alg = {
-        "center_to_corner": 48 * (nd1 - nd0) / max(args.steps, 1),   # 8 cells' ucat via cache + node write
-        "advect_locate": LOCATE_PER_PARTICLE * n_avg + ROW_BYTES * evals / max(args.steps, 1),
-        # keys + slot writes + PID reads of the per-cell ordering + the histogram scan (read + write)
-        "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
-        "wait_corner": 0,
-        "gather_interpolate": GATHER_PER_PARTICLE * n_avg + 24 * Nn,
-        "deposit": 4 * (Nc + 1) + 32 * n_avg + 16 * Nn + 8 * Nf,
-    }
+    psteps, evals = ps1 - ps0, e1 - e0
+    K = max(args.steps, 1)
+    n_avg = psteps / K
+    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf)
     per = {k: (v[0] / max(v[1], 1)) for k, v in stages.items()}
+    return dict(form=form, psteps=psteps, evals=evals, ms=ms_max, launches=launches, clocks=clk, per=per, alg=alg,
+                value=psteps * int(os.environ.get("WORLD_SIZE", "1")) / (ms_max / 1000.0))
+
+
+def fp32_accuracy(ctx, wl, steps: int, nthreads: int) -> dict:
+    """The precision form against the plain FP64 oracle from the same initial state, on the
+    full workload: per-field max / RMS errors over the particles present in both."""
+    from fdf_gb300.context import FORM_FP32, SwarmArrays
+    from oracle import oracle as O
+    ctx.load_workload(wl, form=FORM_FP32)
+    ctx.initial_setup()
+    ctx.steps(steps)
+    gpu = ctx.get_swarm().sorted_by_pid()
+    gfaces = ctx.get_faces()
+    gcount, gavg = ctx.get_scattered()
+    g = O.Grid(wl.coor)
+    s0 = SwarmArrays.create(wl.pos, cell=wl.cell0)
+    os_ = O.Swarm(pos=s0.position, vel=s0.velocity, weight=s0.weight, P=s0.P, cell=s0.cell, pid=s0.pid,
+                  status=s0.status, n=s0.n)
+    sim = O.Simulation(g, wl.ucat_node_sized(), os_, wl.dt, nthreads=nthreads)
+    sim.initial_setup()
+    for _ in range(steps):
+        sim.step()
+    ref = os_.sorted_by_pid()
+    common, ia, ib = np.intersect1d(gpu.pid, ref["pid"], return_indices=True)
+
+    def stats(err):
+        err = np.asarray(err, dtype=np.float64).ravel()
+        return {"max": float(err.max()) if err.size else 0.0, "rms": float(np.sqrt((err ** 2).mean())) if err.size else 0.0}
+
+    umag = np.maximum(np.linalg.norm(ref["vel"][ib], axis=1, keepdims=True), 1e-30)
+    f = O.deposit_faces(g, os_, volume=wl.volume)
+    face_err = np.concatenate([np.abs(gf - f[k]).ravel() / wl.volume for gf, k in zip(gfaces, ("fi", "fj", "fk"))])
+    occupied = sim.count > 0
+    return {"steps": steps, "particles_compared": int(len(common)), "gpu_particles": int(gpu.n),
+            "oracle_particles": int(len(ref["pid"])),
+            "same_cell_fraction": float(np.all(gpu.cell[ia] == ref["cell"][ib], axis=1).mean()),
+            "velocity_rel": stats(np.abs(gpu.velocity[ia] - ref["vel"][ib]) / umag),
+            "position_abs": stats(np.abs(gpu.position[ia] - ref["pos"][ib])),
+            "weight_abs": stats(np.abs(gpu.weight[ia] - ref["weight"][ib])),
+            "face_volume_abs_per_particle_volume": stats(face_err),
+            "count_abs": stats(np.abs(gcount - sim.count)),
+            "P_avg_rel": stats(np.abs(gavg[occupied] - sim.avg[occupied]) / np.abs(sim.avg[occupied]))}
+
+
+def run_gpu(args, rank, ws, local, dist):
+    from fdf_gb300.context import PicContext, SwarmArrays
+    import torch
+
+    wl = workload(args.workload)
+    IM, JM, KM = wl.dims
+    Nc, Nn = IM * JM * KM, (IM + 1) * (JM + 1) * (KM + 1)
+    Nf = (IM + 1) * JM * KM + IM * (JM + 1) * KM + IM * JM * (KM + 1)
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    ctx = PicContext(local)
+    results = {}
+    for q, form in enumerate(forms):
+        results[form] = time_form(ctx, wl, form, args, dist, local, with_clocks=(q == 0))
+    prim = results[forms[0]]
+    value, ms_max, psteps, evals, launches, clk = (prim["value"], prim["ms"], prim["psteps"], prim["evals"],
+                                                   prim["launches"], prim["clocks"])
+
+    # roofline of the dominant stage of the primary form (algorithmic bytes / mean event-timed duration)
+    hbm, peak_kind = peaks()
+    per, alg = prim["per"], prim["alg"]
     dom = max((k for k in per if alg.get(k)), key=per.get)
     achieved = alg[dom] / (per[dom] / 1000.0) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -280,6 +355,12 @@ def run_gpu(args, rank, ws, local, dist):
                 "algorithmic_bytes_per_launch": alg[dom], "traffic": None,
                 "stage_ms_per_step": {k: round(v, 4) for k, v in per.items()},
                 "stage_gbs": {k: round(alg[k] / (per[k] / 1000.0) / 1e9, 1) for k in per if per[k] > 0 and alg.get(k)}}
+    form_lines = {f: {"particle_steps_per_s": r["value"], "ms_per_step": r["ms"] / max(args.steps, 1),
+                      "walk_evals_per_particle_step": r["evals"] / max(r["psteps"], 1),
+                      "stage_ms_per_step": {k: round(v, 4) for k, v in r["per"].items()}}
+                  for f, r in results.items()}
+    ctx.load_workload(wl, form=FORMS[forms[0]])
+    ctx.initial_setup()
 
     # end to end through the C ABI with host (pinned) buffers
     e2e = None
@@ -318,6 +399,10 @@ def run_gpu(args, rank, ws, local, dist):
                "path": "fdf_SetSwarm + fdf_AdvanceStep + fdf_GetSwarm/GetScatteredFields/GetFaceDeposits, "
                        "pinned host DMSwarm-layout arrays"}
 
+    accuracy = None
+    if rank == 0 and ws == 1 and args.accuracy_steps > 0 and "fp32" in forms:
+        accuracy = fp32_accuracy(ctx, wl, args.accuracy_steps, os.cpu_count() or 1)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         from oracle import oracle as O
@@ -329,8 +414,8 @@ def run_gpu(args, rank, ws, local, dist):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": wl.name, "form": "plain_fp64", "grid": f"{IM}x{JM}x{KM}",
+                "scaling": "weak", "vs_baseline": None, "dtype": FORM_DTYPE[forms[0]], "data": "synthetic",
+                "config": {"workload": wl.name, "form": forms[0], "grid": f"{IM}x{JM}x{KM}",
                            "particles": wl.n, "cfl": wl.meta.get("cfl"), "dt": wl.dt,
                            "parallelism": "replicas" if ws > 1 else "single",
                            "initial_cell": ("corner cell (0,0,0), as the reference" if wl.meta.get("corner_start")
@@ -339,8 +424,9 @@ def run_gpu(args, rank, ws, local, dist):
                            "l2": "inputs larger than L2 (plane table %.2f GB, swarm %.0f MB)"
                                  % (38 * 8 * Nc / 1e9, 2 * 93 * wl.n / 1e6),
                            "walk_evals_per_particle_step": evals / max(psteps, 1)},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk}
+                "roofline": roofline, "forms": form_lines, "fp32_accuracy_vs_fp64_oracle": accuracy,
+                "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk}
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -352,9 +438,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="fdf", choices=["fdf", "reference"])
     ap.add_argument("--workload", default="sinusoidal")
+    ap.add_argument("--forms", default="fp32,plain_fp64",
+                    help="comma list; the first is the headline value, the others are reported beside it")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=10,
+                    help="steps of the FP32-form vs FP64-oracle comparison on the full workload (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -18,7 +18,7 @@ c_double_p = ctypes.POINTER(ctypes.c_double)
 
 class FdfStepInfo(ctypes.Structure):
     _fields_ = [("n_start", ctypes.c_int64), ("n_end", ctypes.c_int64), ("removed_lost", ctypes.c_int64),
-                ("removed_oob", ctypes.c_int64), ("walk_evals", ctypes.c_int64)]
+                ("removed_oob", ctypes.c_int64), ("walk_evals", ctypes.c_int64), ("fp64_fallbacks", ctypes.c_int64)]
 
 
 # name -> (restype, argtypes); mirrors include/fdf_gb300.h
@@ -27,6 +27,7 @@ _SIGS = {
     "fdf_ContextDestroy": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_SetGrid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
     "fdf_SetUcat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTimeStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_SetParticleVolume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_ReserveParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),

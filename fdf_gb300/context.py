@@ -21,6 +21,7 @@ ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG"
              73: "PETSC_ERR_ARG_WRONGSTATE", 76: "PETSC_ERR_LIB", 83: "PETSC_ERR_USER", 85: "PETSC_ERR_ARG_NULL",
              97: "PETSC_ERR_GPU"}
 NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
+FORM_PLAIN_FP64, FORM_FP32 = 0, 1
 
 
 class PetscError(RuntimeError):
@@ -130,6 +131,10 @@ class PicContext:
             raise ValueError(f"ucat shape {ucat.shape} matches neither the cell nor the node layout")
         self._check(self.lib.fdf_SetUcat(self.h, _ptr(ucat), node_sized))
 
+    def set_form(self, form: int):
+        """FORM_PLAIN_FP64 (bit-exact) or FORM_FP32 (precision form); applies at the next set_swarm."""
+        self._check(self.lib.fdf_SetForm(self.h, int(form)))
+
     def set_dt(self, dt: float):
         self._check(self.lib.fdf_SetTimeStep(self.h, float(dt)))
 
@@ -146,7 +151,9 @@ class PicContext:
         self._check(self.lib.fdf_SetSwarm(self.h, s.n, *[_ptr(a) for a in arrs]))
         self._cap = max(self._cap, s.n)
 
-    def load_workload(self, wl, P: float = 101325.0):
+    def load_workload(self, wl, P: float = 101325.0, form: int | None = None):
+        if form is not None:
+            self.set_form(form)
         self.set_grid(wl.coor)
         self.set_ucat(wl.ucat)
         self.set_dt(wl.dt)

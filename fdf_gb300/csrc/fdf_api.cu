@@ -13,6 +13,7 @@
 #include "fdf_internal.cuh"
 #include "../../include/fdf_gb300.h"
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -26,6 +27,10 @@ struct FdfContext {
   bool has_grid = false, has_ucat = false;
   double *coor = nullptr, *planes = nullptr, *ucat = nullptr, *corner = nullptr, *bbox = nullptr;
   double *count = nullptr, *avg = nullptr, *fi = nullptr, *fj = nullptr, *fk = nullptr;
+  // precision form (FDF_FORM_FP32)
+  int form = FDF_FORM_PLAIN_FP64;
+  float *table32 = nullptr, *ucat32 = nullptr, *corner32 = nullptr, *fbox = nullptr;
+  float *count32 = nullptr, *avg32 = nullptr, *fi32 = nullptr, *fj32 = nullptr, *fk32 = nullptr;
   double bbox_h[6] = {0, 0, 0, 0, 0, 0};
   double dt = 0.0, volume = 1.0;
   int cap = 0;
@@ -41,6 +46,8 @@ struct FdfContext {
   size_t staging_bytes = 0;
   unsigned int sentinel = 0;
   bool swarm_set = false;
+  int swarm_form = FDF_FORM_PLAIN_FP64;   // form the swarm's device arrays are held in
+  int out_form = FDF_FORM_PLAIN_FP64;     // form of the last deposits
   long long launches = 0;
   // stage timing: events recorded on the context stream between pipeline stages
   bool profiling = false;
@@ -78,7 +85,7 @@ void cfree(T *&p) {
 }
 
 size_t swarm_bytes_per_buf(int cap) {
-  return (size_t)cap * (10 * sizeof(double) + sizeof(long long) + sizeof(int) + 1) + 16 * 256;
+  return (size_t)cap * (10 * sizeof(double) + 7 * sizeof(float) + sizeof(long long) + sizeof(int) + 1) + 24 * 256;
 }
 
 void carve_swarm(char *p, int cap, SwarmBuf &b) {
@@ -91,6 +98,9 @@ void carve_swarm(char *p, int cap, SwarmBuf &b) {
   b.u = (double *)take(8ull * cap); b.v = (double *)take(8ull * cap); b.w = (double *)take(8ull * cap);
   b.a1 = (double *)take(8ull * cap); b.a2 = (double *)take(8ull * cap); b.a3 = (double *)take(8ull * cap);
   b.P = (double *)take(8ull * cap);
+  b.uf = (float *)take(4ull * cap); b.vf = (float *)take(4ull * cap); b.wf = (float *)take(4ull * cap);
+  b.a1f = (float *)take(4ull * cap); b.a2f = (float *)take(4ull * cap); b.a3f = (float *)take(4ull * cap);
+  b.Pf = (float *)take(4ull * cap);
   b.pid = (long long *)take(8ull * cap);
   b.cell = (int *)take(4ull * cap);
   b.status = (unsigned char *)take((size_t)cap);
@@ -134,6 +144,7 @@ int fdf_ContextCreate(FdfContext **out, int device) {
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->cnt, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMemset(ctx->cnt, 0, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->bbox, 6 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->fbox, 16 * sizeof(float));
   if (e != cudaSuccess) {
     fdf_ContextDestroy(ctx);
     return FDF_ERR_GPU;
@@ -148,6 +159,8 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner); cfree(ctx->bbox);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk);
+  cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
+  cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
   cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
   cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
@@ -173,6 +186,8 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk); cfree(ctx->cell_start);
   cfree(ctx->cursor); cfree(ctx->scan_sums);
+  cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
+  cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32);
   GridDims g{};
   g.IM = (int)IM; g.JM = (int)JM; g.KM = (int)KM; g.Nc = Nc; g.Nn = Nn;
   g.fIM.init((unsigned)IM); g.fJM.init((unsigned)JM); g.fMX.init((unsigned)(IM + 1)); g.fMY.init((unsigned)(JM + 1));
@@ -187,6 +202,15 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   CU(cudaMalloc((void **)&ctx->fi, 8ull * nfi));
   CU(cudaMalloc((void **)&ctx->fj, 8ull * nfj));
   CU(cudaMalloc((void **)&ctx->fk, 8ull * nfk));
+  CU(cudaMalloc((void **)&ctx->table32, 4ull * FDF_ROW32 * Nc));
+  CU(cudaMalloc((void **)&ctx->ucat32, 12ull * Nc));
+  CU(cudaMalloc((void **)&ctx->corner32, 12ull * Nn));
+  CU(cudaMalloc((void **)&ctx->count32, 4ull * Nn));
+  CU(cudaMalloc((void **)&ctx->avg32, 4ull * Nn));
+  CU(cudaMalloc((void **)&ctx->fi32, 4ull * nfi));
+  CU(cudaMalloc((void **)&ctx->fj32, 4ull * nfj));
+  CU(cudaMalloc((void **)&ctx->fk32, 4ull * nfk));
+  CU(cudaMemsetAsync(ctx->ucat32, 0, 12ull * Nc, ctx->stream));
   CU(cudaMalloc((void **)&ctx->cell_start, 4ull * (Nc + 2)));
   CU(cudaMalloc((void **)&ctx->cursor, 4ull * (Nc + 1)));
   CU(cudaMalloc((void **)&ctx->scan_sums, 4ull * scan_scratch_words(Nc + 2)));
@@ -197,6 +221,9 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   unsigned int *err = nullptr;
   launch_build_planes(ctx->coor, g, ctx->planes, err, ctx->stream);
   CHECK_LAUNCH();
+  launch_build_table32(ctx->planes, ctx->coor, g, ctx->table32, ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
   ctx->launches += 1;
   // ComputeLocalBoundingBox (grid.c:762-883) on one rank: min/max over every node,
   // widened by 1e-6 -- done on the host, which holds the coordinates.
@@ -211,6 +238,19 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   for (int c = 0; c < 3; ++c) { bb[c] = bb[c] - FDF_BBOX_TOL; bb[3 + c] = bb[3 + c] + FDF_BBOX_TOL; }
   memcpy(ctx->bbox_h, bb, sizeof(bb));
   CU(cudaMemcpyAsync(ctx->bbox, bb, sizeof(bb), cudaMemcpyHostToDevice, ctx->stream));
+  // the precision form's FP32 "surely inside" box: any (hi, lo) position with hi strictly
+  // inside it lies in [bmin, bmax], because |lo| <= 2^-24 |hi| < margin
+  float fb[16] = {0};
+  for (int c = 0; c < 3; ++c) {
+    const double margin = 0x1p-20 * (std::fabs(bb[c]) + std::fabs(bb[3 + c]) + 1.0);
+    const double lo = bb[c] + margin, hi = bb[3 + c] - margin;
+    float flo = (float)lo, fhi = (float)hi;
+    if ((double)flo < lo) flo = std::nextafter(flo, INFINITY);
+    if ((double)fhi > hi) fhi = std::nextafter(fhi, -INFINITY);
+    fb[c] = flo;
+    fb[4 + c] = fhi;
+  }
+  CU(cudaMemcpyAsync(ctx->fbox, fb, sizeof(fb), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->sentinel = (unsigned int)Nc;
   ctx->has_grid = true;
@@ -235,8 +275,19 @@ int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized) {
       }
   CU(cudaSetDevice(ctx->device));
   CU(cudaMemcpyAsync(ctx->ucat, soa.data(), 24ull * g.Nc, cudaMemcpyHostToDevice, ctx->stream));
+  launch_f64_to_f32(ctx->ucat, ctx->ucat32, 3 * g.Nc, ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->has_ucat = true;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetForm(FdfContext *ctx, int form) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (form != FDF_FORM_PLAIN_FP64 && form != FDF_FORM_FP32)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetForm: unknown form");
+  ctx->form = form;
   return FDF_SUCCESS;
 }
 
@@ -299,7 +350,10 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
     CU(cudaMemcpyAsync(d_pid, pid, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
     CU(cudaMemcpyAsync(d_st, status, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
     ctx->cur = 0;
-    launch_swarm_from_aos(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
+    if (ctx->form == FDF_FORM_FP32)
+      launch_swarm_from_aos32(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
+    else
+      launch_swarm_from_aos(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
     CHECK_LAUNCH();
     ctx->launches += 1;
   }
@@ -310,6 +364,7 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->cur = 0;
   ctx->swarm_set = true;
+  ctx->swarm_form = ctx->form;
   return FDF_SUCCESS;
 }
 
@@ -337,8 +392,12 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *positio
   char *st = (char *)ctx->staging;
   double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
-  launch_swarm_to_aos(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
-                      ctx->stream);
+  if (ctx->swarm_form == FDF_FORM_FP32)
+    launch_swarm_to_aos32(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
+                          ctx->stream);
+  else
+    launch_swarm_to_aos(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
+                        ctx->stream);
   CHECK_LAUNCH();
   ctx->launches += 1;
   CU(cudaMemcpyAsync(position, d_pos, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
@@ -356,6 +415,11 @@ int fdf_GetScatteredFields(FdfContext *ctx, double *count, double *P_avg) {
   if (!ctx || !count || !P_avg) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetScatteredFields: null argument");
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetScatteredFields: no grid");
   CU(cudaSetDevice(ctx->device));
+  if (ctx->out_form == FDF_FORM_FP32) {
+    launch_f32_to_f64(ctx->count32, ctx->count, ctx->g.Nn, ctx->stream);
+    launch_f32_to_f64(ctx->avg32, ctx->avg, ctx->g.Nn, ctx->stream);
+    CHECK_LAUNCH();
+  }
   CU(cudaMemcpyAsync(count, ctx->count, 8ull * ctx->g.Nn, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaMemcpyAsync(P_avg, ctx->avg, 8ull * ctx->g.Nn, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -387,6 +451,12 @@ int fdf_GetFaceDeposits(FdfContext *ctx, double *fi, double *fj, double *fk) {
   const GridDims &g = ctx->g;
   long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM, nfk = (long long)g.IM * g.JM * (g.KM + 1LL);
   CU(cudaSetDevice(ctx->device));
+  if (ctx->out_form == FDF_FORM_FP32) {
+    launch_f32_to_f64(ctx->fi32, ctx->fi, nfi, ctx->stream);
+    launch_f32_to_f64(ctx->fj32, ctx->fj, nfj, ctx->stream);
+    launch_f32_to_f64(ctx->fk32, ctx->fk, nfk, ctx->stream);
+    CHECK_LAUNCH();
+  }
   CU(cudaMemcpyAsync(fi, ctx->fi, 8ull * nfi, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaMemcpyAsync(fj, ctx->fj, 8ull * nfj, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaMemcpyAsync(fk, ctx->fk, 8ull * nfk, cudaMemcpyDeviceToHost, ctx->stream));
@@ -417,16 +487,24 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   const bool prof = ctx->profiling;
   SwarmBuf &src = ctx->buf[ctx->cur];
   SwarmBuf &dst = ctx->buf[1 - ctx->cur];
+  const bool f32 = ctx->swarm_form == FDF_FORM_FP32;
   size_t e0 = prof ? record_event(ctx, s) : 0;
-  launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys,
-                ctx->cell_start, ctx->sentinel, s);
+  if (f32)
+    launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
+                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, s);
+  else
+    launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys,
+                  ctx->cell_start, ctx->sentinel, s);
   size_t e1 = prof ? record_event(ctx, s) : 0;
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
   // the corner field needs only cell_start: compute it beside the slot assignment
   CU(cudaEventRecord(ctx->ev_scan, s));
   CU(cudaStreamWaitEvent(ctx->side, ctx->ev_scan, 0));
   size_t c0 = prof ? record_event(ctx, ctx->side) : 0;
-  launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->side);
+  if (f32)   // FP32 arithmetic is cheap: every node, no occupancy test
+    launch_center_to_corner32(ctx->ucat32, g, ctx->corner32, nullptr, nullptr, ctx->side);
+  else
+    launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->side);
   size_t c1 = prof ? record_event(ctx, ctx->side) : 0;
   CU(cudaEventRecord(ctx->ev_corner, ctx->side));
   launch_scatter_slots(ctx->keys, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start, ctx->cursor,
@@ -435,9 +513,17 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   size_t e2 = prof ? record_event(ctx, s) : 0;
   CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
   size_t e3 = prof ? record_event(ctx, s) : 0;
-  launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s);
+  if (f32)
+    launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s);
+  else
+    launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s);
   size_t e4 = prof ? record_event(ctx, s) : 0;
-  launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, s);
+  if (f32)
+    launch_deposit32(dst, g, ctx->cell_start, ctx->volume, ctx->count32, ctx->avg32, ctx->fi32, ctx->fj32, ctx->fk32,
+                     s);
+  else
+    launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, s);
+  ctx->out_form = ctx->swarm_form;
   size_t e5 = prof ? record_event(ctx, s) : 0;
   if (prof) {
     ctx->ev_spans.push_back({STAGE_LOCATE, {e0, e1}});
@@ -459,6 +545,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     info->removed_lost = (int64_t)c.removed_lost;
     info->removed_oob = (int64_t)c.removed_oob;
     info->walk_evals = (int64_t)c.evals;
+    info->fp64_fallbacks = (int64_t)c.fallbacks;
     if (c.err & ERRBIT_DEGENERATE)
       return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
   }

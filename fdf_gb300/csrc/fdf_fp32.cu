@@ -1,0 +1,539 @@
+// fdf_fp32.cu -- the precision form: interpolation, advection and deposition in FP32,
+// cell location decided exactly as the FP64 reference walk decides it.
+//
+// Positions.  The form holds each coordinate as a float pair (hi, lo) with |lo| <=
+// ulp(hi)/2; the form's position is the exact sum hi + lo (a double).  Advection adds
+// the FP32 displacement fl32(u * dt) by double-float addition (FP32 operations only).
+// Uploads split the caller's FP64 position (an error of at most 2^-48 |p|); downloads
+// return hi + lo exactly.
+//
+// Walk.  Each face class the walk needs -- d < 0, d == 0 (|d| < thr), d > 0 -- is
+// decided from an FP32 signed distance when that is provably the FP64 class for the
+// form's position, and from the exact FP64 distance (the plain path's plane table)
+// otherwise.  With c0 = c0h + c0l the cell's first vertex as a float pair (exact),
+// fcr = fl32(fc - c0), pr = fl32(fl32(ph - c0h) + fl32(pl - c0l)), n32 = fl32(n) and
+// d32 = (fcr - pr) . n32 (FP32, fused), every rounding is bounded by u32 = 2^-24 times
+// the magnitudes involved:
+//     |pr_i - (p_i - c0_i)| <= u32 (2 B_i + 2 u32 (|ph_i| + |c0h_i|)),  B_i = |p_i - c0_i|
+//     |d32 - d64| <= 7.001 u32 S,   S = sum_i (A_i + B_i + u32 (|ph_i| + |c0h_i|)) |n_i|
+// with A_i = |fc_i - c0_i| (d64 is the reference's FP64 value; its own error is
+// ~1e-16 S).  The kernel uses E = 12 u32 S32 (S32, the FP32 estimate of S, is within
+// 8 u32 of S) and M = fl32(E + thr32) with thr32 >= thr (1 + 2^-22) rounded up, and
+// classifies
+//     d32 > M -> d64 >= thr (positive);  d32 < -M -> d64 <= -thr (negative);
+// anything else (including NaN) falls back to the exact FP64 distance of that face.
+// The cells, statuses and walk paths are therefore the reference's for the form's own
+// positions.  Fallbacks are counted.  The hot loop issues no FP64 instruction.
+//
+// Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32), c0l (3 x f32),
+// degenerate flag (u32), then per face LEFT..BACK: fcr (3 x f32), n32 (3 x f32).
+#include "fdf_internal.cuh"
+#include "fdf_exact.cuh"
+
+namespace {
+
+using fdfx::add;
+using fdfx::mul;
+using fdfx::sub;
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void k_build_table32(const double *__restrict__ planes, const double *__restrict__ coor, GridDims g,
+                                float *__restrict__ table) {
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= g.Nc) return;
+  int i, j, k;
+  cell_ijk(g, (unsigned int)c, i, j, k);
+  const double *v0 = coor + 3 * (((long long)k * (g.JM + 1) + j) * (long long)(g.IM + 1) + i);
+  const double *row = planes + c * FDF_ROW;
+  float *t = table + c * FDF_ROW32;
+  double c0[3];
+  for (int q = 0; q < 3; ++q) {
+    const float h = __double2float_rn(v0[q]);
+    const float l = __double2float_rn(sub(v0[q], (double)h));
+    t[q] = h;
+    t[4 + q] = l;
+    c0[q] = add((double)h, (double)l);   // exact: the pair's value
+  }
+  const double thr = row[36];
+  // rounded up with a little headroom: thr32 * (1 - 2^-24) >= thr, which the error bound uses
+  t[3] = __double2float_ru(mul(thr, 1.0 + 0x1p-22));
+  reinterpret_cast<unsigned int *>(t)[7] = (fdfx::ubits(row[37]) != 0ULL) ? 1u : 0u;
+  for (int f = 0; f < 6; ++f) {
+    const double *p = row + 6 * f;
+    float *o = t + 8 + 6 * f;
+    o[0] = __double2float_rn(sub(p[0], c0[0]));
+    o[1] = __double2float_rn(sub(p[1], c0[1]));
+    o[2] = __double2float_rn(sub(p[2], c0[2]));
+    o[3] = __double2float_rn(p[3]);
+    o[4] = __double2float_rn(p[4]);
+    o[5] = __double2float_rn(p[5]);
+  }
+}
+
+// (hi, lo) float pair held in a double slot of the swarm arrays
+__device__ __forceinline__ float2 ld_pair(const double *a, int s) {
+  return *reinterpret_cast<const float2 *>(a + s);
+}
+__device__ __forceinline__ void st_pair(double *a, int s, float2 v) { *reinterpret_cast<float2 *>(a + s) = v; }
+
+// (hi, lo) + v for a float v (double-float addition, FP32 operations only).
+__device__ __forceinline__ float2 pair_add(float2 p, float v) {
+  const float sh = __fadd_rn(p.x, v);
+  const float bv = __fsub_rn(sh, p.x);
+  const float e = __fadd_rn(__fsub_rn(p.x, __fsub_rn(sh, bv)), __fsub_rn(v, bv));   // exact error of p.x + v
+  const float t = __fadd_rn(p.y, e);
+  const float h = __fadd_rn(sh, t);
+  return make_float2(h, __fsub_rn(t, __fsub_rn(h, sh)));
+}
+
+__device__ __forceinline__ double pair_value(float2 p) { return __dadd_rn((double)p.x, (double)p.y); }
+
+// Exact FP64 signed distance of face f (the plain path's arithmetic), thresholded.
+__device__ __forceinline__ double exact_face(const double *__restrict__ row64, int f, double x, double y, double z) {
+  const double2 *r = reinterpret_cast<const double2 *>(row64);
+  double2 p0 = __ldg(r + 3 * f), p1 = __ldg(r + 3 * f + 1), p2 = __ldg(r + 3 * f + 2);
+  double2 tf = __ldg(r + 18);
+  double dd = add(add(mul(sub(p0.x, x), p1.y), mul(sub(p0.y, y), p2.x)), mul(sub(p1.x, z), p2.y));
+  if (fdfx::abs_lt_bits(dd, fdfx::ubits(tf.x), fdfx::is_nan(tf.x))) dd = 0.0;
+  return dd;
+}
+
+__global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
+                                                  const double *__restrict__ planes, float dt32, int advect,
+                                                  int reset_first, const double *__restrict__ bbox,
+                                                  const float *__restrict__ fbox, int drop_removed,
+                                                  DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                  unsigned int *__restrict__ count, unsigned int sentinel) {
+  const int n = cnt->n_sorted;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
+  unsigned long long my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0, my_fb = 0;
+  unsigned int my_err = 0;
+  unsigned int hkey = 0xffffffffu;
+  if (s < n) {
+    float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
+    if (advect) {   // FP32 displacement added to the (hi, lo) position
+      px = pair_add(px, __fmul_rn(b.uf[s], dt32));
+      py = pair_add(py, __fmul_rn(b.vf[s], dt32));
+      pz = pair_add(pz, __fmul_rn(b.wf[s], dt32));
+      st_pair(b.x, s, px); st_pair(b.y, s, py); st_pair(b.z, s, pz);
+    }
+    unsigned char st = b.status[s];
+    if (reset_first && st == ST_ACTIVE_AND_LOCATED) st = ST_NEEDS_LOCATION;
+    int cell = b.cell[s];
+    bool lost = false;
+    if (st != ST_ACTIVE_AND_LOCATED) {
+      int i = 0, j = 0, k = 0;
+      if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, i, j, k);
+      int steps = 0, evaluated = 0;
+      bool concluded = false, cycle = false;
+      long long saved = -1;
+      int power = 1, lam = 0;
+      float dv[6];       // distances used for the weights
+      bool negf[6];
+      const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
+      while (!concluded && steps < FDF_MAX_TRAVERSAL) {
+        ++steps;
+        if (i < 0 || i >= g.IM || j < 0 || j >= g.JM || k < 0 || k >= g.KM) { lost = true; break; }
+        const long long cur = ((long long)k * g.JM + j) * g.IM + i;
+        if (cur == saved) { cycle = true; lost = true; break; }
+        if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
+        const float4 *row = reinterpret_cast<const float4 *>(table + cur * FDF_ROW32);
+        const float4 h0 = __ldg(row), h1 = __ldg(row + 1);
+        const float thr32 = h0.w;
+        if (__float_as_uint(h1.w) != 0u) { my_err |= ERRBIT_DEGENERATE; lost = true; break; }
+        ++evaluated;
+        const float prx = __fadd_rn(__fsub_rn(px.x, h0.x), __fsub_rn(px.y, h1.x));
+        const float pry = __fadd_rn(__fsub_rn(py.x, h0.y), __fsub_rn(py.y, h1.y));
+        const float prz = __fadd_rn(__fsub_rn(pz.x, h0.z), __fsub_rn(pz.y, h1.z));
+        // the split term u32 (|ph| + |c0h|) of the bound, per component
+        const float ex = __fmul_rn(__fadd_rn(sx, fabsf(h0.x)), 5.9604644775390625e-8f);
+        const float ey = __fmul_rn(__fadd_rn(sy, fabsf(h0.y)), 5.9604644775390625e-8f);
+        const float ez = __fmul_rn(__fadd_rn(sz, fabsf(h0.z)), 5.9604644775390625e-8f);
+        float fr[36];   // per face: fcr (3), n32 (3); nine 16-B loads
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+          const float4 v = __ldg(row + 2 + q);
+          fr[4 * q] = v.x; fr[4 * q + 1] = v.y; fr[4 * q + 2] = v.z; fr[4 * q + 3] = v.w;
+        }
+        bool neg = false, zero = false;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+          const float fx = fr[6 * f], fy = fr[6 * f + 1], fz = fr[6 * f + 2];
+          const float nx = fr[6 * f + 3], ny = fr[6 * f + 4], nz = fr[6 * f + 5];
+          const float tx = __fsub_rn(fx, prx), ty = __fsub_rn(fy, pry), tz = __fsub_rn(fz, prz);
+          const float d32 = __fmaf_rn(tz, nz, __fmaf_rn(ty, ny, __fmul_rn(tx, nx)));
+          const float S = __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fz), fabsf(prz)), ez), fabsf(nz),
+                                    __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fy), fabsf(pry)), ey), fabsf(ny),
+                                              __fmul_rn(__fadd_rn(__fadd_rn(fabsf(fx), fabsf(prx)), ex),
+                                                        fabsf(nx))));
+          const float M = __fadd_rn(__fmul_rn(S, 12.0f * 5.9604644775390625e-8f), thr32);
+          bool ng, zr;
+          float dval;
+          if (d32 > M) {
+            ng = false; zr = false; dval = d32;
+          } else if (d32 < -M) {
+            ng = true; zr = false; dval = d32;
+          } else {
+            const double d64 = exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py),
+                                          pair_value(pz));
+            ng = fdfx::lt0(d64);
+            zr = fdfx::eq0(d64);
+            dval = __double2float_rn(d64);
+            ++my_fb;
+          }
+          negf[f] = ng;
+          dv[f] = dval;
+          neg |= ng;
+          zero |= zr;
+        }
+        if (!neg || zero) {
+          concluded = true;
+        } else {
+          if (negf[F_FRONT]) k += 1; else if (negf[F_BACK]) k -= 1;
+          if (negf[F_LEFT]) i -= 1; else if (negf[F_RIGHT]) i += 1;
+          if (negf[F_BOTTOM]) j -= 1; else if (negf[F_TOP]) j += 1;
+        }
+      }
+      my_evals = (unsigned long long)(cycle ? FDF_MAX_TRAVERSAL : steps);
+      my_done = (unsigned long long)evaluated;
+      if (lost || !concluded) {
+        lost = true;
+        cell = -1;
+        st = ST_LOST;
+      } else {
+        // UpdateParticleWeights in FP32 (clamp d <= 1e-14, then the three ratios)
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+          if (!(dv[f] > 1e-14f)) dv[f] = (dv[f] != dv[f]) ? dv[f] : 1e-14f;
+        b.a1f[s] = __fdiv_rn(dv[F_LEFT], __fadd_rn(dv[F_LEFT], dv[F_RIGHT]));
+        b.a2f[s] = __fdiv_rn(dv[F_BOTTOM], __fadd_rn(dv[F_BOTTOM], dv[F_TOP]));
+        b.a3f[s] = __fdiv_rn(dv[F_BACK], __fadd_rn(dv[F_FRONT], dv[F_BACK]));
+        cell = (int)(((long long)k * g.JM + j) * g.IM + i);
+        st = ST_ACTIVE_AND_LOCATED;
+      }
+      b.cell[s] = cell;
+      b.status[s] = st;
+    } else {
+      lost = (cell < 0);
+    }
+    unsigned int key = lost ? sentinel : (unsigned int)cell;
+    if (lost) my_lost_total = 1;
+    if (drop_removed) {
+      if (lost) {
+        my_lost = 1;
+      } else {
+        // IsParticleInBox on the form's position: decided in FP32 when the hi parts are
+        // clear of the box faces by more than the lo parts and rounding can move them
+        // (fbox = the box rounded outwards/inwards), exactly in FP64 otherwise.
+        const float4 fb0 = *reinterpret_cast<const float4 *>(fbox), fb1 = *reinterpret_cast<const float4 *>(fbox + 4);
+        const float4 fb2 = *reinterpret_cast<const float4 *>(fbox + 8);
+        // fb0 = (lo_in x, y, z, -), fb1 = (hi_in x, y, z, -): strictly inside; fb2 = margin scale
+        const bool surely_in = px.x > fb0.x && px.x < fb1.x && py.x > fb0.y && py.x < fb1.y && pz.x > fb0.z &&
+                               pz.x < fb1.z;
+        bool inside = surely_in;
+        if (!surely_in) {
+          const double x = pair_value(px), y = pair_value(py), z = pair_value(pz);
+          inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
+        }
+        (void)fb2;
+        if (!inside) { my_oob = 1; key = sentinel; }
+      }
+    }
+    keys[s] = key;
+    if (key < sentinel) hkey = key;
+    else if (!drop_removed) hkey = sentinel;
+  }
+  {
+    const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
+    const int lane = threadIdx.x & 31;
+    if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
+  }
+  my_lost = warp_sum_u64(my_lost);
+  my_oob = warp_sum_u64(my_oob);
+  my_evals = warp_sum_u64(my_evals);
+  my_done = warp_sum_u64(my_done);
+  my_lost_total = warp_sum_u64(my_lost_total);
+  my_fb = warp_sum_u64(my_fb);
+  my_err = __reduce_or_sync(0xffffffffu, my_err);
+  if ((threadIdx.x & 31) == 0) {
+    if (my_lost) atomicAdd(&cnt->removed_lost, my_lost);
+    if (my_oob) atomicAdd(&cnt->removed_oob, my_oob);
+    if (my_evals) atomicAdd(&cnt->evals, my_evals);
+    if (my_done) atomicAdd(&cnt->evals_total, my_done);
+    if (my_lost_total) atomicAdd(&cnt->lost_total, my_lost_total);
+    if (my_fb) { atomicAdd(&cnt->fallbacks, my_fb); atomicAdd(&cnt->fallbacks_total, my_fb); }
+    if (my_err) atomicOr(&cnt->err, my_err);
+  }
+}
+
+// Corner field in FP32: mean of the valid adjacent cells (nodes next to occupied cells).
+__global__ void k_center_to_corner32(const float *__restrict__ ucat, GridDims g, float *__restrict__ corner,
+                                     const unsigned int *__restrict__ cell_start, unsigned long long *nodes_done) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool work = q < g.Nn;
+  int i = 0, j = 0, k = 0;
+  if (work) node_ijk(g, (unsigned int)q, i, j, k);
+  if (cell_start) {
+    bool need = false;
+    if (work)
+      for (int dk = -1; dk <= 0 && !need; ++dk)
+        for (int dj = -1; dj <= 0 && !need; ++dj)
+          for (int di = -1; di <= 0 && !need; ++di) {
+            int ck = k + dk, cj = j + dj, ci = i + di;
+            if (ci < 0 || ci >= g.IM || cj < 0 || cj >= g.JM || ck < 0 || ck >= g.KM) continue;
+            long long c = ((long long)ck * g.JM + cj) * g.IM + ci;
+            need = __ldg(cell_start + c + 1) > __ldg(cell_start + c);
+          }
+    unsigned int bal = __ballot_sync(0xffffffffu, need);
+    if (nodes_done && (threadIdx.x & 31) == 0 && bal) atomicAdd(nodes_done, (unsigned long long)__popc(bal));
+    if (!need) return;
+  }
+  if (!work) return;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  int count = 0;
+#pragma unroll
+  for (int dk = -1; dk <= 0; ++dk)
+#pragma unroll
+    for (int dj = -1; dj <= 0; ++dj)
+#pragma unroll
+      for (int di = -1; di <= 0; ++di) {
+        const int ck = k + dk, cj = j + dj, ci = i + di;
+        if (ci < 0 || ci >= g.IM || cj < 0 || cj >= g.JM || ck < 0 || ck >= g.KM) continue;
+        const long long c = ((long long)ck * g.JM + cj) * g.IM + ci;
+        sx += __ldg(ucat + c); sy += __ldg(ucat + g.Nc + c); sz += __ldg(ucat + 2 * g.Nc + c);
+        ++count;
+      }
+  const float r = count == 8 ? 0.125f : count == 4 ? 0.25f : count == 2 ? 0.5f : count == 1 ? 1.0f : 0.0f;
+  corner[q] = sx * r; corner[g.Nn + q] = sy * r; corner[2 * g.Nn + q] = sz * r;
+}
+
+__global__ void __launch_bounds__(256) k_gather_interp32(SwarmBuf src, SwarmBuf dst, GridDims g,
+                                                         const float *__restrict__ corner,
+                                                         const unsigned int *__restrict__ perm,
+                                                         const unsigned int *__restrict__ cell_start,
+                                                         DevCounters *cnt) {
+  const int n = (int)cell_start[g.Nc + 1];
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {
+    cnt->n = (int)cell_start[g.Nc];
+    cnt->n_sorted = n;
+  }
+  if (s >= n) return;
+  const unsigned int p = perm[s];
+  const int cell = src.cell[p];
+  float a1 = src.a1f[p], a2 = src.a2f[p], a3 = src.a3f[p];
+  dst.x[s] = src.x[p]; dst.y[s] = src.y[p]; dst.z[s] = src.z[p];
+  dst.a1f[s] = a1; dst.a2f[s] = a2; dst.a3f[s] = a3;
+  dst.Pf[s] = src.Pf[p];
+  dst.pid[s] = src.pid[p];
+  float ux = 0.f, uy = 0.f, uz = 0.f;
+  if (cell < 0) {
+    dst.cell[s] = -1;
+    dst.status[s] = ST_LOST;
+  } else {
+    dst.cell[s] = cell;
+    dst.status[s] = ST_ACTIVE_AND_LOCATED;
+    int i, j, k;
+    cell_ijk(g, (unsigned int)cell, i, j, k);
+    a1 = fminf(fmaxf(a1, 0.f), 1.f);   // NaN -> 0 as PetscMax(0, PetscMin(1, NaN))
+    a2 = fminf(fmaxf(a2, 0.f), 1.f);
+    a3 = fminf(fmaxf(a3, 0.f), 1.f);
+    const float oa1 = 1.f - a1, oa2 = 1.f - a2, oa3 = 1.f - a3;
+    const float p00 = oa1 * oa2, p10 = a1 * oa2, p01 = oa1 * a2, p11 = a1 * a2;
+    const float w[8] = {p00 * oa3, p10 * oa3, p01 * oa3, p11 * oa3, p00 * a3, p10 * a3, p01 * a3, p11 * a3};
+    const long long mx = g.IM + 1, my = g.JM + 1;
+    const long long q0 = ((long long)k * my + j) * mx + i;
+    const long long off[8] = {0, 1, mx, mx + 1, mx * my, mx * my + 1, mx * my + mx, mx * my + mx + 1};
+    float sw = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const long long q = q0 + off[c];
+      ax = fmaf(w[c], __ldg(corner + q), ax);
+      ay = fmaf(w[c], __ldg(corner + g.Nn + q), ay);
+      az = fmaf(w[c], __ldg(corner + 2 * g.Nn + q), az);
+      sw += w[c];
+    }
+    if (sw > 1.0e-14f) { ux = ax / sw; uy = ay / sw; uz = az / sw; }
+  }
+  dst.uf[s] = ux; dst.vf[s] = uy; dst.wf[s] = uz;
+}
+
+// Neumaier-compensated running sum.
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    float t = s + v;
+    if (fabsf(s) >= fabsf(v)) c += (s - t) + v; else c += (v - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return s + c; }
+};
+
+__global__ void __launch_bounds__(256) k_deposit32(SwarmBuf b, GridDims g, const unsigned int *__restrict__ cs,
+                                                   float third, float *__restrict__ count, float *__restrict__ avg,
+                                                   float *__restrict__ fi, float *__restrict__ fj,
+                                                   float *__restrict__ fk) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= g.Nn) return;
+  const int IM = g.IM, JM = g.JM, KM = g.KM;
+  int i, j, k;
+  node_ijk(g, (unsigned int)q, i, j, k);
+  const bool is_cell = i < IM && j < JM && k < KM;
+  const long long c = ((long long)k * JM + j) * IM + i;
+  int s0 = 0, s1 = 0;
+  if (is_cell) { s0 = (int)__ldg(cs + c); s1 = (int)__ldg(cs + c + 1); }
+  {
+    KSum sum;
+    for (int s = s0; s < s1; ++s) sum.add(__ldg(b.Pf + s));
+    const int nc = s1 - s0;
+    count[q] = (float)nc;
+    avg[q] = nc > 0 ? sum.value() / (float)nc : 0.f;
+  }
+  if (j < JM && k < KM) {
+    KSum acc;
+    if (i > 0) {
+      const long long cl = c - 1;
+      const int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
+      for (int s = l0; s < l1; ++s) acc.add(__ldg(b.a1f + s) * third);
+    }
+    if (i < IM)
+      for (int s = s0; s < s1; ++s) acc.add((1.f - __ldg(b.a1f + s)) * third);
+    fi[((long long)k * JM + j) * (IM + 1) + i] = acc.value();
+  }
+  if (i < IM && k < KM) {
+    KSum acc;
+    if (j > 0) {
+      const long long cl = ((long long)k * JM + (j - 1)) * IM + i;
+      const int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
+      for (int s = l0; s < l1; ++s) acc.add(__ldg(b.a2f + s) * third);
+    }
+    if (j < JM)
+      for (int s = s0; s < s1; ++s) acc.add((1.f - __ldg(b.a2f + s)) * third);
+    fj[((long long)k * (JM + 1) + j) * IM + i] = acc.value();
+  }
+  if (i < IM && j < JM) {
+    KSum acc;
+    if (k > 0) {
+      const long long cl = ((long long)(k - 1) * JM + j) * IM + i;
+      const int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
+      for (int s = l0; s < l1; ++s) acc.add(__ldg(b.a3f + s) * third);
+    }
+    if (k < KM)
+      for (int s = s0; s < s1; ++s) acc.add((1.f - __ldg(b.a3f + s)) * third);
+    fk[c] = acc.value();
+  }
+}
+
+__global__ void k_from_aos32(const double *__restrict__ pos, const double *__restrict__ vel,
+                             const double *__restrict__ wgt, const double *__restrict__ P,
+                             const long long *__restrict__ cell3, const long long *__restrict__ pid,
+                             const long long *__restrict__ status, int n, GridDims g, SwarmBuf b) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  for (int q = 0; q < 3; ++q) {
+    const double v = pos[3 * p + q];
+    const float h = __double2float_rn(v);
+    const float l = __double2float_rn(__dsub_rn(v, (double)h));
+    st_pair(q == 0 ? b.x : q == 1 ? b.y : b.z, p, make_float2(h, l));
+  }
+  b.uf[p] = (float)vel[3 * p]; b.vf[p] = (float)vel[3 * p + 1]; b.wf[p] = (float)vel[3 * p + 2];
+  b.a1f[p] = (float)wgt[3 * p]; b.a2f[p] = (float)wgt[3 * p + 1]; b.a3f[p] = (float)wgt[3 * p + 2];
+  b.Pf[p] = (float)P[p];
+  b.pid[p] = pid[p];
+  const long long i = cell3[3 * p], j = cell3[3 * p + 1], k = cell3[3 * p + 2];
+  int c = -1;
+  if (i >= 0 && i < g.IM && j >= 0 && j < g.JM && k >= 0 && k < g.KM) c = (int)((k * g.JM + j) * g.IM + i);
+  b.cell[p] = c;
+  const long long st = status[p];
+  b.status[p] = (unsigned char)((st >= 0 && st <= ST_UNINITIALIZED) ? st : ST_UNINITIALIZED);
+}
+
+__global__ void k_to_aos32(SwarmBuf b, int n, GridDims g, double *__restrict__ pos, double *__restrict__ vel,
+                           double *__restrict__ wgt, double *__restrict__ P, long long *__restrict__ cell3,
+                           long long *__restrict__ pid, long long *__restrict__ status) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  pos[3 * p] = pair_value(ld_pair(b.x, p));
+  pos[3 * p + 1] = pair_value(ld_pair(b.y, p));
+  pos[3 * p + 2] = pair_value(ld_pair(b.z, p));
+  vel[3 * p] = b.uf[p]; vel[3 * p + 1] = b.vf[p]; vel[3 * p + 2] = b.wf[p];
+  wgt[3 * p] = b.a1f[p]; wgt[3 * p + 1] = b.a2f[p]; wgt[3 * p + 2] = b.a3f[p];
+  P[p] = b.Pf[p];
+  pid[p] = b.pid[p];
+  const int c = b.cell[p];
+  if (c >= 0) {
+    int i, j, k;
+    cell_ijk(g, (unsigned int)c, i, j, k);
+    cell3[3 * p] = i; cell3[3 * p + 1] = j; cell3[3 * p + 2] = k;
+  } else {
+    cell3[3 * p] = -1; cell3[3 * p + 1] = -1; cell3[3 * p + 2] = -1;
+  }
+  status[p] = b.status[p];
+}
+
+__global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ out, long long n) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < n) out[q] = (float)in[q];
+}
+
+__global__ void k_f32_to_f64(const float *__restrict__ in, double *__restrict__ out, long long n) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < n) out[q] = (double)in[q];
+}
+
+inline unsigned int blocks_for(long long n, int th) { return (unsigned int)(n > 0 ? (n + th - 1) / th : 1); }
+
+}  // namespace
+
+void launch_build_table32(const double *planes, const double *coor, GridDims g, float *table, cudaStream_t s) {
+  k_build_table32<<<blocks_for(g.Nc, 128), 128, 0, s>>>(planes, coor, g, table);
+}
+
+void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
+                     int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
+                     unsigned int *keys, unsigned int *count, unsigned int sentinel, cudaStream_t s) {
+  k_locate32<<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox, fbox,
+                                                    drop_removed, cnt, keys, count, sentinel);
+}
+
+void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
+                               unsigned long long *nodes_done, cudaStream_t s) {
+  k_center_to_corner32<<<blocks_for(g.Nn, 256), 256, 0, s>>>(ucat, g, corner, cell_start, nodes_done);
+}
+
+void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,
+                            const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
+                            cudaStream_t s) {
+  k_gather_interp32<<<blocks_for(n_cap, 256), 256, 0, s>>>(src, dst, g, corner, perm, cell_start, cnt);
+}
+
+void launch_deposit32(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, float *count,
+                      float *avg, float *fi, float *fj, float *fk, cudaStream_t s) {
+  k_deposit32<<<blocks_for(g.Nn, 256), 256, 0, s>>>(b, g, cell_start, (float)(volume / 3.0), count, avg, fi, fj, fk);
+}
+
+void launch_swarm_from_aos32(const double *pos, const double *vel, const double *wgt, const double *P,
+                             const long long *cell3, const long long *pid, const long long *status, int n, GridDims g,
+                             const SwarmBuf &b, cudaStream_t s) {
+  if (n <= 0) return;
+  k_from_aos32<<<blocks_for(n, 256), 256, 0, s>>>(pos, vel, wgt, P, cell3, pid, status, n, g, b);
+}
+
+void launch_swarm_to_aos32(const SwarmBuf &b, int n, GridDims g, double *pos, double *vel, double *wgt, double *P,
+                           long long *cell3, long long *pid, long long *status, cudaStream_t s) {
+  if (n <= 0) return;
+  k_to_aos32<<<blocks_for(n, 256), 256, 0, s>>>(b, n, g, pos, vel, wgt, P, cell3, pid, status);
+}
+
+void launch_f64_to_f32(const double *in, float *out, long long n, cudaStream_t s) {
+  k_f64_to_f32<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
+}
+
+void launch_f32_to_f64(const float *in, double *out, long long n, cudaStream_t s) {
+  k_f32_to_f64<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
+}

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #define FDF_ROW 38            // doubles per plane-table row (36 plane values + thr + flag)
+#define FDF_ROW32 44          // floats per precision-form row (c0 as 3 doubles, thr32, flag, 36 face values)
 #define FDF_MAX_TRAVERSAL 1000
 #define FDF_DISTANCE_THRESHOLD 1e-11
 #define FDF_INTERP_DIST_TOL 1e-14
@@ -35,10 +36,13 @@ enum { ERRBIT_DEGENERATE = 1u, ERRBIT_BAD_CELL = 2u };
 
 // Counters kept on the device so that a step needs no host round trip.
 struct DevCounters {
+  // reset at the start of every pipeline run
   unsigned long long removed_lost;
   unsigned long long removed_oob;
   unsigned long long evals;        // walk evaluations the reference makes for this run (cycles count MAX_TRAVERSAL)
   unsigned long long lost_total;
+  unsigned long long fallbacks;    // precision form: faces decided by the exact FP64 distance
+  // kept across runs
   unsigned int err;
   unsigned int pad;
   int n;            // live particle count after the last removal
@@ -46,10 +50,13 @@ struct DevCounters {
   unsigned long long psteps_total;  // sum over steps of the particles at step start (never reset per step)
   unsigned long long evals_total;   // walk evaluations actually made, all pipeline runs (never reset per step)
   unsigned long long nodes_total;   // corner nodes computed by the steps (never reset per step)
+  unsigned long long fallbacks_total;
 };
 
 struct SwarmBuf {
-  double *x, *y, *z, *u, *v, *w, *a1, *a2, *a3, *P;
+  double *x, *y, *z;                         // positions (both forms)
+  double *u, *v, *w, *a1, *a2, *a3, *P;       // plain FP64 form
+  float *uf, *vf, *wf, *a1f, *a2f, *a3f, *Pf;  // precision form
   long long *pid;
   int *cell;
   unsigned char *status;
@@ -135,3 +142,25 @@ void launch_swarm_from_aos(const double *pos, const double *vel, const double *w
                            GridDims g, const SwarmBuf &b, cudaStream_t s);
 void launch_swarm_to_aos(const SwarmBuf &b, int n, GridDims g, double *pos, double *vel, double *wgt,
                          double *P, long long *cell3, long long *pid, long long *status, cudaStream_t s);
+
+// Precision form (fdf_fp32.cu).
+void launch_build_table32(const double *planes, const double *coor, GridDims g, float *table, cudaStream_t s);
+// fbox: 12 floats, (x, y, z, -) lower and (x, y, z, -) upper bounds strictly inside the
+// bounding box by more than any lo part of a position inside it, then 4 unused.
+void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
+                     int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
+                     unsigned int *keys, unsigned int *count, unsigned int sentinel, cudaStream_t s);
+void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
+                               unsigned long long *nodes_done, cudaStream_t s);
+void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,
+                            const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
+                            cudaStream_t s);
+void launch_deposit32(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, float *count,
+                      float *avg, float *fi, float *fj, float *fk, cudaStream_t s);
+void launch_swarm_from_aos32(const double *pos, const double *vel, const double *wgt, const double *P,
+                             const long long *cell3, const long long *pid, const long long *status, int n, GridDims g,
+                             const SwarmBuf &b, cudaStream_t s);
+void launch_swarm_to_aos32(const SwarmBuf &b, int n, GridDims g, double *pos, double *vel, double *wgt, double *P,
+                           long long *cell3, long long *pid, long long *status, cudaStream_t s);
+void launch_f64_to_f32(const double *in, float *out, long long n, cudaStream_t s);
+void launch_f32_to_f64(const float *in, double *out, long long n, cudaStream_t s);

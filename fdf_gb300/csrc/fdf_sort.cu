@@ -48,15 +48,29 @@ __device__ __forceinline__ unsigned int block_exclusive_scan(unsigned int v, uns
   return warp_prefix + x - v;
 }
 
+// Loads SCAN_ITEMS (= 8) consecutive values as two 16-B vectors when the block is
+// fully inside and the base is aligned, element by element otherwise.
+__device__ __forceinline__ void load8(const unsigned int *__restrict__ in, long long base, long long count,
+                                      unsigned int v[SCAN_ITEMS]) {
+  if (base + SCAN_ITEMS <= count && ((reinterpret_cast<size_t>(in + base) & 15) == 0)) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(in + base);
+    const uint4 b = *reinterpret_cast<const uint4 *>(in + base + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; ++q) v[q] = (base + q < count) ? in[base + q] : 0u;
+  }
+}
+
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const unsigned int *__restrict__ in, long long count,
                                                              unsigned int *__restrict__ sums) {
   long long base = (long long)blockIdx.x * SCAN_BLOCK + (long long)threadIdx.x * SCAN_ITEMS;
-  unsigned int v = 0;
+  unsigned int v[SCAN_ITEMS], t = 0;
+  load8(in, base, count, v);
 #pragma unroll
-  for (int q = 0; q < SCAN_ITEMS; ++q)
-    if (base + q < count) v += in[base + q];
+  for (int q = 0; q < SCAN_ITEMS; ++q) t += v[q];
   unsigned int tot;
-  block_exclusive_scan(v, &tot);
+  block_exclusive_scan(t, &tot);
   if (threadIdx.x == 0) sums[blockIdx.x] = tot;
 }
 
@@ -77,13 +91,20 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(unsigned int *__res
                                                             const unsigned int *__restrict__ sums) {
   long long base = (long long)blockIdx.x * SCAN_BLOCK + (long long)threadIdx.x * SCAN_ITEMS;
   unsigned int v[SCAN_ITEMS], t = 0;
+  load8(data, base, count, v);
 #pragma unroll
-  for (int q = 0; q < SCAN_ITEMS; ++q) { v[q] = (base + q < count) ? data[base + q] : 0u; t += v[q]; }
+  for (int q = 0; q < SCAN_ITEMS; ++q) t += v[q];
   unsigned int ex = block_exclusive_scan(t, nullptr) + sums[blockIdx.x];
+  unsigned int o[SCAN_ITEMS];
 #pragma unroll
-  for (int q = 0; q < SCAN_ITEMS; ++q) {
-    if (base + q < count) data[base + q] = ex;
-    ex += v[q];
+  for (int q = 0; q < SCAN_ITEMS; ++q) { o[q] = ex; ex += v[q]; }
+  if (base + SCAN_ITEMS <= count && ((reinterpret_cast<size_t>(data + base) & 15) == 0)) {
+    *reinterpret_cast<uint4 *>(data + base) = make_uint4(o[0], o[1], o[2], o[3]);
+    *reinterpret_cast<uint4 *>(data + base + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; ++q)
+      if (base + q < count) data[base + q] = o[q];
   }
 }
 

@@ -59,7 +59,16 @@ typedef struct {
   int64_t removed_oob;     /* CheckAndRemoveOutOfBoundsParticles count      */
   int64_t walk_evals;      /* cell evaluations the reference's walk makes (a walk that cycles
                               until MAX_TRAVERSAL counts 1000; the GPU walk stops at the cycle) */
+  int64_t fp64_fallbacks;  /* precision form: faces whose class needed the exact FP64 distance */
 } FdfStepInfo;
+
+/* Forms of the path.  PLAIN_FP64: every value as the reference computes it, bit for bit.
+ * FP32: interpolation, advection and deposition in FP32 (compensated deposit sums),
+ * positions kept in FP64, and every walk decision -- hence every cell and status --
+ * exactly the FP64 reference's for the form's own positions (FP32 signed distances
+ * with a rigorous error bound, exact FP64 distance where the bound cannot decide). */
+#define FDF_FORM_PLAIN_FP64 0
+#define FDF_FORM_FP32 1
 
 /* ---- context, grid and fields (replace UserCtx set-up: setup.c:197-290, grid.c:34-160) ---- */
 int fdf_ContextCreate(FdfContext **ctx, int device);
@@ -70,6 +79,8 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
 /* Cell-centred Cartesian velocity.  node_sized=1: the reference's DMDA layout
  * [KM+1][JM+1][IM+1][3] with cell (i,j,k) at [k][j][i]; node_sized=0: [KM][JM][IM][3]. */
 int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized);
+/* Selects the form used by the next fdf_SetSwarm (default PLAIN_FP64). */
+int fdf_SetForm(FdfContext *ctx, int form);
 int fdf_SetTimeStep(FdfContext *ctx, double dt);                 /* user->dt            */
 int fdf_SetParticleVolume(FdfContext *ctx, double volume);       /* face deposit V_p    */
 
