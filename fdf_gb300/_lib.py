@@ -32,6 +32,8 @@ _SIGS = {
     "fdf_SetParticleVolume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_ReserveParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
     "fdf_SetSwarm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 7),
+    "fdf_SeedParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int,
+                                         ctypes.c_int64, ctypes.c_double]),
     "fdf_GetSwarmSize": (ctypes.c_int, [ctypes.c_void_p, c_int64_p]),
     "fdf_GetSwarm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, c_int64_p] + [ctypes.c_void_p] * 7),
     "fdf_GetScatteredFields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

@@ -158,7 +158,18 @@ class PicContext:
         self.set_ucat(wl.ucat)
         self.set_dt(wl.dt)
         self.set_volume(wl.volume)
-        self.set_swarm(SwarmArrays.create(wl.pos, cell=wl.cell0, P=P))
+        if wl.pos is None:
+            self.seed_particles(wl.seed_n, wl.meta.get("seed", 0),
+                                start_in_generating_cell=not wl.meta.get("corner_start", False), P=P)
+        else:
+            self.set_swarm(SwarmArrays.create(wl.pos, cell=wl.cell0, P=P))
+
+    def seed_particles(self, n: int, seed: int = 0, start_in_generating_cell: bool = True, pid_base: int = 0,
+                       P: float = 101325.0):
+        """n particles seeded on the device, bit-identical to workloads.volumetric_particles."""
+        self._check(self.lib.fdf_SeedParticles(self.h, int(n), int(seed), 1 if start_in_generating_cell else 0,
+                                               int(pid_base), float(P)))
+        self._cap = max(self._cap, int(n))
 
     # -- read back
     def size(self) -> int:

@@ -368,6 +368,31 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   return FDF_SUCCESS;
 }
 
+int fdf_SeedParticles(FdfContext *ctx, int64_t n, uint64_t seed, int start_in_generating_cell, int64_t pid_base,
+                      double P) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_SeedParticles: call fdf_SetGrid first");
+  if (n < 0) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SeedParticles: negative particle count");
+  if (n > ctx->cap || !ctx->swarm_mem) {
+    int r = fdf_ReserveParticles(ctx, n);
+    if (r) return r;
+  }
+  CU(cudaSetDevice(ctx->device));
+  ctx->cur = 0;
+  launch_seed(ctx->coor, ctx->g, n, seed, pid_base, start_in_generating_cell ? 1 : 0,
+              ctx->form == FDF_FORM_FP32 ? 1 : 0, P, ctx->buf[0], ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  DevCounters c{};
+  c.n = (int)n;
+  c.n_sorted = (int)n;
+  CU(cudaMemcpyAsync(ctx->cnt, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->swarm_set = true;
+  ctx->swarm_form = ctx->form;
+  return FDF_SUCCESS;
+}
+
 int fdf_GetSwarmSize(FdfContext *ctx, int64_t *n) {
   if (!ctx || !n) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetSwarmSize: null argument");
   CU(cudaSetDevice(ctx->device));

@@ -164,3 +164,7 @@ void launch_swarm_to_aos32(const SwarmBuf &b, int n, GridDims g, double *pos, do
                            long long *cell3, long long *pid, long long *status, cudaStream_t s);
 void launch_f64_to_f32(const double *in, float *out, long long n, cudaStream_t s);
 void launch_f32_to_f64(const float *in, double *out, long long n, cudaStream_t s);
+
+// On-device volumetric seeding (fdf_seed.cu), bit-identical to the host generator.
+void launch_seed(const double *coor, GridDims g, long long n, unsigned long long seed, long long pid_base, int hint,
+                 int form32, double P0, const SwarmBuf &b, cudaStream_t s);

@@ -224,12 +224,13 @@ class Workload:
     name: str
     coor: np.ndarray            # [KM+1][JM+1][IM+1][3]
     ucat: np.ndarray            # [KM][JM][IM][3] cell-centred
-    pos: np.ndarray             # [n][3]
-    cell0: np.ndarray           # [n][3] initial DMSwarm_CellID (-1 = walk from the corner)
+    pos: np.ndarray | None      # [n][3]; None: seeded on the device (seed_n particles, meta seed)
+    cell0: np.ndarray | None    # [n][3] initial DMSwarm_CellID (-1 = walk from the corner)
     dt: float
     steps: int
     volume: float = 1.0
     meta: dict = field(default_factory=dict)
+    seed_n: int = 0
 
     @property
     def dims(self):
@@ -238,7 +239,14 @@ class Workload:
 
     @property
     def n(self):
-        return len(self.pos)
+        return len(self.pos) if self.pos is not None else self.seed_n
+
+    def sample(self, m: int):
+        """The first m particles (an i.i.d. sample) as host arrays: (pos, cell0, pid)."""
+        if self.pos is not None:
+            return self.pos[:m], self.cell0[:m], np.arange(min(m, self.n))
+        pos, cell = volumetric_particles(self.coor, min(m, self.seed_n), self.meta.get("seed", 0))
+        return pos, cell, np.arange(len(pos))
 
     def ucat_node_sized(self) -> np.ndarray:
         return node_sized(self.ucat)
@@ -252,43 +260,54 @@ def config1(n: int = 10_000, IM: int = 20, JM: int = 20, KM: int = 280, steps: i
     pos = box_particles(n, seed)
     return Workload("uniform_%dx%dx%d_n%d" % (IM, JM, KM, n), coor, ucat, pos,
                     np.full((n, 3), -1, dtype=np.int64), dt=0.1 / KM, steps=steps,
-                    meta=dict(family="uniform", cfl=None, seed=seed))
+                    meta=dict(family="uniform", cfl=None, seed=seed, corner_start=True), seed_n=n)
+
+
+def _particles(coor, n, seed, materialize):
+    if not materialize:
+        return None, None
+    return volumetric_particles(coor, n, seed)
 
 
 def config_sinusoidal(IM: int = 64, JM: int = 64, KM: int = 1024, n: int = 1_000_000, cfl: float = 0.5,
-                      steps: int = 50, seed: int = 0, corner_start: bool = False) -> Workload:
+                      steps: int = 50, seed: int = 0, corner_start: bool = False, materialize: bool = True) -> Workload:
     """Curvilinear box (amplitude 0.04) with a Taylor-Green vortex plus w = 1; particles
     uniform in (xi, eta, zeta); dt = cfl * min edge / max |ucat|."""
     coor = sinusoidal_grid(IM, JM, KM)
     ucat = field_taylor_green(cell_centroids(coor))
-    pos, cell = volumetric_particles(coor, n, seed)
+    pos, cell = _particles(coor, n, seed, materialize)
     umax = float(np.sqrt((ucat ** 2).sum(-1)).max())
     dt = cfl * min_edge_length(coor) / umax
-    if corner_start:
+    if corner_start and cell is not None:
         cell = np.full((n, 3), -1, dtype=np.int64)
     return Workload("sinusoidal_%dx%dx%d_n%d_cfl%g" % (IM, JM, KM, n, cfl), coor, ucat, pos, cell, dt=dt,
-                    steps=steps, meta=dict(family="sinusoidal", cfl=cfl, seed=seed, corner_start=corner_start))
+                    steps=steps, meta=dict(family="sinusoidal", cfl=cfl, seed=seed, corner_start=corner_start),
+                    seed_n=n)
 
 
 def config_bent_pipe(IM: int = 96, JM: int = 96, KM: int = 1536, n: int = 64_000_000, cfl: float = 4.0,
-                     steps: int = 50, seed: int = 0) -> Workload:
+                     steps: int = 50, seed: int = 0, materialize: bool = True) -> Workload:
+    """90-degree bend (pipe radius 0.5, bend radius 3), O-type 96x96 section, Poiseuille
+    axial flow 2U(1 - r^2/R^2) along the bend; dt = cfl * min edge / max |ucat|."""
     coor = bent_pipe_grid(IM, JM, KM)
     cent = cell_centroids(coor)
     ucat = field_pipe(coor, cent, secondary=0.0)
-    pos, cell = volumetric_particles(coor, n, seed)
+    pos, cell = _particles(coor, n, seed, materialize)
     umax = float(np.sqrt((ucat ** 2).sum(-1)).max())
     dt = cfl * min_edge_length(coor) / umax
     return Workload("bent_pipe_%dx%dx%d_n%d_cfl%g" % (IM, JM, KM, n, cfl), coor, ucat, pos, cell, dt=dt,
-                    steps=steps, meta=dict(family="bent_pipe", cfl=cfl, seed=seed))
+                    steps=steps, meta=dict(family="bent_pipe", cfl=cfl, seed=seed), seed_n=n)
 
 
 def config_curved_pipe(IM: int = 128, JM: int = 128, KM: int = 2048, n: int = 128_000_000, cfl: float = 1.0,
-                       steps: int = 200, seed: int = 0) -> Workload:
+                       steps: int = 200, seed: int = 0, materialize: bool = True) -> Workload:
+    """Curved pipe (radius 0.5) along a planar curve, Poiseuille axial flow plus a
+    Taylor-Green-like secondary swirl of amplitude 0.2; dt = cfl * min edge / max |ucat|."""
     coor = curved_pipe_grid(IM, JM, KM)
     cent = cell_centroids(coor)
     ucat = field_pipe(coor, cent, secondary=0.2)
-    pos, cell = volumetric_particles(coor, n, seed)
+    pos, cell = _particles(coor, n, seed, materialize)
     umax = float(np.sqrt((ucat ** 2).sum(-1)).max())
     dt = cfl * min_edge_length(coor) / umax
     return Workload("curved_pipe_%dx%dx%d_n%d_cfl%g" % (IM, JM, KM, n, cfl), coor, ucat, pos, cell, dt=dt,
-                    steps=steps, meta=dict(family="curved_pipe", cfl=cfl, seed=seed))
+                    steps=steps, meta=dict(family="curved_pipe", cfl=cfl, seed=seed), seed_n=n)

@@ -89,6 +89,14 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity);
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity,
                  const double *weight, const double *P, const int64_t *cell_id, const int64_t *pid,
                  const int64_t *status);
+/* Replaces the swarm by n particles seeded on the device like the reference's volumetric
+ * initialisation (ParticleSwarm.c:229-312 + Metric.c:48-62): a random cell and random
+ * logical coordinates from counter-based splitmix64 streams (seed), bit-identical to the
+ * harness generator fdf_gb300/workloads.py volumetric_particles.  PIDs pid_base + p, P as
+ * given, status UNINITIALIZED; DMSwarm_CellID is the generating cell when
+ * start_in_generating_cell, else (-1,-1,-1) (the reference's corner start). */
+int fdf_SeedParticles(FdfContext *ctx, int64_t n, uint64_t seed, int start_in_generating_cell, int64_t pid_base,
+                      double P);
 int fdf_GetSwarmSize(FdfContext *ctx, int64_t *n);
 int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n, double *position, double *velocity,
                  double *weight, double *P, int64_t *cell_id, int64_t *pid, int64_t *status);

@@ -182,3 +182,18 @@ def test_full_size_properties_sinusoidal(ctx):
     assert abs(tot - after.n * wl.volume) <= 1e-9 * after.n
     assert cnt.sum() == after.n
     assert np.all(after.cell >= 0) and np.all(after.status == ACTIVE_AND_LOCATED)
+
+
+def test_device_seeding_matches_host_generator(ctx):
+    """fdf_SeedParticles reproduces workloads.volumetric_particles bit for bit."""
+    wl = W.config_bent_pipe(IM=16, JM=12, KM=40, n=50_000, cfl=2.0, steps=1)
+    ctx.set_grid(wl.coor)
+    ctx.set_ucat(wl.ucat)
+    ctx.seed_particles(wl.n, seed=0, start_in_generating_cell=True)
+    s = ctx.get_swarm()
+    assert np.array_equal(s.pid, np.arange(wl.n))
+    assert np.array_equal(s.position.view(np.int64), wl.pos.view(np.int64))
+    assert np.array_equal(s.cell, wl.cell0)
+    assert np.all(s.status == 4) and np.all(s.P == 101325.0)
+    ctx.seed_particles(1000, seed=0, start_in_generating_cell=False)
+    assert np.all(ctx.get_swarm().cell == -1)
