@@ -134,6 +134,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def pinned_like(a: np.ndarray) -> np.ndarray:
     try:
         import torch
@@ -221,14 +230,39 @@ def run_reference(args, rank):
 
 # ----------------------------------------------------------------------------- GPU
 
-FORMS = {"plain_fp64": 0, "fp32": 1}
-FORM_DTYPE = {"plain_fp64": "f64", "fp32": "f32 (positions and walk decisions f64)"}
+FORMS = {"plain_fp64": 0, "fp32": 1, "learned_fp32": 2}
+FORM_DTYPE = {"plain_fp64": "f64", "fp32": "f32 (positions and walk decisions f64)",
+              "learned_fp32": "f32 (positions and walk decisions f64; bf16 MLP, f32 accumulate)"}
+MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, one inference
+
+_TRAINED = {}   # workload name -> (trained parameters, training report)
+
+
+def prepare(ctx, wl, form, args):
+    """Loads the workload in a form; the learned form gets its locator (trained once per
+    workload on the device, then reinstalled)."""
+    ctx.load_workload(wl, form=FORMS[form])
+    if form != "learned_fp32":
+        return
+    if wl.name not in _TRAINED:
+        import torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist = ctx.locator_train(args.train_samples, seed=17, steps=args.train_steps, batch=args.train_batch,
+                                 lr=args.train_lr)
+        el = time.perf_counter() - t0
+        _TRAINED[wl.name] = (ctx.locator_get_params(), {
+            "samples": args.train_samples, "steps": args.train_steps, "batch": args.train_batch, "lr": args.train_lr,
+            "seconds": round(el, 3), "loss_first": float(np.mean(hist[:20])), "loss_last": float(np.mean(hist[-50:])),
+            "loss_unit": "mean squared error in cells per axis"})
+    else:
+        ctx.locator_set_params(_TRAINED[wl.name][0])
 
 
 def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_step: float, Nc: int, Nn: int,
                       Nf: int) -> dict:
     """Algorithmic bytes per launch of each stage (the accounting of the design doc 3.3)."""
-    if form == "fp32":
+    if form in ("fp32", "learned_fp32"):
         return {
             "center_to_corner": 24 * nodes_per_step,
             "advect_locate": 86 * n_avg + 176 * evals_per_step,
@@ -253,10 +287,11 @@ def time_form(ctx, wl, form, args, dist, local, with_clocks):
     IM, JM, KM = wl.dims
     Nc, Nn = IM * JM * KM, (IM + 1) * (JM + 1) * (KM + 1)
     Nf = (IM + 1) * JM * KM + IM * (JM + 1) * KM + IM * JM * (KM + 1)
-    ctx.load_workload(wl, form=FORMS[form])
+    prepare(ctx, wl, form, args)
     ctx.initial_setup()
     ctx.steps(args.warmup)
     ctx.synchronize()
+    guess0 = ctx.locator_stats() if form == "learned_fp32" else None
     stream = torch.cuda.ExternalStream(ctx.stream, device=local)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ps0, e0, nd0 = ctx.counters()
@@ -284,9 +319,37 @@ def time_form(ctx, wl, form, args, dist, local, with_clocks):
     K = max(args.steps, 1)
     n_avg = psteps / K
     alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf)
-    per = {k: (v[0] / max(v[1], 1)) for k, v in stages.items()}
+    runs = max(stages["sort_by_cell"][1], 1)     # one span per pipeline run
+    per = {k: (v[0] / runs) for k, v in stages.items() if v[1] > 0}
+    learned = None
+    if form == "learned_fp32":
+        asked, taken, gev = (b - a for a, b in zip(guess0, ctx.locator_stats()))
+        mlp_ms = per.get("learned_guess", 0.0)
+        tfl = MLP_FLOPS * asked / K / (mlp_ms / 1000.0) / 1e12 if mlp_ms > 0 else None
+        learned = {"guesses_per_step": asked / K, "guess_fraction": asked / max(psteps, 1),
+                   "guesses_kept": taken / max(asked, 1), "guess_walk_evals_per_guess": gev / max(asked, 1),
+                   "mlp_tflops": tfl, "mlp_flops_per_particle": MLP_FLOPS,
+                   "training": _TRAINED[wl.name][1]}
     return dict(form=form, psteps=psteps, evals=evals, ms=ms_max, launches=launches, clocks=clk, per=per, alg=alg,
-                value=psteps * int(os.environ.get("WORLD_SIZE", "1")) / (ms_max / 1000.0))
+                learned=learned, value=psteps * int(os.environ.get("WORLD_SIZE", "1")) / (ms_max / 1000.0))
+
+
+def learned_identity(ctx, wl, args, steps: int) -> dict:
+    """The learned form against the FP32 form from the same initial state on the full
+    workload: the swarms (cells, statuses, positions, velocities, weights) and the face
+    deposits must be identical."""
+    out = {}
+    for form in ("fp32", "learned_fp32"):
+        prepare(ctx, wl, form, args)
+        ctx.initial_setup()
+        ctx.steps(steps)
+        out[form] = (ctx.get_swarm(), ctx.get_faces())
+    (sa, fa), (sb, fb) = out["fp32"], out["learned_fp32"]
+    same = {f: bool(np.array_equal(getattr(sa, f), getattr(sb, f)))
+            for f in ("cell", "status", "pid", "position", "velocity", "weight", "P")}
+    same["faces"] = all(bool(np.array_equal(x, y)) for x, y in zip(fa, fb))
+    return {"steps": steps, "particles": int(sa.n), "identical": same,
+            "cells_differing": int(np.any(sa.cell != sb.cell, axis=1).sum()) if sa.n == sb.n else None}
 
 
 def fp32_accuracy(ctx, wl, steps: int, nthreads: int) -> dict:
@@ -363,11 +426,25 @@ def run_gpu(args, rank, ws, local, dist):
                 "algorithmic_bytes_per_launch": alg[dom], "traffic": None,
                 "stage_ms_per_step": {k: round(v, 4) for k, v in per.items()},
                 "stage_gbs": {k: round(alg[k] / (per[k] / 1000.0) / 1e9, 1) for k in per if per[k] > 0 and alg.get(k)}}
+    lp = prim.get("learned")
+    if lp and lp["mlp_tflops"] and per.get("learned_guess", 0.0) > per[dom]:
+        # the network inference dominates: its roofline is the tensor one
+        tf, tf_kind = bf16_peak()
+        roofline.update({"bound": "tensor", "kernel": "learned_guess (k_mlp_guess)", "achieved": lp["mlp_tflops"],
+                         "peak": tf, "unit": "TFLOP/s", "frac": lp["mlp_tflops"] / tf,
+                         "peak_source": f"{tf_kind} (MEASURED_PEAKS.json bf16_tflops)",
+                         "algorithmic_flops_per_launch": MLP_FLOPS * lp["guesses_per_step"],
+                         "hbm_stage": {"kernel": dom, "achieved_gbs": achieved, "frac": achieved / hbm}})
+        roofline.pop("algorithmic_bytes_per_launch", None)
     form_lines = {f: {"particle_steps_per_s": r["value"], "ms_per_step": r["ms"] / max(args.steps, 1),
                       "walk_evals_per_particle_step": r["evals"] / max(r["psteps"], 1),
-                      "stage_ms_per_step": {k: round(v, 4) for k, v in r["per"].items()}}
+                      "stage_ms_per_step": {k: round(v, 4) for k, v in r["per"].items()},
+                      **({"learned_locator": r["learned"]} if r["learned"] else {})}
                   for f, r in results.items()}
-    ctx.load_workload(wl, form=FORMS[forms[0]])
+    identity = None
+    if "learned_fp32" in forms and args.identity_steps > 0:
+        identity = learned_identity(ctx, wl, args, args.identity_steps)
+    prepare(ctx, wl, forms[0], args)
     ctx.initial_setup()
 
     # end to end through the C ABI with host (pinned) buffers
@@ -409,7 +486,7 @@ def run_gpu(args, rank, ws, local, dist):
                        "pinned host DMSwarm-layout arrays"}
 
     accuracy = None
-    if rank == 0 and ws == 1 and args.accuracy_steps > 0 and "fp32" in forms:
+    if rank == 0 and ws == 1 and args.accuracy_steps > 0 and ("fp32" in forms or "learned_fp32" in forms):
         accuracy = fp32_accuracy(ctx, wl, args.accuracy_steps, os.cpu_count() or 1)
 
     cpu = None
@@ -434,6 +511,7 @@ def run_gpu(args, rank, ws, local, dist):
                                  % (38 * 8 * Nc / 1e9, 2 * 93 * wl.n / 1e6),
                            "walk_evals_per_particle_step": evals / max(psteps, 1)},
                 "roofline": roofline, "forms": form_lines, "fp32_accuracy_vs_fp64_oracle": accuracy,
+                "learned_vs_fp32_form": identity,
                 "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clk}
         print(json.dumps(line), flush=True)
@@ -446,9 +524,15 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="fdf", choices=["fdf", "reference"])
-    ap.add_argument("--workload", default="sinusoidal")
-    ap.add_argument("--forms", default="fp32,plain_fp64",
+    ap.add_argument("--workload", default="bent_pipe")
+    ap.add_argument("--forms", default="learned_fp32,fp32,plain_fp64",
                     help="comma list; the first is the headline value, the others are reported beside it")
+    ap.add_argument("--train-samples", type=int, default=4_000_000)
+    ap.add_argument("--train-steps", type=int, default=4000)
+    ap.add_argument("--train-batch", type=int, default=8192)
+    ap.add_argument("--train-lr", type=float, default=2e-3)
+    ap.add_argument("--identity-steps", type=int, default=3,
+                    help="steps of the learned-vs-FP32-form identity check on the full workload (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

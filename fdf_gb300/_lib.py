@@ -53,6 +53,17 @@ _SIGS = {
     "fdf_SetProfiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_GetCounters": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p]),
     "fdf_GetStageTimes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "fdf_LocatorInit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "fdf_LocatorTrain": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int64,
+                                        ctypes.c_int64, ctypes.c_double, ctypes.c_void_p]),
+    "fdf_LocatorSetParams": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "fdf_LocatorGetParams": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "fdf_LocatorGetNormalization": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_LocatorGradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                            ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_LocatorPredict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "fdf_LocatorGetStats": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p]),
 }
 
 

@@ -21,7 +21,8 @@ ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG"
              73: "PETSC_ERR_ARG_WRONGSTATE", 76: "PETSC_ERR_LIB", 83: "PETSC_ERR_USER", 85: "PETSC_ERR_ARG_NULL",
              97: "PETSC_ERR_GPU"}
 NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
-FORM_PLAIN_FP64, FORM_FP32 = 0, 1
+FORM_PLAIN_FP64, FORM_FP32, FORM_LEARNED_FP32 = 0, 1, 2
+LOCATOR_NPARAM = 33923
 
 
 class PetscError(RuntimeError):
@@ -132,7 +133,8 @@ class PicContext:
         self._check(self.lib.fdf_SetUcat(self.h, _ptr(ucat), node_sized))
 
     def set_form(self, form: int):
-        """FORM_PLAIN_FP64 (bit-exact) or FORM_FP32 (precision form); applies at the next set_swarm."""
+        """FORM_PLAIN_FP64 (bit-exact), FORM_FP32 (precision form) or FORM_LEARNED_FP32 (precision
+        form with the learned start cell); applies at the next set_swarm / seed_particles."""
         self._check(self.lib.fdf_SetForm(self.h, int(form)))
 
     def set_dt(self, dt: float):
@@ -234,7 +236,7 @@ class PicContext:
         return int(self.lib.fdf_GetLaunchCount(self.h))
 
     STAGES = ("center_to_corner", "advect_locate", "sort_by_cell", "wait_corner", "gather_interpolate",
-              "deposit")
+              "deposit", "learned_guess")
 
     def counters(self) -> tuple[int, int, int]:
         """(particle-steps advanced, walk evaluations made, corner nodes computed) since the swarm was set."""
@@ -251,3 +253,52 @@ class PicContext:
         runs = np.zeros(len(self.STAGES), dtype=np.int64)
         self._check(self.lib.fdf_GetStageTimes(self.h, _ptr(ms), _ptr(runs), len(self.STAGES)))
         return {name: (float(ms[i]), int(runs[i])) for i, name in enumerate(self.STAGES)}
+
+    # -- learned start-cell locator
+    def locator_init(self, seed: int = 0):
+        self._check(self.lib.fdf_LocatorInit(self.h, int(seed)))
+
+    def locator_train(self, n_samples: int, seed: int = 0, steps: int = 4000, batch: int = 8192,
+                      lr: float = 2e-3) -> np.ndarray:
+        """Trains the locator on the device; returns the loss of every step."""
+        hist = np.zeros(max(int(steps), 1), dtype=np.float32)
+        self._check(self.lib.fdf_LocatorTrain(self.h, int(n_samples), int(seed), int(steps), int(batch), float(lr),
+                                              _ptr(hist)))
+        return hist[:int(steps)]
+
+    def locator_set_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, dtype=np.float32).ravel()
+        self._check(self.lib.fdf_LocatorSetParams(self.h, _ptr(p), p.size))
+
+    def locator_get_params(self) -> np.ndarray:
+        p = np.zeros(LOCATOR_NPARAM, dtype=np.float32)
+        self._check(self.lib.fdf_LocatorGetParams(self.h, _ptr(p), p.size))
+        return p
+
+    def locator_normalization(self) -> tuple[np.ndarray, np.ndarray]:
+        c = np.zeros(3, dtype=np.float32)
+        h = np.zeros(3, dtype=np.float32)
+        self._check(self.lib.fdf_LocatorGetNormalization(self.h, _ptr(c), _ptr(h)))
+        return c, h
+
+    def locator_gradients(self, xhat: np.ndarray, target: np.ndarray) -> tuple[np.ndarray, float]:
+        x = np.ascontiguousarray(xhat, dtype=np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(target, dtype=np.float32).reshape(-1, 3)
+        g = np.zeros(LOCATOR_NPARAM, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        self._check(self.lib.fdf_LocatorGradients(self.h, _ptr(x), _ptr(t), len(x), _ptr(g), _ptr(loss)))
+        return g, float(loss[0])
+
+    def locator_predict(self, pos: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """(cells [n][3] i64, network outputs [n][3] f32) for host positions [n][3]."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        cells = np.zeros((len(p), 3), dtype=np.int64)
+        out = np.zeros((len(p), 3), dtype=np.float32)
+        self._check(self.lib.fdf_LocatorPredict(self.h, _ptr(p), len(p), _ptr(cells), _ptr(out)))
+        return cells, out
+
+    def locator_stats(self) -> tuple[int, int, int]:
+        """(particles given a guess, guesses kept, evaluations of the walks from the guesses)."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.fdf_LocatorGetStats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value

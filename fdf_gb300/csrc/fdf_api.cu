@@ -10,8 +10,7 @@
 //   slot assignment (counting sort) + per-cell ordering by PID
 //   gather + interpolate into the alternate buffer (sorted order)
 //   deposit (cell count / P average, face volumes) from the sorted segments
-#include "fdf_internal.cuh"
-#include "../../include/fdf_gb300.h"
+#include "fdf_context.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -19,99 +18,14 @@
 #include <string>
 #include <vector>
 
-struct FdfContext {
-  int device = 0;
-  cudaStream_t stream = nullptr, side = nullptr;
-  cudaEvent_t ev_scan = nullptr, ev_corner = nullptr;
-  GridDims g{};
-  bool has_grid = false, has_ucat = false;
-  double *coor = nullptr, *planes = nullptr, *ucat = nullptr, *corner = nullptr, *bbox = nullptr;
-  double *count = nullptr, *avg = nullptr, *fi = nullptr, *fj = nullptr, *fk = nullptr;
-  // precision form (FDF_FORM_FP32)
-  int form = FDF_FORM_PLAIN_FP64;
-  float *table32 = nullptr, *ucat32 = nullptr, *corner32 = nullptr, *fbox = nullptr;
-  float *count32 = nullptr, *avg32 = nullptr, *fi32 = nullptr, *fj32 = nullptr, *fk32 = nullptr;
-  double bbox_h[6] = {0, 0, 0, 0, 0, 0};
-  double dt = 0.0, volume = 1.0;
-  int cap = 0;
-  SwarmBuf buf[2];
-  int cur = 0;
-  void *swarm_mem = nullptr;
-  unsigned int *keys = nullptr, *perm = nullptr;   // [cap]: cell key per slot, sorted slot -> previous slot
-  unsigned int *cell_start = nullptr;              // [Nc+2]: histogram, then its exclusive scan
-  unsigned int *cursor = nullptr;                  // [Nc+1]: per-cell slot cursors of the counting sort
-  unsigned int *scan_sums = nullptr;
-  DevCounters *cnt = nullptr;
-  void *staging = nullptr;
-  size_t staging_bytes = 0;
-  unsigned int sentinel = 0;
-  bool swarm_set = false;
-  int swarm_form = FDF_FORM_PLAIN_FP64;   // form the swarm's device arrays are held in
-  int out_form = FDF_FORM_PLAIN_FP64;     // form of the last deposits
-  long long launches = 0;
-  // stage timing: events recorded on the context stream between pipeline stages
-  bool profiling = false;
-  std::vector<cudaEvent_t> ev_pool;
-  size_t ev_used = 0;
-  std::vector<std::pair<int, std::pair<size_t, size_t>>> ev_spans;   // (stage, (start ev, end ev))
-  std::string last_error;
-};
-
 namespace {
-
-int fail(FdfContext *ctx, int code, const std::string &msg) {
-  if (ctx) ctx->last_error = msg;
-  return code;
-}
-
-#define CU(call)                                                                          \
-  do {                                                                                    \
-    cudaError_t e_ = (call);                                                              \
-    if (e_ != cudaSuccess)                                                                \
-      return fail(ctx, e_ == cudaErrorMemoryAllocation ? FDF_ERR_MEM : FDF_ERR_GPU,       \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));                    \
-  } while (0)
-
-#define CHECK_LAUNCH()                                                                    \
-  do {                                                                                    \
-    cudaError_t e_ = cudaGetLastError();                                                  \
-    if (e_ != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("launch: ") + cudaGetErrorString(e_)); \
-  } while (0)
-
-template <typename T>
-void cfree(T *&p) {
-  if (p) cudaFree((void *)p);
-  p = nullptr;
-}
-
-size_t swarm_bytes_per_buf(int cap) {
-  return (size_t)cap * (10 * sizeof(double) + 7 * sizeof(float) + sizeof(long long) + sizeof(int) + 1) + 24 * 256;
-}
-
-void carve_swarm(char *p, int cap, SwarmBuf &b) {
-  auto take = [&](size_t bytes) {
-    char *r = p;
-    p += (bytes + 255) / 256 * 256;
-    return r;
-  };
-  b.x = (double *)take(8ull * cap); b.y = (double *)take(8ull * cap); b.z = (double *)take(8ull * cap);
-  b.u = (double *)take(8ull * cap); b.v = (double *)take(8ull * cap); b.w = (double *)take(8ull * cap);
-  b.a1 = (double *)take(8ull * cap); b.a2 = (double *)take(8ull * cap); b.a3 = (double *)take(8ull * cap);
-  b.P = (double *)take(8ull * cap);
-  b.uf = (float *)take(4ull * cap); b.vf = (float *)take(4ull * cap); b.wf = (float *)take(4ull * cap);
-  b.a1f = (float *)take(4ull * cap); b.a2f = (float *)take(4ull * cap); b.a3f = (float *)take(4ull * cap);
-  b.Pf = (float *)take(4ull * cap);
-  b.pid = (long long *)take(8ull * cap);
-  b.cell = (int *)take(4ull * cap);
-  b.status = (unsigned char *)take((size_t)cap);
-}
 
 constexpr long long FDF_MAX_PARTICLES = 512LL * 1024 * 1024;
 
 
 // Stage ids reported by fdf_GetStageTimes.
 enum { STAGE_CORNER = 0, STAGE_LOCATE = 1, STAGE_SORT = 2, STAGE_WAIT = 3, STAGE_GATHER_INTERP = 4,
-       STAGE_DEPOSIT = 5, NUM_STAGES = 6 };
+       STAGE_DEPOSIT = 5, STAGE_GUESS = 6, NUM_STAGES = 7 };
 
 size_t record_event(FdfContext *ctx, cudaStream_t stream) {
   if (ctx->ev_used == ctx->ev_pool.size()) {
@@ -145,6 +59,7 @@ int fdf_ContextCreate(FdfContext **out, int device) {
   if (e == cudaSuccess) e = cudaMemset(ctx->cnt, 0, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->bbox, 6 * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->fbox, 16 * sizeof(float));
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
     fdf_ContextDestroy(ctx);
     return FDF_ERR_GPU;
@@ -164,6 +79,7 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   if (ctx->side) cudaStreamSynchronize(ctx->side);
   cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
   cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
+  locator_free(ctx);
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->ev_scan) cudaEventDestroy(ctx->ev_scan);
   if (ctx->ev_corner) cudaEventDestroy(ctx->ev_corner);
@@ -253,6 +169,7 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   CU(cudaMemcpyAsync(ctx->fbox, fb, sizeof(fb), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->sentinel = (unsigned int)Nc;
+  ctx->loc.has_params = false;   // a locator is trained for one grid
   ctx->has_grid = true;
   ctx->has_ucat = false;
   ctx->swarm_set = false;
@@ -285,7 +202,7 @@ int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized) {
 
 int fdf_SetForm(FdfContext *ctx, int form) {
   if (!ctx) return FDF_ERR_ARG_NULL;
-  if (form != FDF_FORM_PLAIN_FP64 && form != FDF_FORM_FP32)
+  if (form != FDF_FORM_PLAIN_FP64 && form != FDF_FORM_FP32 && form != FDF_FORM_LEARNED_FP32)
     return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetForm: unknown form");
   ctx->form = form;
   return FDF_SUCCESS;
@@ -350,7 +267,7 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
     CU(cudaMemcpyAsync(d_pid, pid, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
     CU(cudaMemcpyAsync(d_st, status, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
     ctx->cur = 0;
-    if (ctx->form == FDF_FORM_FP32)
+    if (form_is32(ctx->form))
       launch_swarm_from_aos32(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
     else
       launch_swarm_from_aos(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
@@ -380,7 +297,7 @@ int fdf_SeedParticles(FdfContext *ctx, int64_t n, uint64_t seed, int start_in_ge
   CU(cudaSetDevice(ctx->device));
   ctx->cur = 0;
   launch_seed(ctx->coor, ctx->g, n, seed, pid_base, start_in_generating_cell ? 1 : 0,
-              ctx->form == FDF_FORM_FP32 ? 1 : 0, P, ctx->buf[0], ctx->stream);
+              form_is32(ctx->form) ? 1 : 0, P, ctx->buf[0], ctx->stream);
   CHECK_LAUNCH();
   ctx->launches += 1;
   DevCounters c{};
@@ -417,7 +334,7 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *positio
   char *st = (char *)ctx->staging;
   double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
-  if (ctx->swarm_form == FDF_FORM_FP32)
+  if (form_is32(ctx->swarm_form))
     launch_swarm_to_aos32(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
                           ctx->stream);
   else
@@ -440,7 +357,7 @@ int fdf_GetScatteredFields(FdfContext *ctx, double *count, double *P_avg) {
   if (!ctx || !count || !P_avg) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetScatteredFields: null argument");
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetScatteredFields: no grid");
   CU(cudaSetDevice(ctx->device));
-  if (ctx->out_form == FDF_FORM_FP32) {
+  if (form_is32(ctx->out_form)) {
     launch_f32_to_f64(ctx->count32, ctx->count, ctx->g.Nn, ctx->stream);
     launch_f32_to_f64(ctx->avg32, ctx->avg, ctx->g.Nn, ctx->stream);
     CHECK_LAUNCH();
@@ -476,7 +393,7 @@ int fdf_GetFaceDeposits(FdfContext *ctx, double *fi, double *fj, double *fk) {
   const GridDims &g = ctx->g;
   long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM, nfk = (long long)g.IM * g.JM * (g.KM + 1LL);
   CU(cudaSetDevice(ctx->device));
-  if (ctx->out_form == FDF_FORM_FP32) {
+  if (form_is32(ctx->out_form)) {
     launch_f32_to_f64(ctx->fi32, ctx->fi, nfi, ctx->stream);
     launch_f32_to_f64(ctx->fj32, ctx->fj, nfj, ctx->stream);
     launch_f32_to_f64(ctx->fk32, ctx->fk, nfk, ctx->stream);
@@ -499,6 +416,12 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   if (!ctx->has_ucat) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no ucat: call fdf_SetUcat first");
   if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
   CU(cudaSetDevice(ctx->device));
+  if (ctx->swarm_form == FDF_FORM_LEARNED_FP32) {
+    if (!ctx->loc.has_params)
+      return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "learned form: no locator (fdf_LocatorTrain or fdf_LocatorSetParams)");
+    int r = locator_reserve(ctx);
+    if (r) return r;
+  }
   cudaStream_t s = ctx->stream;
   const GridDims &g = ctx->g;
   int n_start = 0;
@@ -512,14 +435,29 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   const bool prof = ctx->profiling;
   SwarmBuf &src = ctx->buf[ctx->cur];
   SwarmBuf &dst = ctx->buf[1 - ctx->cur];
-  const bool f32 = ctx->swarm_form == FDF_FORM_FP32;
-  size_t e0 = prof ? record_event(ctx, s) : 0;
-  if (f32)
+  const bool f32 = form_is32(ctx->swarm_form);
+  const bool learned = ctx->swarm_form == FDF_FORM_LEARNED_FP32;
+  size_t e0 = prof ? record_event(ctx, s) : 0, eg0 = 0, eg1 = 0;
+  if (learned) {
+    // one evaluation in the previous cell; the particles that left it get a learned
+    // start cell and walk from there (k_locate32_guess)
+    LocatorState &L = ctx->loc;
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
-                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, s);
-  else
+                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, s);
+    eg0 = prof ? record_event(ctx, s) : 0;
+    mlp_guess(L.frag, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0, ctx->cap, g, L.guess,
+              ctx->num_sms, s);
+    eg1 = prof ? record_event(ctx, s) : 0;
+    launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
+                          ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
+    ctx->launches += 2;
+  } else if (f32) {
+    launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
+                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, nullptr, s);
+  } else {
     launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys,
                   ctx->cell_start, ctx->sentinel, s);
+  }
   size_t e1 = prof ? record_event(ctx, s) : 0;
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
   // the corner field needs only cell_start: compute it beside the slot assignment
@@ -550,8 +488,14 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, s);
   ctx->out_form = ctx->swarm_form;
   size_t e5 = prof ? record_event(ctx, s) : 0;
-  if (prof) {
+  if (prof && learned) {
+    ctx->ev_spans.push_back({STAGE_LOCATE, {e0, eg0}});
+    ctx->ev_spans.push_back({STAGE_GUESS, {eg0, eg1}});
+    ctx->ev_spans.push_back({STAGE_LOCATE, {eg1, e1}});
+  } else if (prof) {
     ctx->ev_spans.push_back({STAGE_LOCATE, {e0, e1}});
+  }
+  if (prof) {
     ctx->ev_spans.push_back({STAGE_SORT, {e1, e2}});
     ctx->ev_spans.push_back({STAGE_CORNER, {c0, c1}});
     ctx->ev_spans.push_back({STAGE_WAIT, {e2, e3}});

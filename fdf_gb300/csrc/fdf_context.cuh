@@ -1,0 +1,127 @@
+// fdf_context.cuh -- the device context behind the opaque FdfContext of the C ABI,
+// shared by the API translation units (fdf_api.cu, fdf_locator.cu).
+#pragma once
+#include "fdf_internal.cuh"
+#include "fdf_mlp.cuh"
+#include "../../include/fdf_gb300.h"
+
+#include <string>
+#include <utility>
+#include <vector>
+
+// The learned start-cell locator of one context (FDF_FORM_LEARNED_FP32).
+struct LocatorState {
+  bool has_params = false;
+  float *params = nullptr;            // [MLP_NPARAM] FP32 master weights
+  float *grads = nullptr, *adam_m = nullptr, *adam_v = nullptr;
+  __nv_bfloat16 *params_bf = nullptr; // bfloat16 copy the training GEMMs read
+  uint2 *frag = nullptr;              // inference weights in fragment order
+  float *bias = nullptr;
+  MlpNorm norm{};
+  long long adam_t = 0;
+  // per-particle buffers of the learned form's locate
+  unsigned int *pending = nullptr;
+  int *guess = nullptr;
+  int pending_cap = 0;
+  // training scratch for batches up to `batch_cap`
+  int batch_cap = 0;
+  void *scratch = nullptr;
+};
+
+struct FdfContext {
+  int device = 0;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t ev_scan = nullptr, ev_corner = nullptr;
+  GridDims g{};
+  bool has_grid = false, has_ucat = false;
+  double *coor = nullptr, *planes = nullptr, *ucat = nullptr, *corner = nullptr, *bbox = nullptr;
+  double *count = nullptr, *avg = nullptr, *fi = nullptr, *fj = nullptr, *fk = nullptr;
+  // precision form (FDF_FORM_FP32)
+  int form = FDF_FORM_PLAIN_FP64;
+  float *table32 = nullptr, *ucat32 = nullptr, *corner32 = nullptr, *fbox = nullptr;
+  float *count32 = nullptr, *avg32 = nullptr, *fi32 = nullptr, *fj32 = nullptr, *fk32 = nullptr;
+  double bbox_h[6] = {0, 0, 0, 0, 0, 0};
+  double dt = 0.0, volume = 1.0;
+  int cap = 0;
+  SwarmBuf buf[2];
+  int cur = 0;
+  void *swarm_mem = nullptr;
+  unsigned int *keys = nullptr, *perm = nullptr;   // [cap]: cell key per slot, sorted slot -> previous slot
+  unsigned int *cell_start = nullptr;              // [Nc+2]: histogram, then its exclusive scan
+  unsigned int *cursor = nullptr;                  // [Nc+1]: per-cell slot cursors of the counting sort
+  unsigned int *scan_sums = nullptr;
+  DevCounters *cnt = nullptr;
+  void *staging = nullptr;
+  size_t staging_bytes = 0;
+  unsigned int sentinel = 0;
+  bool swarm_set = false;
+  int swarm_form = FDF_FORM_PLAIN_FP64;   // form the swarm's device arrays are held in
+  int out_form = FDF_FORM_PLAIN_FP64;     // form of the last deposits
+  long long launches = 0;
+  // stage timing: events recorded on the context stream between pipeline stages
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<std::pair<int, std::pair<size_t, size_t>>> ev_spans;   // (stage, (start ev, end ev))
+  std::string last_error;
+  int num_sms = 0;
+  LocatorState loc;
+};
+
+
+// forms whose swarm is held in the precision-form arrays
+inline bool form_is32(int form) { return form == FDF_FORM_FP32 || form == FDF_FORM_LEARNED_FP32; }
+
+inline int fail(FdfContext *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+#define CU(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? FDF_ERR_MEM : FDF_ERR_GPU,       \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+  } while (0)
+
+#define CHECK_LAUNCH()                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                  \
+    if (e_ != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+inline void cfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+
+inline size_t swarm_bytes_per_buf(int cap) {
+  return (size_t)cap * (10 * sizeof(double) + 7 * sizeof(float) + sizeof(long long) + sizeof(int) + 1) + 24 * 256;
+}
+
+inline void carve_swarm(char *p, int cap, SwarmBuf &b) {
+  auto take = [&](size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) / 256 * 256;
+    return r;
+  };
+  b.x = (double *)take(8ull * cap); b.y = (double *)take(8ull * cap); b.z = (double *)take(8ull * cap);
+  b.u = (double *)take(8ull * cap); b.v = (double *)take(8ull * cap); b.w = (double *)take(8ull * cap);
+  b.a1 = (double *)take(8ull * cap); b.a2 = (double *)take(8ull * cap); b.a3 = (double *)take(8ull * cap);
+  b.P = (double *)take(8ull * cap);
+  b.uf = (float *)take(4ull * cap); b.vf = (float *)take(4ull * cap); b.wf = (float *)take(4ull * cap);
+  b.a1f = (float *)take(4ull * cap); b.a2f = (float *)take(4ull * cap); b.a3f = (float *)take(4ull * cap);
+  b.Pf = (float *)take(4ull * cap);
+  b.pid = (long long *)take(8ull * cap);
+  b.cell = (int *)take(4ull * cap);
+  b.status = (unsigned char *)take((size_t)cap);
+}
+
+
+// fdf_locator.cu
+void locator_free(FdfContext *ctx);
+// Learned form: make sure the per-particle guess buffers hold ctx->cap particles.
+int locator_reserve(FdfContext *ctx);

@@ -25,8 +25,9 @@
 // The cells, statuses and walk paths are therefore the reference's for the form's own
 // positions.  Fallbacks are counted.  The hot loop issues no FP64 instruction.
 //
-// Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32), c0l (3 x f32),
-// degenerate flag (u32), then per face LEFT..BACK: fcr (3 x f32), n32 (3 x f32).
+// Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32, negative for a degenerate
+// cell), c0l (3 x f32), overlap margin (f32, see cell_margin), then per face LEFT..BACK:
+// fcr (3 x f32), n32 (3 x f32).
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
 
@@ -39,6 +40,62 @@ using fdfx::sub;
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Overlap margin of cell c (FP64): an upper bound on |d_f(p) - d'(p)| over the six faces f
+// of the cell, every plane P' of the same grid surface on the 3x3 patches around face f
+// (the same face of the in-surface neighbours and the opposite face of the cells across
+// those patches, oriented like f), for p within R = 2.2 max_v |v - centroid| of the face
+// centroid:  |(fc - fc') . n'| + R |n - n'|,  plus twice the largest distance threshold
+// involved.  A point whose six distances all exceed thr + margin lies on the negative side
+// of one face, by more than its threshold, of each of the 26 neighbouring cells.
+// Degenerate rows in the neighbourhood give an infinite margin.
+__device__ double cell_margin(const double *__restrict__ planes, const double *__restrict__ coor, GridDims g, int i,
+                              int j, int k) {
+  double cen[3] = {0.0, 0.0, 0.0}, v[8][3];
+  for (int q = 0; q < 8; ++q) {
+    const long long node = ((long long)(k + (q >> 2)) * (g.JM + 1) + (j + ((q >> 1) & 1))) * (long long)(g.IM + 1) +
+                           (i + (q & 1));
+    for (int d = 0; d < 3; ++d) { v[q][d] = coor[3 * node + d]; cen[d] += v[q][d]; }
+  }
+  double rv = 0.0;
+  for (int q = 0; q < 8; ++q) {
+    const double dx = v[q][0] - cen[0] / 8.0, dy = v[q][1] - cen[1] / 8.0, dz = v[q][2] - cen[2] / 8.0;
+    rv = fmax(rv, sqrt(dx * dx + dy * dy + dz * dz));
+  }
+  const double R = 2.2 * rv;
+  const long long c = ((long long)k * g.JM + j) * g.IM + i;
+  const int idx[3] = {i, j, k}, dims[3] = {g.IM, g.JM, g.KM};
+  // face -> (axis, upper side), partner face
+  const int axis[6] = {0, 0, 1, 1, 2, 2};
+  const int upper[6] = {0, 1, 0, 1, 1, 0};           // LEFT, RIGHT, BOTTOM, TOP, FRONT (k+1), BACK (k)
+  const int partner[6] = {F_RIGHT, F_LEFT, F_TOP, F_BOTTOM, F_BACK, F_FRONT};
+  double worst = 0.0, thr_max = planes[c * FDF_ROW + 36];
+  for (int f = 0; f < 6; ++f) {
+    const double *pf = planes + c * FDF_ROW + 6 * f;
+    const int a = axis[f], b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+    for (int side = 0; side < 2; ++side) {           // 0: same face of in-surface neighbours, 1: across
+      const int da = side == 0 ? 0 : (upper[f] ? 1 : -1);
+      const int face = side == 0 ? f : partner[f];
+      const double sg = side == 0 ? 1.0 : -1.0;
+      for (int o1 = -1; o1 <= 1; ++o1)
+        for (int o2 = -1; o2 <= 1; ++o2) {
+          int n[3] = {idx[0], idx[1], idx[2]};
+          n[a] += da; n[b1] += o1; n[b2] += o2;
+          if (n[0] < 0 || n[0] >= dims[0] || n[1] < 0 || n[1] >= dims[1] || n[2] < 0 || n[2] >= dims[2]) continue;
+          const long long cn = ((long long)n[2] * g.JM + n[1]) * g.IM + n[0];
+          const double *rn = planes + cn * FDF_ROW;
+          if (fdfx::ubits(rn[37]) != 0ULL) return INFINITY;
+          thr_max = fmax(thr_max, rn[36]);
+          const double *q = rn + 6 * face;
+          const double nx = sg * q[3], ny = sg * q[4], nz = sg * q[5];
+          const double off = fabs((pf[0] - q[0]) * nx + (pf[1] - q[1]) * ny + (pf[2] - q[2]) * nz);
+          const double dnx = pf[3] - nx, dny = pf[4] - ny, dnz = pf[5] - nz;
+          worst = fmax(worst, off + R * sqrt(dnx * dnx + dny * dny + dnz * dnz));
+        }
+    }
+  }
+  return worst * (1.0 + 1e-6) + 2.0 * thr_max + 1e-12 * R;
 }
 
 __global__ void k_build_table32(const double *__restrict__ planes, const double *__restrict__ coor, GridDims g,
@@ -59,9 +116,12 @@ __global__ void k_build_table32(const double *__restrict__ planes, const double 
     c0[q] = add((double)h, (double)l);   // exact: the pair's value
   }
   const double thr = row[36];
-  // rounded up with a little headroom: thr32 * (1 - 2^-24) >= thr, which the error bound uses
-  t[3] = __double2float_ru(mul(thr, 1.0 + 0x1p-22));
-  reinterpret_cast<unsigned int *>(t)[7] = (fdfx::ubits(row[37]) != 0ULL) ? 1u : 0u;
+  // rounded up with a little headroom: thr32 * (1 - 2^-24) >= thr, which the error bound uses;
+  // a degenerate cell carries the sign bit
+  float thr32 = __double2float_ru(mul(thr, 1.0 + 0x1p-22));
+  if (fdfx::ubits(row[37]) != 0ULL) thr32 = -fabsf(thr32) - 1.0f;
+  t[3] = thr32;
+  t[7] = __double2float_ru(cell_margin(planes, coor, g, i, j, k));
   for (int f = 0; f < 6; ++f) {
     const double *p = row + 6 * f;
     float *o = t + 8 + 6 * f;
@@ -102,18 +162,201 @@ __device__ __forceinline__ double exact_face(const double *__restrict__ row64, i
   return dd;
 }
 
+// One cell evaluated for the form's position: the face classes the walk needs, the
+// distances the weights use, and (CERT) whether every face is positive by more than
+// thr + the cell's overlap margin, which the FP32 bound certifies without FP64.
+struct Eval32 {
+  unsigned int neg;   // bit f: face f negative
+  bool zero;          // some face within its threshold
+  bool degenerate;
+  bool clear;
+  float dv[6];
+};
+
+template <bool CERT>
+__device__ __forceinline__ void eval_cell32(const float *__restrict__ table, const double *__restrict__ planes,
+                                            long long cur, float2 px, float2 py, float2 pz, float sx, float sy,
+                                            float sz, Eval32 &e, unsigned long long &fb) {
+  const float4 *row = reinterpret_cast<const float4 *>(table + cur * FDF_ROW32);
+  const float4 h0 = __ldg(row), h1 = __ldg(row + 1);
+  e.neg = 0u;
+  e.zero = false;
+  e.clear = CERT;
+  e.degenerate = (__float_as_uint(h0.w) >> 31) != 0u;
+  if (e.degenerate) return;
+  const float thr32 = h0.w;
+  const float prx = __fadd_rn(__fsub_rn(px.x, h0.x), __fsub_rn(px.y, h1.x));
+  const float pry = __fadd_rn(__fsub_rn(py.x, h0.y), __fsub_rn(py.y, h1.y));
+  const float prz = __fadd_rn(__fsub_rn(pz.x, h0.z), __fsub_rn(pz.y, h1.z));
+  // the split term u32 (|ph| + |c0h|) of the bound, per component
+  const float ex = __fmul_rn(__fadd_rn(sx, fabsf(h0.x)), 5.9604644775390625e-8f);
+  const float ey = __fmul_rn(__fadd_rn(sy, fabsf(h0.y)), 5.9604644775390625e-8f);
+  const float ez = __fmul_rn(__fadd_rn(sz, fabsf(h0.z)), 5.9604644775390625e-8f);
+  float fr[36];   // per face: fcr (3), n32 (3); nine 16-B loads
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const float4 v = __ldg(row + 2 + q);
+    fr[4 * q] = v.x; fr[4 * q + 1] = v.y; fr[4 * q + 2] = v.z; fr[4 * q + 3] = v.w;
+  }
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    const float fx = fr[6 * f], fy = fr[6 * f + 1], fz = fr[6 * f + 2];
+    const float nx = fr[6 * f + 3], ny = fr[6 * f + 4], nz = fr[6 * f + 5];
+    const float tx = __fsub_rn(fx, prx), ty = __fsub_rn(fy, pry), tz = __fsub_rn(fz, prz);
+    const float d32 = __fmaf_rn(tz, nz, __fmaf_rn(ty, ny, __fmul_rn(tx, nx)));
+    const float S = __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fz), fabsf(prz)), ez), fabsf(nz),
+                              __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fy), fabsf(pry)), ey), fabsf(ny),
+                                        __fmul_rn(__fadd_rn(__fadd_rn(fabsf(fx), fabsf(prx)), ex), fabsf(nx))));
+    const float M = __fadd_rn(__fmul_rn(S, 12.0f * 5.9604644775390625e-8f), thr32);
+    if (d32 > M) {
+      e.dv[f] = d32;
+      if (CERT) e.clear = e.clear && d32 > __fadd_ru(M, h1.w);
+    } else if (d32 < -M) {
+      e.neg |= 1u << f;
+      e.dv[f] = d32;
+      if (CERT) e.clear = false;
+    } else {
+      const double d64 = exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py), pair_value(pz));
+      if (fdfx::lt0(d64)) e.neg |= 1u << f;
+      e.zero = e.zero || fdfx::eq0(d64);
+      e.dv[f] = __double2float_rn(d64);
+      if (CERT) e.clear = false;
+      ++fb;
+    }
+  }
+}
+
+// The reference walk from (i, j, k) for at most `limit` evaluations, with Brent cycle
+// detection (a revisited cell repeats forever, which the reference ends as LOST after
+// MAX_TRAVERSAL evaluations).
+struct Walk32 {
+  int i, j, k, steps, evaluated;
+  bool concluded, lost, cycle;
+  unsigned int err;
+  Eval32 e;
+};
+
+__device__ __forceinline__ void walk_ref32(const float *__restrict__ table, const double *__restrict__ planes,
+                                           const GridDims &g, float2 px, float2 py, float2 pz, int limit, Walk32 &w,
+                                           unsigned long long &fb) {
+  const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
+  long long saved = -1;
+  int power = 1, lam = 0;
+  w.steps = 0; w.evaluated = 0;
+  w.concluded = false; w.lost = false; w.cycle = false;
+  while (!w.concluded && w.steps < limit) {
+    ++w.steps;
+    if (w.i < 0 || w.i >= g.IM || w.j < 0 || w.j >= g.JM || w.k < 0 || w.k >= g.KM) { w.lost = true; break; }
+    const long long cur = ((long long)w.k * g.JM + w.j) * g.IM + w.i;
+    if (cur == saved) { w.cycle = true; w.lost = true; break; }
+    if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
+    eval_cell32<false>(table, planes, cur, px, py, pz, sx, sy, sz, w.e, fb);
+    if (w.e.degenerate) { w.err |= ERRBIT_DEGENERATE; w.lost = true; break; }
+    ++w.evaluated;
+    if (!w.e.neg || w.e.zero) {
+      w.concluded = true;
+    } else {
+      const unsigned int ng = w.e.neg;
+      if (ng & (1u << F_FRONT)) w.k += 1; else if (ng & (1u << F_BACK)) w.k -= 1;
+      if (ng & (1u << F_LEFT)) w.i -= 1; else if (ng & (1u << F_RIGHT)) w.i += 1;
+      if (ng & (1u << F_BOTTOM)) w.j -= 1; else if (ng & (1u << F_TOP)) w.j += 1;
+    }
+  }
+}
+
+// Writes the located (or LOST) particle: weights (UpdateParticleWeights in FP32: clamp
+// d <= 1e-14, then the three ratios), cell and status.
+__device__ __forceinline__ void store_located32(const SwarmBuf &b, int s, const GridDims &g, bool lost, int i, int j,
+                                                int k, float (&dv)[6]) {
+  if (lost) {
+    b.cell[s] = -1;
+    b.status[s] = ST_LOST;
+    return;
+  }
+#pragma unroll
+  for (int f = 0; f < 6; ++f)
+    if (!(dv[f] > 1e-14f)) dv[f] = (dv[f] != dv[f]) ? dv[f] : 1e-14f;
+  b.a1f[s] = __fdiv_rn(dv[F_LEFT], __fadd_rn(dv[F_LEFT], dv[F_RIGHT]));
+  b.a2f[s] = __fdiv_rn(dv[F_BOTTOM], __fadd_rn(dv[F_BOTTOM], dv[F_TOP]));
+  b.a3f[s] = __fdiv_rn(dv[F_BACK], __fadd_rn(dv[F_FRONT], dv[F_BACK]));
+  b.cell[s] = (int)(((long long)k * g.JM + j) * g.IM + i);
+  b.status[s] = ST_ACTIVE_AND_LOCATED;
+}
+
+// Sort key of a particle whose location is final, with IsParticleInBox on the form's
+// position: decided in FP32 when the hi parts are clear of the box faces by more than the
+// lo parts and rounding can move them (fbox = the box shrunk accordingly), exactly in
+// FP64 otherwise.
+__device__ __forceinline__ unsigned int settle_key32(bool lost, int cell, float2 px, float2 py, float2 pz,
+                                                     int drop_removed, const double *__restrict__ bbox,
+                                                     const float *__restrict__ fbox, unsigned int sentinel,
+                                                     unsigned long long &my_lost, unsigned long long &my_oob,
+                                                     unsigned long long &my_lost_total) {
+  unsigned int key = lost ? sentinel : (unsigned int)cell;
+  if (lost) my_lost_total += 1;
+  if (drop_removed) {
+    if (lost) {
+      my_lost += 1;
+    } else {
+      const float4 fb0 = *reinterpret_cast<const float4 *>(fbox), fb1 = *reinterpret_cast<const float4 *>(fbox + 4);
+      const bool surely_in = px.x > fb0.x && px.x < fb1.x && py.x > fb0.y && py.x < fb1.y && pz.x > fb0.z &&
+                             pz.x < fb1.z;
+      bool inside = surely_in;
+      if (!surely_in) {
+        const double x = pair_value(px), y = pair_value(py), z = pair_value(pz);
+        inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
+      }
+      if (!inside) { my_oob += 1; key = sentinel; }
+    }
+  }
+  return key;
+}
+
+struct LocCounts {
+  unsigned long long lost = 0, oob = 0, evals = 0, done = 0, lost_total = 0, fb = 0;
+  unsigned int err = 0;
+};
+
+// Warp-aggregated histogram of the kept keys and the counters (all 32 lanes call it).
+__device__ __forceinline__ void flush_counts(unsigned int hkey, unsigned int *__restrict__ count, LocCounts &m,
+                                             DevCounters *cnt) {
+  const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
+  const int lane = threadIdx.x & 31;
+  if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
+  const unsigned long long lost = warp_sum_u64(m.lost), oob = warp_sum_u64(m.oob), evals = warp_sum_u64(m.evals),
+                           done = warp_sum_u64(m.done), lt = warp_sum_u64(m.lost_total), fb = warp_sum_u64(m.fb);
+  const unsigned int err = __reduce_or_sync(0xffffffffu, m.err);
+  if (lane == 0) {
+    if (lost) atomicAdd(&cnt->removed_lost, lost);
+    if (oob) atomicAdd(&cnt->removed_oob, oob);
+    if (evals) atomicAdd(&cnt->evals, evals);
+    if (done) atomicAdd(&cnt->evals_total, done);
+    if (lt) atomicAdd(&cnt->lost_total, lt);
+    if (fb) { atomicAdd(&cnt->fallbacks, fb); atomicAdd(&cnt->fallbacks_total, fb); }
+    if (err) atomicOr(&cnt->err, err);
+  }
+  m = LocCounts();
+}
+
+// Advect + locate, one thread per particle.
+//   FIRST == false: the reference walk from the previous cell (or cell (0,0,0)).
+//   FIRST == true:  the reference's first evaluation only, in the previous cell; a particle
+//                   that it does not conclude is appended to `pending` and finished by
+//                   k_locate32_guess (its key and histogram entry are written there).
+template <bool FIRST>
 __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
                                                   int reset_first, const double *__restrict__ bbox,
                                                   const float *__restrict__ fbox, int drop_removed,
                                                   DevCounters *cnt, unsigned int *__restrict__ keys,
-                                                  unsigned int *__restrict__ count, unsigned int sentinel) {
+                                                  unsigned int *__restrict__ count, unsigned int sentinel,
+                                                  unsigned int *__restrict__ pending) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
-  unsigned long long my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0, my_fb = 0;
-  unsigned int my_err = 0;
+  LocCounts m;
   unsigned int hkey = 0xffffffffu;
+  bool wait = false;
   if (s < n) {
     float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
     if (advect) {   // FP32 displacement added to the (hi, lo) position
@@ -127,148 +370,136 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
     int cell = b.cell[s];
     bool lost = false;
     if (st != ST_ACTIVE_AND_LOCATED) {
-      int i = 0, j = 0, k = 0;
-      if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, i, j, k);
-      int steps = 0, evaluated = 0;
-      bool concluded = false, cycle = false;
-      long long saved = -1;
-      int power = 1, lam = 0;
-      float dv[6];       // distances used for the weights
-      bool negf[6];
-      const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
-      while (!concluded && steps < FDF_MAX_TRAVERSAL) {
-        ++steps;
-        if (i < 0 || i >= g.IM || j < 0 || j >= g.JM || k < 0 || k >= g.KM) { lost = true; break; }
-        const long long cur = ((long long)k * g.JM + j) * g.IM + i;
-        if (cur == saved) { cycle = true; lost = true; break; }
-        if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
-        const float4 *row = reinterpret_cast<const float4 *>(table + cur * FDF_ROW32);
-        const float4 h0 = __ldg(row), h1 = __ldg(row + 1);
-        const float thr32 = h0.w;
-        if (__float_as_uint(h1.w) != 0u) { my_err |= ERRBIT_DEGENERATE; lost = true; break; }
-        ++evaluated;
-        const float prx = __fadd_rn(__fsub_rn(px.x, h0.x), __fsub_rn(px.y, h1.x));
-        const float pry = __fadd_rn(__fsub_rn(py.x, h0.y), __fsub_rn(py.y, h1.y));
-        const float prz = __fadd_rn(__fsub_rn(pz.x, h0.z), __fsub_rn(pz.y, h1.z));
-        // the split term u32 (|ph| + |c0h|) of the bound, per component
-        const float ex = __fmul_rn(__fadd_rn(sx, fabsf(h0.x)), 5.9604644775390625e-8f);
-        const float ey = __fmul_rn(__fadd_rn(sy, fabsf(h0.y)), 5.9604644775390625e-8f);
-        const float ez = __fmul_rn(__fadd_rn(sz, fabsf(h0.z)), 5.9604644775390625e-8f);
-        float fr[36];   // per face: fcr (3), n32 (3); nine 16-B loads
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-          const float4 v = __ldg(row + 2 + q);
-          fr[4 * q] = v.x; fr[4 * q + 1] = v.y; fr[4 * q + 2] = v.z; fr[4 * q + 3] = v.w;
-        }
-        bool neg = false, zero = false;
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
-          const float fx = fr[6 * f], fy = fr[6 * f + 1], fz = fr[6 * f + 2];
-          const float nx = fr[6 * f + 3], ny = fr[6 * f + 4], nz = fr[6 * f + 5];
-          const float tx = __fsub_rn(fx, prx), ty = __fsub_rn(fy, pry), tz = __fsub_rn(fz, prz);
-          const float d32 = __fmaf_rn(tz, nz, __fmaf_rn(ty, ny, __fmul_rn(tx, nx)));
-          const float S = __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fz), fabsf(prz)), ez), fabsf(nz),
-                                    __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fy), fabsf(pry)), ey), fabsf(ny),
-                                              __fmul_rn(__fadd_rn(__fadd_rn(fabsf(fx), fabsf(prx)), ex),
-                                                        fabsf(nx))));
-          const float M = __fadd_rn(__fmul_rn(S, 12.0f * 5.9604644775390625e-8f), thr32);
-          bool ng, zr;
-          float dval;
-          if (d32 > M) {
-            ng = false; zr = false; dval = d32;
-          } else if (d32 < -M) {
-            ng = true; zr = false; dval = d32;
-          } else {
-            const double d64 = exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py),
-                                          pair_value(pz));
-            ng = fdfx::lt0(d64);
-            zr = fdfx::eq0(d64);
-            dval = __double2float_rn(d64);
-            ++my_fb;
-          }
-          negf[f] = ng;
-          dv[f] = dval;
-          neg |= ng;
-          zero |= zr;
-        }
-        if (!neg || zero) {
-          concluded = true;
-        } else {
-          if (negf[F_FRONT]) k += 1; else if (negf[F_BACK]) k -= 1;
-          if (negf[F_LEFT]) i -= 1; else if (negf[F_RIGHT]) i += 1;
-          if (negf[F_BOTTOM]) j -= 1; else if (negf[F_TOP]) j += 1;
-        }
-      }
-      my_evals = (unsigned long long)(cycle ? FDF_MAX_TRAVERSAL : steps);
-      my_done = (unsigned long long)evaluated;
-      if (lost || !concluded) {
-        lost = true;
-        cell = -1;
-        st = ST_LOST;
+      Walk32 w;
+      w.i = 0; w.j = 0; w.k = 0; w.err = 0u;
+      if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, w.i, w.j, w.k);
+      walk_ref32(table, planes, g, px, py, pz, FIRST ? 1 : FDF_MAX_TRAVERSAL, w, m.fb);
+      m.err |= w.err;
+      m.done += (unsigned long long)w.evaluated;
+      // learned form: the walk's next cell (w.i, w.j, k) is where the reference continues;
+      // outside the grid it ends there as LOST, as the reference's next loop test does
+      const bool next_inside = w.i >= 0 && w.i < g.IM && w.j >= 0 && w.j < g.JM && w.k >= 0 && w.k < g.KM;
+      if (FIRST && !w.concluded && !w.lost && next_inside) {
+        wait = true;
+        m.evals += (unsigned long long)w.evaluated;
+        b.cell[s] = (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
       } else {
-        // UpdateParticleWeights in FP32 (clamp d <= 1e-14, then the three ratios)
-#pragma unroll
-        for (int f = 0; f < 6; ++f)
-          if (!(dv[f] > 1e-14f)) dv[f] = (dv[f] != dv[f]) ? dv[f] : 1e-14f;
-        b.a1f[s] = __fdiv_rn(dv[F_LEFT], __fadd_rn(dv[F_LEFT], dv[F_RIGHT]));
-        b.a2f[s] = __fdiv_rn(dv[F_BOTTOM], __fadd_rn(dv[F_BOTTOM], dv[F_TOP]));
-        b.a3f[s] = __fdiv_rn(dv[F_BACK], __fadd_rn(dv[F_FRONT], dv[F_BACK]));
-        cell = (int)(((long long)k * g.JM + j) * g.IM + i);
-        st = ST_ACTIVE_AND_LOCATED;
+        m.evals += FIRST ? (unsigned long long)w.evaluated
+                         : (unsigned long long)(w.cycle ? FDF_MAX_TRAVERSAL : w.steps);
+        lost = w.lost || !w.concluded;
+        store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
+        cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
       }
-      b.cell[s] = cell;
-      b.status[s] = st;
     } else {
       lost = (cell < 0);
     }
-    unsigned int key = lost ? sentinel : (unsigned int)cell;
-    if (lost) my_lost_total = 1;
-    if (drop_removed) {
-      if (lost) {
-        my_lost = 1;
-      } else {
-        // IsParticleInBox on the form's position: decided in FP32 when the hi parts are
-        // clear of the box faces by more than the lo parts and rounding can move them
-        // (fbox = the box rounded outwards/inwards), exactly in FP64 otherwise.
-        const float4 fb0 = *reinterpret_cast<const float4 *>(fbox), fb1 = *reinterpret_cast<const float4 *>(fbox + 4);
-        const float4 fb2 = *reinterpret_cast<const float4 *>(fbox + 8);
-        // fb0 = (lo_in x, y, z, -), fb1 = (hi_in x, y, z, -): strictly inside; fb2 = margin scale
-        const bool surely_in = px.x > fb0.x && px.x < fb1.x && py.x > fb0.y && py.x < fb1.y && pz.x > fb0.z &&
-                               pz.x < fb1.z;
-        bool inside = surely_in;
-        if (!surely_in) {
-          const double x = pair_value(px), y = pair_value(py), z = pair_value(pz);
-          inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
-        }
-        (void)fb2;
-        if (!inside) { my_oob = 1; key = sentinel; }
-      }
+    if (!wait) {
+      const unsigned int key =
+          settle_key32(lost, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
+      keys[s] = key;
+      if (key < sentinel) hkey = key;
+      else if (!drop_removed) hkey = sentinel;
     }
-    keys[s] = key;
-    if (key < sentinel) hkey = key;
-    else if (!drop_removed) hkey = sentinel;
   }
-  {
-    const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
-    const int lane = threadIdx.x & 31;
-    if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
+  if (FIRST) {
+    const unsigned int ask = __ballot_sync(0xffffffffu, wait);
+    if (ask) {
+      const int lane = threadIdx.x & 31;
+      unsigned long long base = 0;
+      if (lane == __ffs(ask) - 1) base = atomicAdd(&cnt->pending, (unsigned long long)__popc(ask));
+      base = __shfl_sync(0xffffffffu, base, __ffs(ask) - 1);
+      if (wait) pending[base + __popc(ask & ((1u << lane) - 1u))] = (unsigned int)s;
+    }
   }
-  my_lost = warp_sum_u64(my_lost);
-  my_oob = warp_sum_u64(my_oob);
-  my_evals = warp_sum_u64(my_evals);
-  my_done = warp_sum_u64(my_done);
-  my_lost_total = warp_sum_u64(my_lost_total);
-  my_fb = warp_sum_u64(my_fb);
-  my_err = __reduce_or_sync(0xffffffffu, my_err);
-  if ((threadIdx.x & 31) == 0) {
-    if (my_lost) atomicAdd(&cnt->removed_lost, my_lost);
-    if (my_oob) atomicAdd(&cnt->removed_oob, my_oob);
-    if (my_evals) atomicAdd(&cnt->evals, my_evals);
-    if (my_done) atomicAdd(&cnt->evals_total, my_done);
-    if (my_lost_total) atomicAdd(&cnt->lost_total, my_lost_total);
-    if (my_fb) { atomicAdd(&cnt->fallbacks, my_fb); atomicAdd(&cnt->fallbacks_total, my_fb); }
-    if (my_err) atomicOr(&cnt->err, my_err);
+  flush_counts(hkey, count, m, cnt);
+}
+
+// The particles that left their previous cell (the list from k_locate32<true>, whose
+// cell field now holds the reference walk's second cell P1): the walk starts in the
+// learned guess and runs for at most FDF_GUESS_WALK evaluations.  Its cell C is taken
+// when C == P1 (the reference evaluates P1 next and concludes there with the same exact
+// decisions), or when it ends with every face positive by more than thr + C's overlap
+// margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise the reference
+// walk continues from P1 as its second evaluation.  Grid-stride over the list,
+// warp-uniform trip count.
+__global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
+                                                        const double *__restrict__ planes,
+                                                        const double *__restrict__ bbox,
+                                                        const float *__restrict__ fbox, int drop_removed,
+                                                        DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                        unsigned int *__restrict__ count, unsigned int sentinel,
+                                                        const unsigned int *__restrict__ pending,
+                                                        const int *__restrict__ guess) {
+  const long long npend = (long long)cnt->pending;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  unsigned long long acc = 0, gev = 0;
+  for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < npend; base += stride) {
+    const long long t = base + lane;
+    LocCounts m;
+    unsigned int hkey = 0xffffffffu;
+    if (t < npend) {
+      const int s = (int)pending[t];
+      const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
+      const int prev = b.cell[s];
+      int pi = 0, pj = 0, pk = 0;
+      if (prev >= 0 && (long long)prev < g.Nc) cell_ijk(g, (unsigned int)prev, pi, pj, pk);
+      // walk from the guess
+      Eval32 e;
+      int gi, gj, gk;
+      cell_ijk(g, (unsigned int)guess[t], gi, gj, gk);
+      const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
+      bool taken = false;
+      for (int step = 0; step < FDF_GUESS_WALK; ++step) {
+        if (gi < 0 || gi >= g.IM || gj < 0 || gj >= g.JM || gk < 0 || gk >= g.KM) break;
+        const long long cur = ((long long)gk * g.JM + gj) * g.IM + gi;
+        eval_cell32<true>(table, planes, cur, px, py, pz, sx, sy, sz, e, m.fb);
+        if (e.degenerate) break;
+        ++m.done; ++m.evals; ++gev;
+        if (!e.neg || e.zero) {
+          taken = (gi == pi && gj == pj && gk == pk) ||
+                  (e.clear && abs(gi - pi) <= FDF_GUESS_REACH && abs(gj - pj) <= FDF_GUESS_REACH &&
+                   abs(gk - pk) <= FDF_GUESS_REACH);
+          break;
+        }
+        const unsigned int ng = e.neg;
+        if (ng & (1u << F_FRONT)) gk += 1; else if (ng & (1u << F_BACK)) gk -= 1;
+        if (ng & (1u << F_LEFT)) gi -= 1; else if (ng & (1u << F_RIGHT)) gi += 1;
+        if (ng & (1u << F_BOTTOM)) gj -= 1; else if (ng & (1u << F_TOP)) gj += 1;
+      }
+      bool lost;
+      int cell;
+      if (taken) {
+        ++acc;
+        lost = false;
+        store_located32(b, s, g, false, gi, gj, gk, e.dv);
+        cell = (int)(((long long)gk * g.JM + gj) * g.IM + gi);
+      } else {
+        Walk32 w;   // the reference walk from its second evaluation on (one step already made)
+        w.i = pi; w.j = pj; w.k = pk; w.err = 0u;
+        walk_ref32(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w, m.fb);
+        m.err |= w.err;
+        m.done += (unsigned long long)w.evaluated;
+        m.evals += (unsigned long long)w.evaluated;
+        lost = w.lost || !w.concluded;
+        store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
+        cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
+      }
+      const unsigned int key =
+          settle_key32(lost, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
+      keys[s] = key;
+      if (key < sentinel) hkey = key;
+      else if (!drop_removed) hkey = sentinel;
+    }
+    flush_counts(hkey, count, m, cnt);
   }
+  acc = warp_sum_u64(acc);
+  gev = warp_sum_u64(gev);
+  if (lane == 0) {
+    if (acc) atomicAdd(&cnt->guess_taken_total, acc);
+    if (gev) atomicAdd(&cnt->guess_evals_total, gev);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->guess_asked_total, (unsigned long long)npend);
 }
 
 // Corner field in FP32: mean of the valid adjacent cells (nodes next to occupied cells).
@@ -496,9 +727,27 @@ void launch_build_table32(const double *planes, const double *coor, GridDims g, 
 
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                     unsigned int *keys, unsigned int *count, unsigned int sentinel, cudaStream_t s) {
-  k_locate32<<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox, fbox,
-                                                    drop_removed, cnt, keys, count, sentinel);
+                     unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
+                     cudaStream_t s) {
+  if (pending)
+    k_locate32<true><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox,
+                                                            fbox, drop_removed, cnt, keys, count, sentinel, pending);
+  else
+    k_locate32<false><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed,
+                                                             bbox, fbox, drop_removed, cnt, keys, count, sentinel,
+                                                             nullptr);
+}
+
+void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
+                           const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
+                           unsigned int *keys, unsigned int *count, unsigned int sentinel,
+                           const unsigned int *pending, const int *guess, int num_sms, cudaStream_t s) {
+  long long blocks = ((long long)n_cap + 255) / 256;
+  const long long cap = (long long)num_sms * 8;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  k_locate32_guess<<<(unsigned)blocks, 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
+                                                    sentinel, pending, guess);
 }
 
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,

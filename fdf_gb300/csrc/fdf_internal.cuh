@@ -19,11 +19,13 @@
 #include <cuda_runtime.h>
 
 #define FDF_ROW 38            // doubles per plane-table row (36 plane values + thr + flag)
-#define FDF_ROW32 44          // floats per precision-form row (c0 as 3 doubles, thr32, flag, 36 face values)
+#define FDF_ROW32 44          // floats per precision-form row (c0 pair, thr32, overlap margin, 36 face values)
 #define FDF_MAX_TRAVERSAL 1000
 #define FDF_DISTANCE_THRESHOLD 1e-11
 #define FDF_INTERP_DIST_TOL 1e-14
 #define FDF_BBOX_TOL 1e-6
+#define FDF_GUESS_WALK 8      // evaluations allowed to the walk from a learned guess
+#define FDF_GUESS_REACH 16    // largest index distance from the previous cell a guess may settle at
 
 // Face order of the reference (common.h Face enum).
 enum { F_LEFT = 0, F_RIGHT = 1, F_BOTTOM = 2, F_TOP = 3, F_FRONT = 4, F_BACK = 5 };
@@ -42,6 +44,7 @@ struct DevCounters {
   unsigned long long evals;        // walk evaluations the reference makes for this run (cycles count MAX_TRAVERSAL)
   unsigned long long lost_total;
   unsigned long long fallbacks;    // precision form: faces decided by the exact FP64 distance
+  unsigned long long pending;      // learned form: particles that left their previous cell
   // kept across runs
   unsigned int err;
   unsigned int pad;
@@ -51,6 +54,9 @@ struct DevCounters {
   unsigned long long evals_total;   // walk evaluations actually made, all pipeline runs (never reset per step)
   unsigned long long nodes_total;   // corner nodes computed by the steps (never reset per step)
   unsigned long long fallbacks_total;
+  unsigned long long guess_asked_total;   // learned form: particles given a learned start cell
+  unsigned long long guess_taken_total;   // ... whose walk from the guess was accepted
+  unsigned long long guess_evals_total;   // ... evaluations made by the walks from the guess
 };
 
 struct SwarmBuf {
@@ -147,9 +153,17 @@ void launch_swarm_to_aos(const SwarmBuf &b, int n, GridDims g, double *pos, doub
 void launch_build_table32(const double *planes, const double *coor, GridDims g, float *table, cudaStream_t s);
 // fbox: 12 floats, (x, y, z, -) lower and (x, y, z, -) upper bounds strictly inside the
 // bounding box by more than any lo part of a position inside it, then 4 unused.
+// pending != nullptr: the learned form's first pass (one evaluation in the previous cell;
+// particles that leave it are appended to pending and counted in cnt->pending).
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                     unsigned int *keys, unsigned int *count, unsigned int sentinel, cudaStream_t s);
+                     unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
+                     cudaStream_t s);
+// The learned form's second pass over pending[0 .. cnt->pending), guess[t] = start cell.
+void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
+                           const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
+                           unsigned int *keys, unsigned int *count, unsigned int sentinel,
+                           const unsigned int *pending, const int *guess, int num_sms, cudaStream_t s);
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
                                unsigned long long *nodes_done, cudaStream_t s);
 void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,

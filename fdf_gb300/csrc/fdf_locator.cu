@@ -1,0 +1,428 @@
+// fdf_locator.cu -- C ABI of the learned start-cell locator (FDF_FORM_LEARNED_FP32):
+// parameter set-up, training on location pairs produced by the walking search, gradients
+// for checking, and inference.  No counterpart in the reference, which starts every walk
+// in the particle's previous cell (walkingsearch.c:571-626, InitializeTraversalParameters).
+//
+// Training (all on the context stream, deterministic):
+//   samples   n points seeded like the volumetric initialisation (random cell, random
+//             logical coordinates), each located by the plain FP64 walk from its generating
+//             cell; the located (position, cell) pairs become (xhat, target) in FP32
+//   step t    minibatch by counter hash -> forward (4 tensor-core GEMMs, bias + SiLU) ->
+//             loss and dloss/dy -> backward (dW by split-K GEMMs reduced in fixed order,
+//             dH by GEMMs, SiLU', bias sums) -> Adam on the FP32 master weights ->
+//             bfloat16 copy for the next step
+//   finally   weights packed in mma fragment order for the inference kernel
+#include "fdf_context.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+struct TrainScratch {
+  __nv_bfloat16 *X, *H[4], *Gb, *Gb4;
+  float *T, *C, *Z[4], *dH, *G, *Y, *G4, *loss_part, *partials;
+  int splits;
+};
+
+int splits_for(int B) {
+  int sp = B / 256;
+  if (sp < 1) sp = 1;
+  if (sp > 64) sp = 64;
+  return sp;
+}
+
+size_t scratch_bytes(int B) {
+  const size_t r = 256;
+  auto up = [&](size_t b) { return (b + r - 1) / r * r; };
+  const size_t bh = (size_t)B * MLP_H;
+  size_t t = 0;
+  t += up(2 * 3 * (size_t)B);                      // X
+  t += 3 * up(2 * bh);                             // H1..H3
+  t += up(2 * bh) + up(2 * 3 * (size_t)B);         // Gb, Gb4
+  t += up(4 * 3 * (size_t)B);                      // T
+  t += up(4 * bh);                                 // C
+  t += 3 * up(4 * bh);                             // Z1..Z3
+  t += 2 * up(4 * bh);                             // dH, G
+  t += 2 * up(4 * 3 * (size_t)B);                  // Y, G4
+  t += up(4 * ((size_t)B / 256 + 2));              // loss partials
+  t += up(4 * (size_t)splits_for(B) * MLP_H * MLP_H);
+  return t;
+}
+
+TrainScratch carve_scratch(void *base, int B) {
+  char *p = (char *)base;
+  auto take = [&](size_t bytes) {
+    char *r = p;
+    p += (bytes + 255) / 256 * 256;
+    return (void *)r;
+  };
+  const size_t bh = (size_t)B * MLP_H;
+  TrainScratch s{};
+  s.X = (__nv_bfloat16 *)take(2 * 3 * (size_t)B);
+  s.H[0] = s.X;
+  for (int l = 1; l < 4; ++l) s.H[l] = (__nv_bfloat16 *)take(2 * bh);
+  s.Gb = (__nv_bfloat16 *)take(2 * bh);
+  s.Gb4 = (__nv_bfloat16 *)take(2 * 3 * (size_t)B);
+  s.T = (float *)take(4 * 3 * (size_t)B);
+  s.C = (float *)take(4 * bh);
+  s.Z[0] = nullptr;
+  for (int l = 1; l < 4; ++l) s.Z[l] = (float *)take(4 * bh);
+  s.dH = (float *)take(4 * bh);
+  s.G = (float *)take(4 * bh);
+  s.Y = (float *)take(4 * 3 * (size_t)B);
+  s.G4 = (float *)take(4 * 3 * (size_t)B);
+  s.loss_part = (float *)take(4 * ((size_t)B / 256 + 2));
+  s.splits = splits_for(B);
+  s.partials = (float *)take(4 * (size_t)s.splits * MLP_H * MLP_H);
+  return s;
+}
+
+int alloc_params(FdfContext *ctx) {
+  LocatorState &L = ctx->loc;
+  if (L.params) return FDF_SUCCESS;
+  CU(cudaMalloc((void **)&L.params, 4ull * MLP_NPARAM));
+  CU(cudaMalloc((void **)&L.grads, 4ull * MLP_NPARAM));
+  CU(cudaMalloc((void **)&L.adam_m, 4ull * MLP_NPARAM));
+  CU(cudaMalloc((void **)&L.adam_v, 4ull * MLP_NPARAM));
+  CU(cudaMalloc((void **)&L.params_bf, 2ull * MLP_NPARAM));
+  CU(cudaMalloc((void **)&L.frag, sizeof(uint2) * (size_t)MLP_FRAG_WORDS));
+  CU(cudaMalloc((void **)&L.bias, 4ull * MLP_BIAS_WORDS));
+  return FDF_SUCCESS;
+}
+
+int ensure_scratch(FdfContext *ctx, int B) {
+  LocatorState &L = ctx->loc;
+  if (L.batch_cap >= B && L.scratch) return FDF_SUCCESS;
+  cfree(L.scratch);
+  L.batch_cap = 0;
+  CU(cudaMalloc(&L.scratch, scratch_bytes(B)));
+  L.batch_cap = B;
+  return FDF_SUCCESS;
+}
+
+void set_norm(FdfContext *ctx) {
+  LocatorState &L = ctx->loc;
+  for (int d = 0; d < 3; ++d) {
+    const double lo = ctx->bbox_h[d], hi = ctx->bbox_h[3 + d];
+    L.norm.centre[d] = (float)(0.5 * (lo + hi));
+    L.norm.inv_half[d] = (float)(2.0 / (hi - lo));
+  }
+}
+
+// Clears the optimiser state and makes the bfloat16 copy and the inference packing.
+void refresh_weights(FdfContext *ctx, cudaStream_t s) {
+  LocatorState &L = ctx->loc;
+  mlp_to_bf16(L.params, L.params_bf, MLP_NPARAM, s);
+  mlp_pack_frag(L.params + MLP_OFF_W1, MLP_H, 3, 16, 1, L.frag, s);
+  mlp_pack_frag(L.params + MLP_OFF_W2, MLP_H, MLP_H, 16, 8, L.frag + MLP_F2, s);
+  mlp_pack_frag(L.params + MLP_OFF_W3, MLP_H, MLP_H, 16, 8, L.frag + MLP_F3, s);
+  mlp_pack_frag(L.params + MLP_OFF_W4, 3, MLP_H, 1, 8, L.frag + MLP_F4, s);
+  mlp_pack_bias(L.params, L.bias, s);
+  ctx->launches += 6;
+}
+
+// Loss and gradients (into L.grads) of the batch in scratch (X, T), current weights.
+void forward_backward(FdfContext *ctx, const TrainScratch &S, int B, float *loss_out, cudaStream_t s) {
+  LocatorState &L = ctx->loc;
+  const __nv_bfloat16 *Wb[4] = {L.params_bf + MLP_OFF_W1, L.params_bf + MLP_OFF_W2, L.params_bf + MLP_OFF_W3,
+                                L.params_bf + MLP_OFF_W4};
+  const float *bvec[4] = {L.params + MLP_OFF_B1, L.params + MLP_OFF_B2, L.params + MLP_OFF_B3, L.params + MLP_OFF_B4};
+  float *dW[4] = {L.grads + MLP_OFF_W1, L.grads + MLP_OFF_W2, L.grads + MLP_OFF_W3, L.grads + MLP_OFF_W4};
+  float *db[4] = {L.grads + MLP_OFF_B1, L.grads + MLP_OFF_B2, L.grads + MLP_OFF_B3, L.grads + MLP_OFF_B4};
+  const int fin[4] = {3, MLP_H, MLP_H, MLP_H};
+  // forward: C = H_{l} W_l^T (A = H [B][fin], B(k, n) = W[n][k])
+  for (int l = 0; l < 3; ++l) {
+    mlp_gemm(S.H[l], fin[l], 1, Wb[l], 1, fin[l], S.C, MLP_H, 1, B, MLP_H, fin[l], 1, nullptr, s);
+    mlp_bias_silu(S.C, bvec[l], B, MLP_H, S.Z[l + 1], S.H[l + 1], s);
+  }
+  mlp_gemm(S.H[3], MLP_H, 1, Wb[3], 1, MLP_H, S.C, 3, 1, B, 3, MLP_H, 1, nullptr, s);
+  float sc[3];
+  const int N[3] = {ctx->g.IM, ctx->g.JM, ctx->g.KM};
+  for (int d = 0; d < 3; ++d) sc[d] = 0.5f * (float)N[d];
+  mlp_out_loss(S.C, bvec[3], S.T, B, sc, S.Y, S.G4, S.Gb4, S.loss_part, s);
+  mlp_sum_partials(S.loss_part, (B + 255) / 256, loss_out, s);
+  // backward, layer 4 then 3, 2, 1: g = dloss/dz_l (FP32 G, bfloat16 Gb)
+  const __nv_bfloat16 *gb = S.Gb4;
+  const float *g = S.G4;
+  int nout = 3;
+  for (int l = 3; l >= 0; --l) {
+    // dW_l [nout][fin] = sum_b gb[b][o] h_l[b][i]: A(m = o, k = b) = gb[b*nout + o], B(k = b, n = i) = h[b*fin + i]
+    mlp_gemm(gb, 1, nout, S.H[l], fin[l], 1, dW[l], fin[l], 1, nout, fin[l], B, S.splits, S.partials, s);
+    mlp_colsum(g, B, nout, db[l], s);
+    if (l == 0) break;
+    // dH_l [B][fin] = gb @ W_l: A(m = b, k = o) = gb[b*nout + o], B(k = o, n = i) = W[o*fin + i]
+    mlp_gemm(gb, nout, 1, Wb[l], fin[l], 1, S.dH, MLP_H, 1, B, MLP_H, nout, 1, nullptr, s);
+    mlp_silu_bwd(S.dH, S.Z[l], (long long)B * MLP_H, S.G, S.Gb, s);
+    gb = S.Gb;
+    g = S.G;
+    nout = MLP_H;
+  }
+  ctx->launches += 2 * 3 + 1 + 2 + 4 * 2 + 3 * 2 + 4 * (S.splits > 1 ? 1 : 0);
+}
+
+}  // namespace
+
+void locator_free(FdfContext *ctx) {
+  LocatorState &L = ctx->loc;
+  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf);
+  cfree(L.frag); cfree(L.bias); cfree(L.pending); cfree(L.guess); cfree(L.scratch);
+  L.pending_cap = 0;
+  L.batch_cap = 0;
+  L.has_params = false;
+}
+
+int locator_reserve(FdfContext *ctx) {
+  LocatorState &L = ctx->loc;
+  if (L.pending_cap >= ctx->cap && L.pending) return FDF_SUCCESS;
+  cfree(L.pending); cfree(L.guess);
+  L.pending_cap = 0;
+  CU(cudaMalloc((void **)&L.pending, 4ull * ctx->cap));
+  CU(cudaMalloc((void **)&L.guess, 4ull * ctx->cap));
+  L.pending_cap = ctx->cap;
+  return FDF_SUCCESS;
+}
+
+extern "C" {
+
+int fdf_LocatorInit(FdfContext *ctx, uint64_t seed) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorInit: call fdf_SetGrid first");
+  CU(cudaSetDevice(ctx->device));
+  int r = alloc_params(ctx);
+  if (r) return r;
+  std::vector<float> p(MLP_NPARAM);
+  mlp_init_params_host(seed, p.data());
+  LocatorState &L = ctx->loc;
+  set_norm(ctx);
+  CU(cudaMemcpyAsync(L.params, p.data(), 4ull * MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemsetAsync(L.adam_m, 0, 4ull * MLP_NPARAM, ctx->stream));
+  CU(cudaMemsetAsync(L.adam_v, 0, 4ull * MLP_NPARAM, ctx->stream));
+  L.adam_t = 0;
+  refresh_weights(ctx, ctx->stream);
+  CHECK_LAUNCH();
+  CU(cudaStreamSynchronize(ctx->stream));
+  L.has_params = true;
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorSetParams(FdfContext *ctx, const float *params, int64_t n) {
+  if (!ctx || !params) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorSetParams: null argument");
+  if (n != MLP_NPARAM) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorSetParams: expected FDF_LOCATOR_NPARAM");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorSetParams: call fdf_SetGrid first");
+  CU(cudaSetDevice(ctx->device));
+  int r = alloc_params(ctx);
+  if (r) return r;
+  LocatorState &L = ctx->loc;
+  set_norm(ctx);
+  CU(cudaMemcpyAsync(L.params, params, 4ull * MLP_NPARAM, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemsetAsync(L.adam_m, 0, 4ull * MLP_NPARAM, ctx->stream));
+  CU(cudaMemsetAsync(L.adam_v, 0, 4ull * MLP_NPARAM, ctx->stream));
+  L.adam_t = 0;
+  refresh_weights(ctx, ctx->stream);
+  CHECK_LAUNCH();
+  CU(cudaStreamSynchronize(ctx->stream));
+  L.has_params = true;
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorGetParams(FdfContext *ctx, float *params, int64_t n) {
+  if (!ctx || !params) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorGetParams: null argument");
+  if (n != MLP_NPARAM) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorGetParams: expected FDF_LOCATOR_NPARAM");
+  if (!ctx->loc.has_params) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorGetParams: no locator");
+  CU(cudaSetDevice(ctx->device));
+  CU(cudaMemcpyAsync(params, ctx->loc.params, 4ull * MLP_NPARAM, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorGetNormalization(FdfContext *ctx, float *centre, float *inv_half) {
+  if (!ctx || !centre || !inv_half) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorGetNormalization: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorGetNormalization: no grid");
+  set_norm(ctx);
+  for (int d = 0; d < 3; ++d) { centre[d] = ctx->loc.norm.centre[d]; inv_half[d] = ctx->loc.norm.inv_half[d]; }
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target, int64_t batch, float *grads,
+                         float *loss) {
+  if (!ctx || !xhat || !target || !grads || !loss) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorGradients: null argument");
+  if (batch < 1 || batch > 65536) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorGradients: batch in [1, 65536]");
+  if (!ctx->loc.has_params) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorGradients: no locator");
+  CU(cudaSetDevice(ctx->device));
+  const int B = (int)batch;
+  int r = ensure_scratch(ctx, B);
+  if (r) return r;
+  TrainScratch S = carve_scratch(ctx->loc.scratch, ctx->loc.batch_cap);
+  cudaStream_t s = ctx->stream;
+  // xhat goes through the G buffer (FP32) into X (bfloat16)
+  CU(cudaMemcpyAsync(S.G, xhat, 12ull * B, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(S.T, target, 12ull * B, cudaMemcpyHostToDevice, s));
+  mlp_to_bf16(S.G, S.X, 3 * B, s);
+  float *d_loss = S.loss_part + (B + 255) / 256;
+  forward_backward(ctx, S, B, d_loss, s);
+  CHECK_LAUNCH();
+  CU(cudaMemcpyAsync(grads, ctx->loc.grads, 4ull * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(loss, d_loss, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t steps, int64_t batch, double lr,
+                     float *loss_history) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorTrain: call fdf_SetGrid first");
+  if (n_samples < 1 || n_samples > 0x7fffffffLL || steps < 0 || batch < 16 || batch > 65536 || !(lr > 0.0))
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorTrain: argument out of range");
+  CU(cudaSetDevice(ctx->device));
+  if (!ctx->loc.has_params) {
+    int r = fdf_LocatorInit(ctx, seed);
+    if (r) return r;
+  }
+  LocatorState &L = ctx->loc;
+  set_norm(ctx);
+  cudaStream_t s = ctx->stream;
+  const GridDims &g = ctx->g;
+  const long long n = n_samples;
+  // --- location pairs from the walking search
+  void *tmp_swarm = nullptr;
+  CU(cudaMalloc(&tmp_swarm, swarm_bytes_per_buf((int)n)));
+  SwarmBuf tb;
+  carve_swarm((char *)tmp_swarm, (int)n, tb);
+  DevCounters *tc = nullptr;
+  unsigned int *keys = nullptr, *hist = nullptr, *flag = nullptr, *slot = nullptr, *sums = nullptr;
+  float *xs = nullptr, *ts = nullptr, *hist_loss = nullptr;
+  auto release = [&]() {
+    cudaStreamSynchronize(s);
+    cudaFree(tmp_swarm); cudaFree(tc); cudaFree(keys); cudaFree(hist); cudaFree(flag); cudaFree(slot);
+    cudaFree(sums); cudaFree(xs); cudaFree(ts); cudaFree(hist_loss);
+  };
+#define CUT(call)                                                                    \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      release();                                                                     \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? FDF_ERR_MEM : FDF_ERR_GPU,  \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));               \
+    }                                                                                \
+  } while (0)
+  CUT(cudaMalloc((void **)&tc, sizeof(DevCounters)));
+  CUT(cudaMalloc((void **)&keys, 4ull * n));
+  CUT(cudaMalloc((void **)&hist, 4ull * (g.Nc + 2)));
+  CUT(cudaMalloc((void **)&flag, 4ull * n));
+  CUT(cudaMalloc((void **)&slot, 4ull * n));
+  CUT(cudaMalloc((void **)&sums, 4ull * scan_scratch_words(n)));
+  DevCounters c0{};
+  c0.n = (int)n;
+  c0.n_sorted = (int)n;
+  CUT(cudaMemcpyAsync(tc, &c0, sizeof(c0), cudaMemcpyHostToDevice, s));
+  CUT(cudaMemsetAsync(hist, 0, 4ull * (g.Nc + 2), s));
+  launch_seed(ctx->coor, g, n, seed, 0, 1, 0, 0.0, tb, s);
+  launch_locate(tb, (int)n, g, ctx->planes, 0.0, 0, ctx->bbox, 0, tc, keys, hist, ctx->sentinel, s);
+  mlp_flag_located(tb.cell, tb.status, n, flag, s);
+  CUT(cudaMemcpyAsync(slot, flag, 4ull * n, cudaMemcpyDeviceToDevice, s));
+  exclusive_scan_u32(slot, n, sums, s);
+  CUT(cudaGetLastError());
+  unsigned int last[2] = {0, 0};
+  CUT(cudaMemcpyAsync(&last[0], slot + n - 1, 4, cudaMemcpyDeviceToHost, s));
+  CUT(cudaMemcpyAsync(&last[1], flag + n - 1, 4, cudaMemcpyDeviceToHost, s));
+  unsigned int err = 0;
+  CUT(cudaMemcpyAsync(&err, &tc->err, 4, cudaMemcpyDeviceToHost, s));
+  CUT(cudaStreamSynchronize(s));
+  if (err & ERRBIT_DEGENERATE) {
+    release();
+    return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
+  }
+  const long long m = (long long)last[0] + last[1];
+  if (m == 0) {
+    release();
+    return fail(ctx, FDF_ERR_ARG_WRONG, "fdf_LocatorTrain: the walk located none of the sample points");
+  }
+  CUT(cudaMalloc((void **)&xs, 12ull * m));
+  CUT(cudaMalloc((void **)&ts, 12ull * m));
+  mlp_make_samples(tb.x, tb.y, tb.z, tb.cell, slot, flag, n, L.norm, g, xs, ts, s);
+  ctx->launches += 4 + 3;
+  // --- training
+  const int B = (int)batch;
+  int r = ensure_scratch(ctx, B);
+  if (r) { release(); return r; }
+  TrainScratch S = carve_scratch(L.scratch, L.batch_cap);
+  CUT(cudaMalloc((void **)&hist_loss, 4ull * (steps > 0 ? steps : 1)));
+  const double pi = 3.14159265358979323846;
+  for (long long t = 0; t < steps; ++t) {
+    mlp_gather_batch(xs, ts, m, seed ^ 0x5DEECE66DULL, t, B, S.X, S.T, s);
+    forward_backward(ctx, S, B, hist_loss + t, s);
+    const double lr_t = lr * (0.02 + 0.98 * 0.5 * (1.0 + std::cos(pi * (double)t / (double)steps)));
+    L.adam_t += 1;
+    const double c1 = 1.0 - std::pow(0.9, (double)L.adam_t), c2 = 1.0 - std::pow(0.999, (double)L.adam_t);
+    mlp_adam(L.params, L.grads, L.adam_m, L.adam_v, MLP_NPARAM, (float)lr_t, (float)c1, (float)c2, s);
+    mlp_to_bf16(L.params, L.params_bf, MLP_NPARAM, s);
+    ctx->launches += 3;
+    if ((t & 255) == 255) CUT(cudaGetLastError());
+  }
+  refresh_weights(ctx, s);
+  CUT(cudaGetLastError());
+  if (loss_history && steps > 0)
+    CUT(cudaMemcpyAsync(loss_history, hist_loss, 4ull * steps, cudaMemcpyDeviceToHost, s));
+  CUT(cudaStreamSynchronize(s));
+#undef CUT
+  release();
+  L.has_params = true;
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs) {
+  if (!ctx || (n > 0 && (!position || !cell_id))) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorPredict: null argument");
+  if (n < 0 || n > 0x7fffffffLL) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorPredict: n out of range");
+  if (!ctx->loc.has_params) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorPredict: no locator");
+  if (n == 0) return FDF_SUCCESS;
+  CU(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  std::vector<double> soa(3 * (size_t)n);
+  for (int64_t p = 0; p < n; ++p)
+    for (int d = 0; d < 3; ++d) soa[d * (size_t)n + p] = position[3 * p + d];
+  double *d_pos = nullptr;
+  int *d_guess = nullptr;
+  float *d_out = nullptr;
+  CU(cudaMalloc((void **)&d_pos, 24ull * n));
+  if (cudaMalloc((void **)&d_guess, 4ull * n) != cudaSuccess || cudaMalloc((void **)&d_out, 12ull * n) != cudaSuccess) {
+    cudaFree(d_pos); cudaFree(d_guess);
+    return fail(ctx, FDF_ERR_MEM, "fdf_LocatorPredict: out of device memory");
+  }
+  cudaError_t e = cudaMemcpyAsync(d_pos, soa.data(), 24ull * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    mlp_guess(ctx->loc.frag, ctx->loc.bias, ctx->loc.norm, d_pos, d_pos + n, d_pos + 2 * n, 0, nullptr, nullptr,
+              (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, s, d_out);
+    ctx->launches += 1;
+    e = cudaGetLastError();
+  }
+  std::vector<int> gh((size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(gh.data(), d_guess, 4ull * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && outputs) e = cudaMemcpyAsync(outputs, d_out, 12ull * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d_pos); cudaFree(d_guess); cudaFree(d_out);
+  if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_LocatorPredict: ") + cudaGetErrorString(e));
+  const long long IM = ctx->g.IM, JM = ctx->g.JM;
+  for (int64_t p = 0; p < n; ++p) {
+    const long long c = gh[p];
+    cell_id[3 * p] = c % IM;
+    cell_id[3 * p + 1] = (c / IM) % JM;
+    cell_id[3 * p + 2] = c / (IM * JM);
+  }
+  return FDF_SUCCESS;
+}
+
+int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals) {
+  if (!ctx || !asked || !taken || !guess_evals) return FDF_ERR_ARG_NULL;
+  CU(cudaSetDevice(ctx->device));
+  DevCounters c{};
+  CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  *asked = (int64_t)c.guess_asked_total;
+  *taken = (int64_t)c.guess_taken_total;
+  *guess_evals = (int64_t)c.guess_evals_total;
+  return FDF_SUCCESS;
+}
+
+}  // extern "C"

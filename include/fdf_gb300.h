@@ -69,6 +69,15 @@ typedef struct {
  * with a rigorous error bound, exact FP64 distance where the bound cannot decide). */
 #define FDF_FORM_PLAIN_FP64 0
 #define FDF_FORM_FP32 1
+/* LEARNED_FP32: the FP32 form whose walk, for a particle that has left its previous cell,
+ * starts in the cell a trained network predicts (fdf_Locator*).  The walk from the guess
+ * is kept only when it ends with every face of its cell positive by more than the
+ * threshold plus the cell's overlap margin (the largest gap between the cell's face planes
+ * and the planes of the same grid surfaces on the neighbouring patches), within
+ * FDF_GUESS_REACH = 16 cells of the previous cell in each index; otherwise the reference
+ * walk from the previous cell decides.  Cells, weights and statuses are then those of the
+ * FP32 form except where the reference's own result depends on where its walk starts. */
+#define FDF_FORM_LEARNED_FP32 2
 
 /* ---- context, grid and fields (replace UserCtx set-up: setup.c:197-290, grid.c:34-160) ---- */
 int fdf_ContextCreate(FdfContext **ctx, int device);
@@ -150,6 +159,38 @@ int fdf_SortByCell(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t 
 int fdf_SortByCellNoAlloc(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t *perm, uint32_t *cell_start,
                           void *stream);
 
+/* ---- learned start-cell locator (FDF_FORM_LEARNED_FP32) ----
+ * No counterpart in the reference, which starts each walk in the particle's previous cell
+ * (walkingsearch.c:571-626).  A 3-128-128-128-3 SiLU network maps the normalised position
+ * xhat = (x - centre) * inv_half (centre and half-extent of the grid's bounding box) to
+ * y, read as cell index floor((y_d + 1) N_d / 2), N = (IM, JM, KM), clamped to the grid.
+ * Weights are bfloat16 in every tensor-core product (FP32 accumulation), with FP32 master
+ * copies for training.  Parameters, one float vector of FDF_LOCATOR_NPARAM values:
+ * W1 [128][3], b1 [128], W2 [128][128], b2, W3 [128][128], b3, W4 [3][128], b4 [3]. */
+#define FDF_LOCATOR_NPARAM 33923
+/* Weights uniform in +-1/sqrt(fan_in) from the seed, biases zero; Adam state cleared. */
+int fdf_LocatorInit(FdfContext *ctx, uint64_t seed);
+/* Trains on the device: n_samples points seeded like fdf_SeedParticles (seed), each located
+ * by the plain FP64 walk from its generating cell; the located (position, cell) pairs are
+ * the training set.  `steps` Adam steps on minibatches of `batch` pairs, learning rate lr
+ * on a cosine schedule; loss = mean over the batch of sum_d (N_d/2 (y_d - t_d))^2 / 3 with
+ * t_d = 2 (idx_d + 0.5) / N_d - 1 (squared error in cells).  loss_history (optional,
+ * [steps]) receives the loss of every step.  Initialises the weights first if none are set. */
+int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t steps, int64_t batch, double lr,
+                     float *loss_history);
+int fdf_LocatorSetParams(FdfContext *ctx, const float *params, int64_t n);
+int fdf_LocatorGetParams(FdfContext *ctx, float *params, int64_t n);
+int fdf_LocatorGetNormalization(FdfContext *ctx, float *centre, float *inv_half);
+/* Loss and gradients of the current weights on one batch given on the host: xhat [batch][3]
+ * (already normalised), target [batch][3]; grads [FDF_LOCATOR_NPARAM]. */
+int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target, int64_t batch, float *grads,
+                         float *loss);
+/* Predicted cells (i, j, k) of n host positions [n][3]; outputs (optional) [n][3] = y. */
+int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs);
+/* Running totals of the learned form: particles given a guess, guesses whose walk was
+ * kept, and evaluations made by the walks from the guesses. */
+int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals);
+
 /* ---- utilities ---- */
 int fdf_Synchronize(FdfContext *ctx);
 /* The context's cudaStream_t, for callers that time or order work around it. */
@@ -160,8 +201,9 @@ int64_t fdf_GetLaunchCount(FdfContext *ctx);
 /* Stage timing with CUDA events on the context stream (enable resets the record).
  * Stages: 0 center->corner (on a second stream, concurrent with 2), 1 advect+locate,
  * 2 sort by cell (histogram scan, slots, per-cell PID order), 3 wait for stage 0,
- * 4 gather+interpolate, 5 deposits.  ms_total[s] sums the stage over all pipeline
- * runs since enabling; launches[s] counts those runs. */
+ * 4 gather+interpolate, 5 deposits, 6 learned guesses (learned form; its stage 1 is the
+ * first evaluation plus the walk from the guess).  ms_total[s] sums the stage over all
+ * pipeline runs since enabling; launches[s] counts the timed spans. */
 int fdf_SetProfiling(FdfContext *ctx, int enable);
 /* Running totals since fdf_SetSwarm: particles advanced (sum over steps of the live
  * particles at step start), walking-search cell evaluations actually made, and

@@ -1,0 +1,178 @@
+"""GPU: the learned start-cell locator (tensor-core MLP) and the learned form.
+
+* Initial weights equal the oracle's (oracle/mlp_oracle.py init_params), bit for bit.
+* Gradients of the tensor-core forward/backward kernels match the oracle's backward
+  with the same bfloat16 rounding points (relative L2 error per block <= 5e-3), and
+  match it far more closely than they match the unrounded FP64 gradient.
+* Inference (fused kernel, SiLU by tanh.approx) matches the oracle's bfloat16 forward to
+  0.02 (outputs are O(1)), and its cells are floor((y + 1) N / 2) of its outputs.
+* Training on walk-produced pairs is deterministic and reduces the loss.
+* The learned form gives the FP32 form's swarm, fields and deposits bit for bit, with a
+  trained and with an untrained network, and the trained network reduces the walk.
+"""
+import numpy as np
+import pytest
+
+from fdf_gb300 import workloads as W
+from fdf_gb300.context import FORM_FP32, FORM_LEARNED_FP32, LOCATOR_NPARAM, PicContext
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+OFFS = [(0, 384), (384, 512), (512, 16896), (16896, 17024), (17024, 33408), (33408, 33536), (33536, 33920),
+        (33920, 33923)]
+NAMES = ["W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4"]
+
+
+def flat(params):
+    return np.concatenate([np.concatenate([W_.ravel(), b.ravel()]) for W_, b in params]).astype(np.float32)
+
+
+def unflat(v):
+    out = []
+    for L in range(4):
+        (a, b), (c, d) = OFFS[2 * L], OFFS[2 * L + 1]
+        out.append((v[a:b].reshape(M.SIZES[L + 1], M.SIZES[L]), v[c:d]))
+    return out
+
+
+@pytest.fixture(scope="module")
+def small(require_gpu):
+    c = PicContext(0)
+    wl = W.config_bent_pipe(12, 12, 48, n=1000, cfl=2.0, materialize=False)
+    c.set_grid(wl.coor)
+    yield c, wl
+    c.close()
+
+
+def test_init_matches_oracle(small):
+    ctx, _ = small
+    ctx.locator_init(seed=3)
+    assert np.array_equal(ctx.locator_get_params(), flat(M.init_params(seed=3)))
+
+
+def test_gradients_match_oracle(small):
+    ctx, wl = small
+    dims = wl.dims
+    rng = np.random.default_rng(11)
+    params = [(W_, (0.2 * rng.standard_normal(b.shape)).astype(np.float32)) for W_, b in M.init_params(seed=4)]
+    ctx.locator_set_params(flat(params))
+    B = 512
+    xhat = rng.uniform(-1, 1, size=(B, 3)).astype(np.float32)
+    cells = np.stack([rng.integers(0, d, size=B) for d in dims], axis=1)
+    t = M.targets(cells, dims).astype(np.float32)
+    g_gpu, loss_gpu = ctx.locator_gradients(xhat, t)
+
+    y, cache = M.forward(params, xhat.astype(np.float64), use_bf16=True)
+    loss, gy = M.loss_and_grad_y(y, t.astype(np.float64), dims)
+    ref = flat([(dW, db) for dW, db in M.backward(params, cache, gy, use_bf16=True)])
+    p64 = [(W_.astype(np.float64), b.astype(np.float64)) for W_, b in params]
+    y6, c6 = M.forward(p64, xhat.astype(np.float64), use_bf16=False)
+    _, gy6 = M.loss_and_grad_y(y6, t.astype(np.float64), dims)
+    exact = flat([(dW, db) for dW, db in M.backward(p64, c6, gy6, use_bf16=False)])
+
+    assert abs(loss_gpu - loss) <= 1e-3 * loss
+    for name, (a, b) in zip(NAMES, OFFS):
+        e_ref = np.linalg.norm(g_gpu[a:b] - ref[a:b]) / np.linalg.norm(ref[a:b])
+        e_exact = np.linalg.norm(g_gpu[a:b] - exact[a:b]) / np.linalg.norm(exact[a:b])
+        print(f"[grad {name}] vs bf16 oracle {e_ref:.2e}  vs FP64 {e_exact:.2e}")
+        assert e_ref <= 5e-3, (name, e_ref)
+        if name in ("W1", "W2", "W3", "b1", "b2", "b3"):
+            assert e_ref <= 0.3 * e_exact, (name, e_ref, e_exact)
+
+
+def test_predict_matches_oracle_forward(small):
+    ctx, wl = small
+    rng = np.random.default_rng(5)
+    params = [(W_, (0.2 * rng.standard_normal(b.shape)).astype(np.float32)) for W_, b in M.init_params(seed=6)]
+    ctx.locator_set_params(flat(params))
+    pos, _ = W.volumetric_particles(wl.coor, 5000, seed=9)
+    cells, y = ctx.locator_predict(pos)
+    c, ih = ctx.locator_normalization()
+    xhat = (pos.astype(np.float32) - c) * ih
+    y_ref, _ = M.forward(params, xhat.astype(np.float64), use_bf16=True)
+    err = np.abs(y.astype(np.float64) - y_ref)
+    print(f"[predict] max |dy| {err.max():.3e} mean {err.mean():.3e} (|y| max {np.abs(y_ref).max():.2f})")
+    assert err.max() <= 0.02 and err.mean() <= 2e-3
+    N = np.array(wl.dims, dtype=np.float32)
+    want = np.clip(np.floor((y + np.float32(1.0)) * np.float32(0.5) * N), 0, N - 1).astype(np.int64)
+    assert np.array_equal(cells, want)
+
+
+def test_training_deterministic_and_learns(small):
+    ctx, wl = small
+    ctx.locator_init(seed=1)
+    h1 = ctx.locator_train(200_000, seed=2, steps=600, batch=4096, lr=3e-3)
+    p1 = ctx.locator_get_params()
+    ctx.locator_init(seed=1)
+    h2 = ctx.locator_train(200_000, seed=2, steps=600, batch=4096, lr=3e-3)
+    assert np.array_equal(p1, ctx.locator_get_params()) and np.array_equal(h1, h2)
+    print(f"[train] loss {h1[:20].mean():.3f} -> {h1[-50:].mean():.4f}")
+    assert np.all(np.isfinite(h1)) and h1[-50:].mean() < 0.1 * h1[:20].mean()
+    pos, cell = W.volumetric_particles(wl.coor, 20000, seed=13)
+    pred, _ = ctx.locator_predict(pos)
+    cheb = np.abs(pred - cell).max(axis=1)
+    print(f"[train] held-out: exact {np.mean(cheb == 0):.3f}, within 1 cell {np.mean(cheb <= 1):.3f}")
+    assert np.mean(cheb <= 1) >= 0.6
+
+
+def _run(form, wl, steps, train=None):
+    ctx = PicContext(0)
+    try:
+        ctx.load_workload(wl, form=form)
+        if form == FORM_LEARNED_FP32:   # the locator belongs to the grid set by load_workload
+            if train is None:
+                ctx.locator_init(seed=0)
+            else:
+                ctx.locator_train(**train)
+        ctx.initial_setup()
+        for _ in range(steps):
+            ctx.step(info=False)
+        ctx.synchronize()
+        s = ctx.get_swarm()
+        faces = ctx.get_faces()
+        sc = ctx.get_scattered()
+        psteps, evals, _ = ctx.counters()
+        stats = ctx.locator_stats() if form == FORM_LEARNED_FP32 else None
+        return s, faces, sc, psteps, evals, stats
+    finally:
+        ctx.close()
+
+
+@pytest.fixture(scope="module")
+def pipe_runs(require_gpu):
+    wl = W.config_bent_pipe(24, 24, 192, n=300_000, cfl=4.0, materialize=False)
+    train = dict(n_samples=1_000_000, seed=7, steps=3000, batch=8192, lr=2e-3)
+    return wl, {
+        "fp32": _run(FORM_FP32, wl, 4),
+        "learned": _run(FORM_LEARNED_FP32, wl, 4, train),
+        "untrained": _run(FORM_LEARNED_FP32, wl, 4, None),
+    }
+
+
+def _same(a, b):
+    sa, fa, ca = a[:3]
+    sb, fb, cb = b[:3]
+    for f in ("position", "velocity", "weight", "P", "cell", "pid", "status"):
+        assert np.array_equal(getattr(sa, f), getattr(sb, f)), f
+    for x, y in zip(fa + ca, fb + cb):
+        assert np.array_equal(x, y)
+
+
+def test_learned_form_identical_to_fp32_form(pipe_runs):
+    _, r = pipe_runs
+    _same(r["fp32"], r["learned"])
+    _same(r["fp32"], r["untrained"])
+
+
+def test_trained_locator_shortens_walk(pipe_runs):
+    _, r = pipe_runs
+    ps = r["fp32"][3]
+    e_fp32, e_learn, e_untr = r["fp32"][4], r["learned"][4], r["untrained"][4]
+    asked, taken, gev = r["learned"][5]
+    asked_u, taken_u, gev_u = r["untrained"][5]
+    print(f"[gain] walk evaluations per particle-step: FP32 form {e_fp32 / ps:.3f}, learned {e_learn / ps:.3f}, "
+          f"untrained {e_untr / ps:.3f}; guesses kept {taken}/{asked} (untrained {taken_u}/{asked_u}), "
+          f"evaluations per kept-or-tried guess {gev / max(asked, 1):.2f}")
+    assert taken > 0.5 * asked
+    assert e_learn < e_untr
