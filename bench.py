@@ -49,6 +49,8 @@ def workload(name: str):
         return W.config_bent_pipe(materialize=False)
     if name == "bent_pipe_8m":
         return W.config_bent_pipe(n=8_000_000, materialize=False)
+    if name == "bent_pipe_small":      # profiling case: 885K cells, 2M particles (> L2)
+        return W.config_bent_pipe(48, 48, 384, n=2_000_000, materialize=False)
     if name == "curved_pipe":
         return W.config_curved_pipe(materialize=False)
     if name == "sinusoidal_medium":
@@ -528,7 +530,7 @@ def main():
     ap.add_argument("--forms", default="learned_fp32,fp32,plain_fp64",
                     help="comma list; the first is the headline value, the others are reported beside it")
     ap.add_argument("--train-samples", type=int, default=4_000_000)
-    ap.add_argument("--train-steps", type=int, default=4000)
+    ap.add_argument("--train-steps", type=int, default=16000)
     ap.add_argument("--train-batch", type=int, default=8192)
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--identity-steps", type=int, default=3,

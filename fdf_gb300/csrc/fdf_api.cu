@@ -443,14 +443,16 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     // start cell and walk from there (k_locate32_guess)
     LocatorState &L = ctx->loc;
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
-                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, s);
+                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, L.pflag, s);
+    exclusive_scan_u32(L.pflag, (long long)ctx->cap + 1, L.scan_sums, s);
+    launch_compact_pending(L.pflag, ctx->cap, L.pending, ctx->cnt, s);
     eg0 = prof ? record_event(ctx, s) : 0;
     mlp_guess(L.frag, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0, ctx->cap, g, L.guess,
               ctx->num_sms, s);
     eg1 = prof ? record_event(ctx, s) : 0;
     launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
                           ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
-    ctx->launches += 2;
+    ctx->launches += 2 + 3 + 1;   // guess, walk from the guess, flag scan, compaction
   } else if (f32) {
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
                     ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, nullptr, s);

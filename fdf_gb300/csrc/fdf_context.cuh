@@ -20,8 +20,10 @@ struct LocatorState {
   MlpNorm norm{};
   long long adam_t = 0;
   // per-particle buffers of the learned form's locate
-  unsigned int *pending = nullptr;
-  int *guess = nullptr;
+  unsigned int *pending = nullptr;    // [cap]: slots that left their previous cell, in slot order
+  unsigned int *pflag = nullptr;      // [cap+1]: their flags, then the flags' exclusive scan
+  unsigned int *scan_sums = nullptr;
+  int *guess = nullptr;               // [cap]: learned start cell of pending[t]
   int pending_cap = 0;
   // training scratch for batches up to `batch_cap`
   int batch_cap = 0;

@@ -1,0 +1,76 @@
+// fdf_counters.cuh -- per-step counters of the locate kernels, reduced per block before
+// they reach the DevCounters words in global memory: every warp of every block adding to
+// the same few addresses serialises in one L2 slice, so each block issues at most one
+// atomic per counter.
+#pragma once
+#include "fdf_internal.cuh"
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct LocCounts {
+  unsigned long long lost = 0, oob = 0, evals = 0, done = 0, lost_total = 0, fb = 0;
+  unsigned int err = 0;
+};
+
+// Histogram of the kept keys: one atomic per distinct key in the warp (all 32 lanes call it;
+// hkey = all ones for none).
+__device__ __forceinline__ void warp_histogram(unsigned int hkey, unsigned int *__restrict__ count) {
+  const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
+  const int lane = threadIdx.x & 31;
+  if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
+}
+
+// Adds the block's counters to cnt.  Every thread of the block calls it (blockDim.x a
+// multiple of 32, at most 1024).
+__device__ __forceinline__ void block_flush_counts(const LocCounts &m, DevCounters *cnt) {
+  __shared__ unsigned long long red[32][6];
+  __shared__ unsigned int rerr[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();   // a previous call's readers are done with the shared words
+  unsigned long long v[6] = {m.lost, m.oob, m.evals, m.done, m.lost_total, m.fb};
+#pragma unroll
+  for (int q = 0; q < 6; ++q) v[q] = warp_sum_u64(v[q]);
+  const unsigned int e = __reduce_or_sync(0xffffffffu, m.err);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) red[w][q] = v[q];
+    rerr[w] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    const int q = threadIdx.x;
+    if (q < 6) {
+      unsigned long long t = 0;
+      for (int k = 0; k < nw; ++k) t += red[k][q];
+      if (t) {
+        unsigned long long *dst[6] = {&cnt->removed_lost, &cnt->removed_oob, &cnt->evals, &cnt->evals_total,
+                                      &cnt->lost_total, &cnt->fallbacks};
+        atomicAdd(dst[q], t);
+        if (q == 5) atomicAdd(&cnt->fallbacks_total, t);
+      }
+    } else {
+      unsigned int t = 0;
+      for (int k = 0; k < nw; ++k) t |= rerr[k];
+      if (t) atomicOr(&cnt->err, t);
+    }
+  }
+}
+
+// Sum of a per-thread count over the block, added to *dst by one thread.  Every thread
+// of the block calls it.
+__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *dst) {
+  __shared__ unsigned long long part[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();   // a previous call's reader is done with the shared words
+  v = warp_sum_u64(v);
+  if (lane == 0) part[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int k = 0; k < nw; ++k) t += part[k];
+    if (t) atomicAdd(dst, t);
+  }
+}

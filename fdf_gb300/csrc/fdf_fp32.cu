@@ -30,17 +30,13 @@
 // fcr (3 x f32), n32 (3 x f32).
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
+#include "fdf_counters.cuh"
 
 namespace {
 
 using fdfx::add;
 using fdfx::mul;
 using fdfx::sub;
-
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // Overlap margin of cell c (FP64): an upper bound on |d_f(p) - d'(p)| over the six faces f
 // of the cell, every plane P' of the same grid surface on the 3x3 patches around face f
@@ -312,37 +308,11 @@ __device__ __forceinline__ unsigned int settle_key32(bool lost, int cell, float2
   return key;
 }
 
-struct LocCounts {
-  unsigned long long lost = 0, oob = 0, evals = 0, done = 0, lost_total = 0, fb = 0;
-  unsigned int err = 0;
-};
-
-// Warp-aggregated histogram of the kept keys and the counters (all 32 lanes call it).
-__device__ __forceinline__ void flush_counts(unsigned int hkey, unsigned int *__restrict__ count, LocCounts &m,
-                                             DevCounters *cnt) {
-  const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
-  const int lane = threadIdx.x & 31;
-  if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
-  const unsigned long long lost = warp_sum_u64(m.lost), oob = warp_sum_u64(m.oob), evals = warp_sum_u64(m.evals),
-                           done = warp_sum_u64(m.done), lt = warp_sum_u64(m.lost_total), fb = warp_sum_u64(m.fb);
-  const unsigned int err = __reduce_or_sync(0xffffffffu, m.err);
-  if (lane == 0) {
-    if (lost) atomicAdd(&cnt->removed_lost, lost);
-    if (oob) atomicAdd(&cnt->removed_oob, oob);
-    if (evals) atomicAdd(&cnt->evals, evals);
-    if (done) atomicAdd(&cnt->evals_total, done);
-    if (lt) atomicAdd(&cnt->lost_total, lt);
-    if (fb) { atomicAdd(&cnt->fallbacks, fb); atomicAdd(&cnt->fallbacks_total, fb); }
-    if (err) atomicOr(&cnt->err, err);
-  }
-  m = LocCounts();
-}
-
 // Advect + locate, one thread per particle.
 //   FIRST == false: the reference walk from the previous cell (or cell (0,0,0)).
 //   FIRST == true:  the reference's first evaluation only, in the previous cell; a particle
-//                   that it does not conclude is appended to `pending` and finished by
-//                   k_locate32_guess (its key and histogram entry are written there).
+//                   that it does not conclude is flagged in `pending` (n_cap + 1 flags) and
+//                   finished by k_locate32_guess (its key and histogram entry are written there).
 template <bool FIRST>
 __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
@@ -350,7 +320,7 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
                                                   const float *__restrict__ fbox, int drop_removed,
                                                   DevCounters *cnt, unsigned int *__restrict__ keys,
                                                   unsigned int *__restrict__ count, unsigned int sentinel,
-                                                  unsigned int *__restrict__ pending) {
+                                                  unsigned int *__restrict__ pending, int n_cap) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
@@ -401,17 +371,24 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
       else if (!drop_removed) hkey = sentinel;
     }
   }
-  if (FIRST) {
-    const unsigned int ask = __ballot_sync(0xffffffffu, wait);
-    if (ask) {
-      const int lane = threadIdx.x & 31;
-      unsigned long long base = 0;
-      if (lane == __ffs(ask) - 1) base = atomicAdd(&cnt->pending, (unsigned long long)__popc(ask));
-      base = __shfl_sync(0xffffffffu, base, __ffs(ask) - 1);
-      if (wait) pending[base + __popc(ask & ((1u << lane) - 1u))] = (unsigned int)s;
-    }
+  if (FIRST && s < n_cap) {   // flags of the pending list (compacted by an exclusive scan)
+    pending[s] = wait ? 1u : 0u;
+    if (s == n_cap - 1) pending[n_cap] = 0u;
   }
-  flush_counts(hkey, count, m, cnt);
+  warp_histogram(hkey, count);
+  block_flush_counts(m, cnt);
+}
+
+// pending[0 .. n_cap] holds the exclusive scan of the flags: slot s is pending when
+// pending[s + 1] > pending[s]; list[pending[s]] = s keeps the slot (cell) order.
+__global__ void k_compact_pending(const unsigned int *__restrict__ scan, int n_cap, unsigned int *__restrict__ list,
+                                  DevCounters *cnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) cnt->pending = scan[n_cap];
+  if (s < n_cap) {
+    const unsigned int a = scan[s];
+    if (scan[s + 1] != a) list[a] = (unsigned int)s;
+  }
 }
 
 // The particles that left their previous cell (the list from k_locate32<true>, whose
@@ -434,9 +411,10 @@ __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, 
   const long long stride = (long long)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   unsigned long long acc = 0, gev = 0;
+  LocCounts mt;   // this thread's counters over all its list entries
   for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < npend; base += stride) {
     const long long t = base + lane;
-    LocCounts m;
+    LocCounts &m = mt;
     unsigned int hkey = 0xffffffffu;
     if (t < npend) {
       const int s = (int)pending[t];
@@ -491,14 +469,11 @@ __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, 
       if (key < sentinel) hkey = key;
       else if (!drop_removed) hkey = sentinel;
     }
-    flush_counts(hkey, count, m, cnt);
+    warp_histogram(hkey, count);
   }
-  acc = warp_sum_u64(acc);
-  gev = warp_sum_u64(gev);
-  if (lane == 0) {
-    if (acc) atomicAdd(&cnt->guess_taken_total, acc);
-    if (gev) atomicAdd(&cnt->guess_evals_total, gev);
-  }
+  block_flush_counts(mt, cnt);
+  block_add_u64(acc, &cnt->guess_taken_total);
+  block_add_u64(gev, &cnt->guess_evals_total);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->guess_asked_total, (unsigned long long)npend);
 }
 
@@ -520,8 +495,7 @@ __global__ void k_center_to_corner32(const float *__restrict__ ucat, GridDims g,
             long long c = ((long long)ck * g.JM + cj) * g.IM + ci;
             need = __ldg(cell_start + c + 1) > __ldg(cell_start + c);
           }
-    unsigned int bal = __ballot_sync(0xffffffffu, need);
-    if (nodes_done && (threadIdx.x & 31) == 0 && bal) atomicAdd(nodes_done, (unsigned long long)__popc(bal));
+    if (nodes_done) block_add_u64(need ? 1ull : 0ull, nodes_done);
     if (!need) return;
   }
   if (!work) return;
@@ -731,11 +705,17 @@ void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *tabl
                      cudaStream_t s) {
   if (pending)
     k_locate32<true><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox,
-                                                            fbox, drop_removed, cnt, keys, count, sentinel, pending);
+                                                            fbox, drop_removed, cnt, keys, count, sentinel, pending,
+                                                            n_cap);
   else
     k_locate32<false><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed,
                                                              bbox, fbox, drop_removed, cnt, keys, count, sentinel,
-                                                             nullptr);
+                                                             nullptr, n_cap);
+}
+
+void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
+                            cudaStream_t s) {
+  k_compact_pending<<<blocks_for(n_cap, 256), 256, 0, s>>>(scan, n_cap, list, cnt);
 }
 
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,

@@ -6,6 +6,7 @@
 // reference (compiled without FMA) rounds it.
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
+#include "fdf_counters.cuh"
 #include <cfloat>
 
 namespace {
@@ -113,8 +114,7 @@ __global__ void k_center_to_corner(const double *__restrict__ ucat, GridDims g, 
             need = __ldg(cell_start + c + 1) > __ldg(cell_start + c);
           }
     }
-    unsigned int bal = __ballot_sync(0xffffffffu, need);
-    if (nodes_done && (threadIdx.x & 31) == 0 && bal) atomicAdd(nodes_done, (unsigned long long)__popc(bal));
+    if (nodes_done) block_add_u64(need ? 1ull : 0ull, nodes_done);
     if (!need) return;
   }
   if (!work) return;

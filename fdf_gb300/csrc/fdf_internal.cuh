@@ -154,11 +154,14 @@ void launch_build_table32(const double *planes, const double *coor, GridDims g, 
 // fbox: 12 floats, (x, y, z, -) lower and (x, y, z, -) upper bounds strictly inside the
 // bounding box by more than any lo part of a position inside it, then 4 unused.
 // pending != nullptr: the learned form's first pass (one evaluation in the previous cell;
-// particles that leave it are appended to pending and counted in cnt->pending).
+// pending[s] = 1 for the particles that leave it, 0 otherwise, for s <= n_cap).
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                      unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
                      cudaStream_t s);
+// The learned form's pending list from the scanned flags (sets cnt->pending).
+void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
+                            cudaStream_t s);
 // The learned form's second pass over pending[0 .. cnt->pending), guess[t] = start cell.
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
                            const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,

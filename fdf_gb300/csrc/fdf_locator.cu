@@ -167,7 +167,8 @@ void forward_backward(FdfContext *ctx, const TrainScratch &S, int B, float *loss
 void locator_free(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
   cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf);
-  cfree(L.frag); cfree(L.bias); cfree(L.pending); cfree(L.guess); cfree(L.scratch);
+  cfree(L.frag); cfree(L.bias); cfree(L.pending); cfree(L.guess); cfree(L.scratch); cfree(L.pflag);
+  cfree(L.scan_sums);
   L.pending_cap = 0;
   L.batch_cap = 0;
   L.has_params = false;
@@ -176,10 +177,12 @@ void locator_free(FdfContext *ctx) {
 int locator_reserve(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
   if (L.pending_cap >= ctx->cap && L.pending) return FDF_SUCCESS;
-  cfree(L.pending); cfree(L.guess);
+  cfree(L.pending); cfree(L.guess); cfree(L.pflag); cfree(L.scan_sums);
   L.pending_cap = 0;
   CU(cudaMalloc((void **)&L.pending, 4ull * ctx->cap));
   CU(cudaMalloc((void **)&L.guess, 4ull * ctx->cap));
+  CU(cudaMalloc((void **)&L.pflag, 4ull * (ctx->cap + 1)));
+  CU(cudaMalloc((void **)&L.scan_sums, 4ull * scan_scratch_words(ctx->cap + 1)));
   L.pending_cap = ctx->cap;
   return FDF_SUCCESS;
 }

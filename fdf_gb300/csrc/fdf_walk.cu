@@ -26,17 +26,13 @@
 // the reference's (MAX_TRAVERSAL).
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
+#include "fdf_counters.cuh"
 
 namespace {
 
 using fdfx::add;
 using fdfx::sub;
 using fdfx::mul;
-
-__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
 
 __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
                                                 double dt, int advect, int reset_first, const double *__restrict__ bbox,
@@ -137,26 +133,11 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
     if (key < sentinel) hkey = key;
     else if (!drop_removed) hkey = sentinel;   // the initial setup keeps LOST particles, at the end
   }
-  {
-    // histogram of the kept keys, one atomic per distinct key in the warp
-    const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
-    const int lane = threadIdx.x & 31;
-    if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
-  }
-  my_lost = warp_sum_u64(my_lost);
-  my_oob = warp_sum_u64(my_oob);
-  my_evals = warp_sum_u64(my_evals);
-  my_done = warp_sum_u64(my_done);
-  my_lost_total = warp_sum_u64(my_lost_total);
-  my_err = __reduce_or_sync(0xffffffffu, my_err);
-  if ((threadIdx.x & 31) == 0) {
-    if (my_lost) atomicAdd(&cnt->removed_lost, my_lost);
-    if (my_oob) atomicAdd(&cnt->removed_oob, my_oob);
-    if (my_evals) atomicAdd(&cnt->evals, my_evals);
-    if (my_done) atomicAdd(&cnt->evals_total, my_done);
-    if (my_lost_total) atomicAdd(&cnt->lost_total, my_lost_total);
-    if (my_err) atomicOr(&cnt->err, my_err);
-  }
+  warp_histogram(hkey, count);
+  LocCounts m;
+  m.lost = my_lost; m.oob = my_oob; m.evals = my_evals; m.done = my_done; m.lost_total = my_lost_total;
+  m.err = my_err;
+  block_flush_counts(m, cnt);
 }
 
 }  // namespace
