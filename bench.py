@@ -240,10 +240,17 @@ MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, on
 _TRAINED = {}   # workload name -> (trained parameters, training report)
 
 
+def momentum_on(wl) -> bool:
+    """The curved-pipe configuration deposits particle momentum as well as volume."""
+    return wl.meta.get("family") == "curved_pipe"
+
+
 def prepare(ctx, wl, form, args):
     """Loads the workload in a form; the learned form gets its locator (trained once per
     workload on the device, then reinstalled)."""
     ctx.load_workload(wl, form=FORMS[form])
+    if momentum_on(wl):
+        ctx.set_momentum_deposit(True)
     if form != "learned_fp32":
         return
     if wl.name not in _TRAINED:
@@ -262,8 +269,9 @@ def prepare(ctx, wl, form, args):
 
 
 def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_step: float, Nc: int, Nn: int,
-                      Nf: int) -> dict:
-    """Algorithmic bytes per launch of each stage (the accounting of the design doc 3.3)."""
+                      Nf: int, momentum: bool = False) -> dict:
+    """Algorithmic bytes per launch of each stage (the accounting of the design doc 3.3); the
+    momentum deposit adds the particles' velocities and three components per face."""
     if form in ("fp32", "learned_fp32"):
         return {
             "center_to_corner": 24 * nodes_per_step,
@@ -271,7 +279,7 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
             "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
             "wait_corner": 0,
             "gather_interpolate": 121 * n_avg + 12 * Nn,
-            "deposit": 4 * (Nc + 1) + 16 * n_avg + 8 * Nn + 4 * Nf,
+            "deposit": 4 * (Nc + 1) + 16 * n_avg + 8 * Nn + 4 * Nf + (12 * n_avg + 12 * Nf if momentum else 0),
         }
     return {
         "center_to_corner": 48 * nodes_per_step,
@@ -279,7 +287,7 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
         "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
         "wait_corner": 0,
         "gather_interpolate": GATHER_PER_PARTICLE * n_avg + 24 * Nn,
-        "deposit": 4 * (Nc + 1) + 32 * n_avg + 16 * Nn + 8 * Nf,
+        "deposit": 4 * (Nc + 1) + 32 * n_avg + 16 * Nn + 8 * Nf + (24 * n_avg + 24 * Nf if momentum else 0),
     }
 
 
@@ -320,7 +328,7 @@ def time_form(ctx, wl, form, args, dist, local, with_clocks):
     psteps, evals = ps1 - ps0, e1 - e0
     K = max(args.steps, 1)
     n_avg = psteps / K
-    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf)
+    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf, momentum_on(wl))
     runs = max(stages["sort_by_cell"][1], 1)     # one span per pipeline run
     per = {k: (v[0] / runs) for k, v in stages.items() if v[1] > 0}
     learned = None
@@ -461,6 +469,10 @@ def run_gpu(args, rank, ws, local, dist):
         avg = pinned_like(np.zeros((KM + 1, JM + 1, IM + 1)))
         fi = pinned_like(np.zeros((KM, JM, IM + 1))); fj = pinned_like(np.zeros((KM, JM + 1, IM)))
         fk = pinned_like(np.zeros((KM + 1, JM, IM)))
+        mom = None
+        if momentum_on(wl):
+            mom = (pinned_like(np.zeros((KM, JM, IM + 1, 3))), pinned_like(np.zeros((KM, JM + 1, IM, 3))),
+                   pinned_like(np.zeros((KM + 1, JM, IM, 3))))
         from fdf_gb300.context import _ptr
         lib, h = ctx.lib, ctx.h
         import ctypes
@@ -479,11 +491,14 @@ def run_gpu(args, rank, ws, local, dist):
                                         _ptr(bufs.status)))
             ctx._check(lib.fdf_GetScatteredFields(h, _ptr(count), _ptr(avg)))
             ctx._check(lib.fdf_GetFaceDeposits(h, _ptr(fi), _ptr(fj), _ptr(fk)))
+            if mom is not None:
+                ctx._check(lib.fdf_GetFaceMomentum(h, _ptr(mom[0]), _ptr(mom[1]), _ptr(mom[2])))
             ps += n_cur
             n_cur = got.value
         el = reduce_max(dist, time.perf_counter() - t0)
         e2e = {"value": ps * ws / el, "unit": UNIT, "h2d_bytes_per_step": int(120 * n0),
-               "d2h_bytes_per_step": int(120 * n0 + 16 * Nn + 8 * Nf), "steps": k_e2e,
+               "d2h_bytes_per_step": int(120 * n0 + 16 * Nn + 8 * Nf + (24 * Nf if mom is not None else 0)),
+               "steps": k_e2e,
                "path": "fdf_SetSwarm + fdf_AdvanceStep + fdf_GetSwarm/GetScatteredFields/GetFaceDeposits, "
                        "pinned host DMSwarm-layout arrays"}
 
@@ -511,7 +526,8 @@ def run_gpu(args, rank, ws, local, dist):
                                             "generating cell of each particle (harness choice)"),
                            "l2": "inputs larger than L2 (plane table %.2f GB, swarm %.0f MB)"
                                  % (38 * 8 * Nc / 1e9, 2 * 93 * wl.n / 1e6),
-                           "walk_evals_per_particle_step": evals / max(psteps, 1)},
+                           "walk_evals_per_particle_step": evals / max(psteps, 1),
+                           "deposits": "face volume" + (" and momentum" if momentum_on(wl) else "")},
                 "roofline": roofline, "forms": form_lines, "fp32_accuracy_vs_fp64_oracle": accuracy,
                 "learned_vs_fp32_form": identity,
                 "cpu_baseline": cpu, "e2e": e2e,

@@ -39,6 +39,8 @@ _SIGS = {
     "fdf_GetScatteredFields": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_GetCornerField": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_GetFaceDeposits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_SetMomentumDeposit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fdf_GetFaceMomentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_PerformInitialSetup": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FdfStepInfo)]),
     "fdf_AdvanceStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FdfStepInfo)]),
     "fdf_AdvanceSteps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

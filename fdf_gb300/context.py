@@ -207,6 +207,15 @@ class PicContext:
         self._check(self.lib.fdf_GetFaceDeposits(self.h, _ptr(fi), _ptr(fj), _ptr(fk)))
         return fi, fj, fk
 
+    def set_momentum_deposit(self, on: bool = True):
+        self._check(self.lib.fdf_SetMomentumDeposit(self.h, 1 if on else 0))
+
+    def get_face_momentum(self):
+        IM, JM, KM = self.dims
+        mi = np.zeros((KM, JM, IM + 1, 3)); mj = np.zeros((KM, JM + 1, IM, 3)); mk = np.zeros((KM + 1, JM, IM, 3))
+        self._check(self.lib.fdf_GetFaceMomentum(self.h, _ptr(mi), _ptr(mj), _ptr(mk)))
+        return mi, mj, mk
+
     # -- the hot path
     def initial_setup(self) -> FdfStepInfo:
         info = FdfStepInfo()

@@ -75,7 +75,7 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner); cfree(ctx->bbox);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk);
   cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
-  cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox);
+  cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox); cfree(ctx->mom); cfree(ctx->mom32);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
   cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
   cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
@@ -103,7 +103,8 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk); cfree(ctx->cell_start);
   cfree(ctx->cursor); cfree(ctx->scan_sums);
   cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
-  cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32);
+  cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->mom); cfree(ctx->mom32);
+  ctx->momentum = false;
   GridDims g{};
   g.IM = (int)IM; g.JM = (int)JM; g.KM = (int)KM; g.Nc = Nc; g.Nn = Nn;
   g.fIM.init((unsigned)IM); g.fJM.init((unsigned)JM); g.fMX.init((unsigned)(IM + 1)); g.fMY.init((unsigned)(JM + 1));
@@ -483,11 +484,17 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   else
     launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s);
   size_t e4 = prof ? record_event(ctx, s) : 0;
-  if (f32)
+  const long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM;
+  if (f32) {
+    float *m = ctx->momentum ? ctx->mom32 : nullptr;
     launch_deposit32(dst, g, ctx->cell_start, ctx->volume, ctx->count32, ctx->avg32, ctx->fi32, ctx->fj32, ctx->fk32,
-                     s);
-  else
-    launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, s);
+                     m, m ? m + 3 * nfi : nullptr, m ? m + 3 * (nfi + nfj) : nullptr, s);
+  } else {
+    double *m = ctx->momentum ? ctx->mom : nullptr;
+    launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, m,
+                   m ? m + 3 * nfi : nullptr, m ? m + 3 * (nfi + nfj) : nullptr, s);
+  }
+  ctx->out_momentum = ctx->momentum;
   ctx->out_form = ctx->swarm_form;
   size_t e5 = prof ? record_event(ctx, s) : 0;
   if (prof && learned) {
@@ -602,6 +609,50 @@ int fdf_SetProfiling(FdfContext *ctx, int enable) {
   ctx->profiling = enable != 0;
   ctx->ev_used = 0;
   ctx->ev_spans.clear();
+  return FDF_SUCCESS;
+}
+
+int fdf_SetMomentumDeposit(FdfContext *ctx, int enable) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_SetMomentumDeposit: call fdf_SetGrid first");
+  CU(cudaSetDevice(ctx->device));
+  if (enable && !ctx->mom) {
+    const GridDims &g = ctx->g;
+    const long long nf = (g.IM + 1LL) * g.JM * g.KM + g.IM * (g.JM + 1LL) * g.KM + (long long)g.IM * g.JM * (g.KM + 1LL);
+    CU(cudaStreamSynchronize(ctx->stream));
+    CU(cudaMalloc((void **)&ctx->mom, 24ull * nf));
+    CU(cudaMalloc((void **)&ctx->mom32, 12ull * nf));
+    CU(cudaMemset(ctx->mom, 0, 24ull * nf));
+    CU(cudaMemset(ctx->mom32, 0, 12ull * nf));
+  }
+  ctx->momentum = enable != 0;
+  return FDF_SUCCESS;
+}
+
+int fdf_GetFaceMomentum(FdfContext *ctx, double *mi, double *mj, double *mk) {
+  if (!ctx || !mi || !mj || !mk) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetFaceMomentum: null argument");
+  if (!ctx->mom || !ctx->out_momentum)
+    return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_GetFaceMomentum: no momentum deposit (fdf_SetMomentumDeposit)");
+  const GridDims &g = ctx->g;
+  const long long nfs[3] = {(g.IM + 1LL) * g.JM * g.KM, g.IM * (g.JM + 1LL) * g.KM, (long long)g.IM * g.JM * (g.KM + 1LL)};
+  const long long nf = nfs[0] + nfs[1] + nfs[2];
+  CU(cudaSetDevice(ctx->device));
+  if (form_is32(ctx->out_form)) {
+    launch_f32_to_f64(ctx->mom32, ctx->mom, 3 * nf, ctx->stream);
+    CHECK_LAUNCH();
+    ctx->launches += 1;
+  }
+  std::vector<double> soa(3 * (size_t)nf);
+  CU(cudaMemcpyAsync(soa.data(), ctx->mom, 24ull * nf, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  double *out[3] = {mi, mj, mk};
+  size_t off = 0;
+  for (int fam = 0; fam < 3; ++fam) {
+    const long long n = nfs[fam];
+    for (long long q = 0; q < n; ++q)
+      for (int c = 0; c < 3; ++c) out[fam][3 * q + c] = soa[off + (size_t)c * n + q];
+    off += 3 * (size_t)n;
+  }
   return FDF_SUCCESS;
 }
 

@@ -43,6 +43,10 @@ struct FdfContext {
   float *table32 = nullptr, *ucat32 = nullptr, *corner32 = nullptr, *fbox = nullptr;
   float *count32 = nullptr, *avg32 = nullptr, *fi32 = nullptr, *fj32 = nullptr, *fk32 = nullptr;
   double bbox_h[6] = {0, 0, 0, 0, 0, 0};
+  // momentum face deposit (fdf_SetMomentumDeposit): SoA [3][faces] per face family
+  bool momentum = false;
+  double *mom = nullptr;   // mi | mj | mk, 3 (nfi + nfj + nfk) doubles
+  float *mom32 = nullptr;
   double dt = 0.0, volume = 1.0;
   int cap = 0;
   SwarmBuf buf[2];
@@ -59,6 +63,7 @@ struct FdfContext {
   bool swarm_set = false;
   int swarm_form = FDF_FORM_PLAIN_FP64;   // form the swarm's device arrays are held in
   int out_form = FDF_FORM_PLAIN_FP64;     // form of the last deposits
+  bool out_momentum = false;              // the last deposits include the momentum
   long long launches = 0;
   // stage timing: events recorded on the context stream between pipeline stages
   bool profiling = false;

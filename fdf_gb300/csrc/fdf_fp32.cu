@@ -579,10 +579,12 @@ struct KSum {
   __device__ __forceinline__ float value() const { return s + c; }
 };
 
+template <bool MOM>
 __global__ void __launch_bounds__(256) k_deposit32(SwarmBuf b, GridDims g, const unsigned int *__restrict__ cs,
                                                    float third, float *__restrict__ count, float *__restrict__ avg,
                                                    float *__restrict__ fi, float *__restrict__ fj,
-                                                   float *__restrict__ fk) {
+                                                   float *__restrict__ fk, float *__restrict__ mi,
+                                                   float *__restrict__ mj, float *__restrict__ mk) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nn) return;
   const int IM = g.IM, JM = g.JM, KM = g.KM;
@@ -599,39 +601,34 @@ __global__ void __launch_bounds__(256) k_deposit32(SwarmBuf b, GridDims g, const
     count[q] = (float)nc;
     avg[q] = nc > 0 ? sum.value() / (float)nc : 0.f;
   }
-  if (j < JM && k < KM) {
-    KSum acc;
-    if (i > 0) {
-      const long long cl = c - 1;
-      const int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
-      for (int s = l0; s < l1; ++s) acc.add(__ldg(b.a1f + s) * third);
+  auto face = [&](const float *__restrict__ wgt, long long lower, bool has_lower, bool has_upper, float *vol,
+                  float *mom, long long nf, long long fidx) {
+    KSum acc, m0, m1, m2;
+    if (has_lower) {
+      const int l0 = (int)__ldg(cs + lower), l1 = (int)__ldg(cs + lower + 1);
+      for (int s = l0; s < l1; ++s) {
+        const float f = __ldg(wgt + s) * third;
+        acc.add(f);
+        if (MOM) { m0.add(f * __ldg(b.uf + s)); m1.add(f * __ldg(b.vf + s)); m2.add(f * __ldg(b.wf + s)); }
+      }
     }
-    if (i < IM)
-      for (int s = s0; s < s1; ++s) acc.add((1.f - __ldg(b.a1f + s)) * third);
-    fi[((long long)k * JM + j) * (IM + 1) + i] = acc.value();
-  }
-  if (i < IM && k < KM) {
-    KSum acc;
-    if (j > 0) {
-      const long long cl = ((long long)k * JM + (j - 1)) * IM + i;
-      const int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
-      for (int s = l0; s < l1; ++s) acc.add(__ldg(b.a2f + s) * third);
-    }
-    if (j < JM)
-      for (int s = s0; s < s1; ++s) acc.add((1.f - __ldg(b.a2f + s)) * third);
-    fj[((long long)k * (JM + 1) + j) * IM + i] = acc.value();
-  }
-  if (i < IM && j < JM) {
-    KSum acc;
-    if (k > 0) {
-      const long long cl = ((long long)(k - 1) * JM + j) * IM + i;
-      const int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
-      for (int s = l0; s < l1; ++s) acc.add(__ldg(b.a3f + s) * third);
-    }
-    if (k < KM)
-      for (int s = s0; s < s1; ++s) acc.add((1.f - __ldg(b.a3f + s)) * third);
-    fk[c] = acc.value();
-  }
+    if (has_upper)
+      for (int s = s0; s < s1; ++s) {
+        const float f = (1.f - __ldg(wgt + s)) * third;
+        acc.add(f);
+        if (MOM) { m0.add(f * __ldg(b.uf + s)); m1.add(f * __ldg(b.vf + s)); m2.add(f * __ldg(b.wf + s)); }
+      }
+    vol[fidx] = acc.value();
+    if (MOM) { mom[fidx] = m0.value(); mom[nf + fidx] = m1.value(); mom[2 * nf + fidx] = m2.value(); }
+  };
+  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
+  if (j < JM && k < KM)
+    face(b.a1f, c - 1, i > 0, i < IM, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);
+  if (i < IM && k < KM)
+    face(b.a2f, ((long long)k * JM + (j - 1)) * IM + i, j > 0, j < JM, fj, mj, nfj,
+         ((long long)k * (JM + 1) + j) * IM + i);
+  if (i < IM && j < JM)
+    face(b.a3f, ((long long)(k - 1) * JM + j) * IM + i, k > 0, k < KM, fk, mk, nfk, c);
 }
 
 __global__ void k_from_aos32(const double *__restrict__ pos, const double *__restrict__ vel,
@@ -742,8 +739,13 @@ void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap,
 }
 
 void launch_deposit32(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, float *count,
-                      float *avg, float *fi, float *fj, float *fk, cudaStream_t s) {
-  k_deposit32<<<blocks_for(g.Nn, 256), 256, 0, s>>>(b, g, cell_start, (float)(volume / 3.0), count, avg, fi, fj, fk);
+                      float *avg, float *fi, float *fj, float *fk, float *mi, float *mj, float *mk, cudaStream_t s) {
+  if (mi)
+    k_deposit32<true><<<blocks_for(g.Nn, 256), 256, 0, s>>>(b, g, cell_start, (float)(volume / 3.0), count, avg, fi,
+                                                            fj, fk, mi, mj, mk);
+  else
+    k_deposit32<false><<<blocks_for(g.Nn, 256), 256, 0, s>>>(b, g, cell_start, (float)(volume / 3.0), count, avg, fi,
+                                                             fj, fk, nullptr, nullptr, nullptr);
 }
 
 void launch_swarm_from_aos32(const double *pos, const double *vel, const double *wgt, const double *P,

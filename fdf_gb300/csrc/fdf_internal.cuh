@@ -127,8 +127,10 @@ void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *plane
 void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g,
                           const double *corner, const unsigned int *perm, const unsigned int *cell_start,
                           DevCounters *cnt, cudaStream_t s);
+// mi, mj, mk (SoA [3][faces], or nullptr): the momentum deposit, V * velocity split like the volume.
 void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,
-                    double *avg, double *fi, double *fj, double *fk, cudaStream_t s);
+                    double *avg, double *fi, double *fj, double *fk, double *mi, double *mj, double *mk,
+                    cudaStream_t s);
 
 // Counting sort helpers (fdf_sort.cu).
 size_t scan_scratch_words(long long count);
@@ -173,7 +175,7 @@ void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap,
                             const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
                             cudaStream_t s);
 void launch_deposit32(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, float *count,
-                      float *avg, float *fi, float *fj, float *fk, cudaStream_t s);
+                      float *avg, float *fi, float *fj, float *fk, float *mi, float *mj, float *mk, cudaStream_t s);
 void launch_swarm_from_aos32(const double *pos, const double *vel, const double *wgt, const double *P,
                              const long long *cell3, const long long *pid, const long long *status, int n, GridDims g,
                              const SwarmBuf &b, cudaStream_t s);

@@ -86,10 +86,15 @@ __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf ds
 // corner is this node: i-face (i,j,k) between cells i-1 and i, and likewise j, k.
 // A face sums its lower cell's particles (weight a) and then its upper cell's
 // (weight 1-a), each in sorted order: a fixed order, so the sum is deterministic.
+// Face deposits of the sorted segments; MOM adds the same split of V * velocity
+// (SoA [3][faces]), each component summed in the same order.
+template <bool MOM>
 __global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const unsigned int *__restrict__ cs,
                                                  double third, double *__restrict__ count,
                                                  double *__restrict__ avg, double *__restrict__ fi,
-                                                 double *__restrict__ fj, double *__restrict__ fk) {
+                                                 double *__restrict__ fj, double *__restrict__ fk,
+                                                 double *__restrict__ mi, double *__restrict__ mj,
+                                                 double *__restrict__ mk) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= g.Nn) return;
   const int IM = g.IM, JM = g.JM, KM = g.KM;
@@ -112,39 +117,43 @@ __global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const u
     if (ncell > 0) a = fdfx::div_count(sum, ncell);
     avg[q] = a;
   }
-  if (j < JM && k < KM) {   // i-face (i,j,k), i in [0, IM]
-    double acc = 0.0;
-    if (i > 0) {
-      long long cl = c - 1;
-      int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
-      for (int s = l0; s < l1; ++s) acc = add(acc, mul(__ldg(b.a1 + s), third));
+  // one face: the lower cell's segment with weight a, then the upper cell's with 1 - a
+  auto face = [&](const double *__restrict__ wgt, long long lower, bool has_lower, bool has_upper, double *vol,
+                  double *mom, long long nf, long long fidx) {
+    double acc = 0.0, m0 = 0.0, m1 = 0.0, m2 = 0.0;
+    if (has_lower) {
+      const int l0 = (int)__ldg(cs + lower), l1 = (int)__ldg(cs + lower + 1);
+      for (int s = l0; s < l1; ++s) {
+        const double f = mul(__ldg(wgt + s), third);
+        acc = add(acc, f);
+        if (MOM) {
+          m0 = add(m0, mul(f, __ldg(b.u + s)));
+          m1 = add(m1, mul(f, __ldg(b.v + s)));
+          m2 = add(m2, mul(f, __ldg(b.w + s)));
+        }
+      }
     }
-    if (i < IM)
-      for (int s = s0; s < s1; ++s) acc = add(acc, mul(sub(1.0, __ldg(b.a1 + s)), third));
-    fi[((long long)k * JM + j) * (IM + 1) + i] = acc;
-  }
-  if (i < IM && k < KM) {   // j-face (i,j,k), j in [0, JM]
-    double acc = 0.0;
-    if (j > 0) {
-      long long cl = ((long long)k * JM + (j - 1)) * IM + i;
-      int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
-      for (int s = l0; s < l1; ++s) acc = add(acc, mul(__ldg(b.a2 + s), third));
-    }
-    if (j < JM)
-      for (int s = s0; s < s1; ++s) acc = add(acc, mul(sub(1.0, __ldg(b.a2 + s)), third));
-    fj[((long long)k * (JM + 1) + j) * IM + i] = acc;
-  }
-  if (i < IM && j < JM) {   // k-face (i,j,k), k in [0, KM]
-    double acc = 0.0;
-    if (k > 0) {
-      long long cl = ((long long)(k - 1) * JM + j) * IM + i;
-      int l0 = (int)__ldg(cs + cl), l1 = (int)__ldg(cs + cl + 1);
-      for (int s = l0; s < l1; ++s) acc = add(acc, mul(__ldg(b.a3 + s), third));
-    }
-    if (k < KM)
-      for (int s = s0; s < s1; ++s) acc = add(acc, mul(sub(1.0, __ldg(b.a3 + s)), third));
-    fk[c] = acc;
-  }
+    if (has_upper)
+      for (int s = s0; s < s1; ++s) {
+        const double f = mul(sub(1.0, __ldg(wgt + s)), third);
+        acc = add(acc, f);
+        if (MOM) {
+          m0 = add(m0, mul(f, __ldg(b.u + s)));
+          m1 = add(m1, mul(f, __ldg(b.v + s)));
+          m2 = add(m2, mul(f, __ldg(b.w + s)));
+        }
+      }
+    vol[fidx] = acc;
+    if (MOM) { mom[fidx] = m0; mom[nf + fidx] = m1; mom[2 * nf + fidx] = m2; }
+  };
+  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
+  if (j < JM && k < KM)   // i-face (i,j,k), i in [0, IM]
+    face(b.a1, c - 1, i > 0, i < IM, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);
+  if (i < IM && k < KM)   // j-face (i,j,k), j in [0, JM]
+    face(b.a2, ((long long)k * JM + (j - 1)) * IM + i, j > 0, j < JM, fj, mj, nfj,
+         ((long long)k * (JM + 1) + j) * IM + i);
+  if (i < IM && j < JM)   // k-face (i,j,k), k in [0, KM]
+    face(b.a3, ((long long)(k - 1) * JM + j) * IM + i, k > 0, k < KM, fk, mk, nfk, c);
 }
 
 __global__ void k_from_aos(const double *__restrict__ pos, const double *__restrict__ vel,
@@ -199,11 +208,16 @@ void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, G
 }
 
 void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,
-                    double *avg, double *fi, double *fj, double *fk, cudaStream_t s) {
+                    double *avg, double *fi, double *fj, double *fk, double *mi, double *mj, double *mk,
+                    cudaStream_t s) {
   int th = 256;
   long long blocks = (g.Nn + th - 1) / th;
   double third = volume / 3.0;
-  k_deposit<<<(unsigned)blocks, th, 0, s>>>(b, g, cell_start, third, count, avg, fi, fj, fk);
+  if (mi)
+    k_deposit<true><<<(unsigned)blocks, th, 0, s>>>(b, g, cell_start, third, count, avg, fi, fj, fk, mi, mj, mk);
+  else
+    k_deposit<false><<<(unsigned)blocks, th, 0, s>>>(b, g, cell_start, third, count, avg, fi, fj, fk, nullptr,
+                                                     nullptr, nullptr);
 }
 
 void launch_swarm_from_aos(const double *pos, const double *vel, const double *wgt, const double *P,

@@ -99,6 +99,7 @@ def test_fp32_cells_exact_bent_pipe(ctx):
 def test_fp32_errors_against_fp64_oracle(ctx, capsys):
     wl = W.config_sinusoidal(IM=24, JM=24, KM=96, n=40_000, cfl=0.5, steps=10)
     ctx.load_workload(wl, form=FORM_FP32)
+    ctx.set_momentum_deposit(True)
     ctx.initial_setup()
     ctx.steps(wl.steps)
     gpu = ctx.get_swarm().sorted_by_pid()
@@ -126,10 +127,19 @@ def test_fp32_errors_against_fp64_oracle(ctx, capsys):
     assert rel_u.max() <= 1e-5
     umax = float(np.sqrt((wl.ucat ** 2).sum(-1)).max())
     assert dx.max() <= 1e-6 * wl.steps * wl.dt * umax
-    f = O.deposit_faces(g, os_, volume=wl.volume)
+    f = O.deposit_faces(g, os_, volume=wl.volume, momentum=True)
     for gf, key, akey in zip((gfi, gfj, gfk), ("fi", "fj", "fk"), ("abs_i", "abs_j", "abs_k")):
         err = np.abs(gf - f[key])
         assert np.all(err <= 1e-5 * f[akey] + 1e-6), key
+    # momentum: the volume bound scaled by max |u| (err <= 1e-5 |V| umax + 1e-6 umax per face)
+    worst = 0.0
+    for gm, key, akey in zip(ctx.get_face_momentum(), ("mom_i", "mom_j", "mom_k"), ("abs_i", "abs_j", "abs_k")):
+        err = np.abs(gm - f[key]).max(axis=-1)
+        worst = max(worst, float((err / (umax * (f[akey] + 0.1))).max()))
+    with capsys.disabled():
+        print(f"[fp32 form momentum deposit] max err / (umax (|V| + 0.1)) {worst:.3e}")
+    assert worst <= 1e-5
+    ctx.set_momentum_deposit(False)
 
 
 def test_fp32_conservation_and_determinism(ctx):

@@ -89,6 +89,30 @@ def test_curved_pipe_reduced_parity(ctx):
     run_parity(ctx, wl, wl.steps, check_every=1)
 
 
+def test_momentum_deposit_parity(ctx):
+    """The curved-pipe family (Poiseuille + swirl) with the momentum face deposit: every
+    component bit-identical to the oracle's (same products, same order), and its total equal
+    to the sum of V u over the particles."""
+    wl = W.config_curved_pipe(IM=12, JM=12, KM=64, n=20_000, cfl=1.0, steps=3)
+    ctx.load_workload(wl)
+    ctx.set_momentum_deposit(True)
+    g, os_, sim = oracle_state(wl, ctx.get_swarm())
+    ctx.initial_setup()
+    sim.initial_setup()
+    for st in range(wl.steps):
+        ctx.step()
+        sim.step()
+        ref = O.deposit_faces(g, os_, volume=wl.volume, momentum=True)
+        got = ctx.get_face_momentum()
+        for gm, key in zip(got, ("mom_i", "mom_j", "mom_k")):
+            assert np.array_equal(gm.view(np.int64), ref[key].view(np.int64)), f"step {st} {key}"
+        s = ctx.get_swarm()
+        tot = sum(m.reshape(-1, 3).sum(axis=0) for m in got)
+        want = wl.volume * s.velocity.sum(axis=0)   # each particle deposits V u over 3 families x (a + 1 - a) / 3
+        assert np.allclose(tot, want, rtol=1e-9, atol=1e-9 * np.abs(s.velocity).sum())
+    ctx.set_momentum_deposit(False)
+
+
 def test_lost_beyond_max_traversal_and_out_of_bounds(ctx):
     """Corner-start walks that need more than 1000 evaluations are LOST at set-up, kept with
     velocity 0, and removed in step 1; particles pushed out of the domain are removed as
