@@ -448,8 +448,8 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     exclusive_scan_u32(L.pflag, (long long)ctx->cap + 1, L.scan_sums, s);
     launch_compact_pending(L.pflag, ctx->cap, L.pending, ctx->cnt, s);
     eg0 = prof ? record_event(ctx, s) : 0;
-    mlp_guess(L.frag, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0, ctx->cap, g, L.guess,
-              ctx->num_sms, s);
+    mlp_guess_tc(L.tc_img, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0, ctx->cap, g,
+                 L.guess, ctx->num_sms, &ctx->cnt->err, s);
     eg1 = prof ? record_event(ctx, s) : 0;
     launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
                           ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
@@ -526,6 +526,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     info->fp64_fallbacks = (int64_t)c.fallbacks;
     if (c.err & ERRBIT_DEGENERATE)
       return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
+    if (c.err & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "learned locator: tensor-core wait timed out");
   }
   return FDF_SUCCESS;
 }
@@ -561,6 +562,7 @@ int fdf_Synchronize(FdfContext *ctx) {
   unsigned int err = 0;
   CU(cudaMemcpy(&err, &ctx->cnt->err, sizeof(err), cudaMemcpyDeviceToHost));
   if (err & ERRBIT_DEGENERATE) return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
+  if (err & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "learned locator: tensor-core wait timed out");
   return FDF_SUCCESS;
 }
 

@@ -15,7 +15,7 @@ struct LocatorState {
   float *params = nullptr;            // [MLP_NPARAM] FP32 master weights
   float *grads = nullptr, *adam_m = nullptr, *adam_v = nullptr;
   __nv_bfloat16 *params_bf = nullptr; // bfloat16 copy the training GEMMs read
-  uint2 *frag = nullptr;              // inference weights in fragment order
+  unsigned char *tc_img = nullptr;    // inference weights as the tcgen05 kernel's shared-memory image
   float *bias = nullptr;
   MlpNorm norm{};
   long long adam_t = 0;

@@ -11,7 +11,7 @@
 //             loss and dloss/dy -> backward (dW by split-K GEMMs reduced in fixed order,
 //             dH by GEMMs, SiLU', bias sums) -> Adam on the FP32 master weights ->
 //             bfloat16 copy for the next step
-//   finally   weights packed in mma fragment order for the inference kernel
+//   finally   weights packed into the tcgen05 inference kernel's shared-memory image
 #include "fdf_context.cuh"
 
 #include <cmath>
@@ -87,8 +87,8 @@ int alloc_params(FdfContext *ctx) {
   CU(cudaMalloc((void **)&L.adam_m, 4ull * MLP_NPARAM));
   CU(cudaMalloc((void **)&L.adam_v, 4ull * MLP_NPARAM));
   CU(cudaMalloc((void **)&L.params_bf, 2ull * MLP_NPARAM));
-  CU(cudaMalloc((void **)&L.frag, sizeof(uint2) * (size_t)MLP_FRAG_WORDS));
   CU(cudaMalloc((void **)&L.bias, 4ull * MLP_BIAS_WORDS));
+  CU(cudaMalloc((void **)&L.tc_img, mlp_tc_image_bytes()));
   return FDF_SUCCESS;
 }
 
@@ -111,16 +111,13 @@ void set_norm(FdfContext *ctx) {
   }
 }
 
-// Clears the optimiser state and makes the bfloat16 copy and the inference packing.
+// Makes the bfloat16 copy of the weights and the inference packing.
 void refresh_weights(FdfContext *ctx, cudaStream_t s) {
   LocatorState &L = ctx->loc;
   mlp_to_bf16(L.params, L.params_bf, MLP_NPARAM, s);
-  mlp_pack_frag(L.params + MLP_OFF_W1, MLP_H, 3, 16, 1, L.frag, s);
-  mlp_pack_frag(L.params + MLP_OFF_W2, MLP_H, MLP_H, 16, 8, L.frag + MLP_F2, s);
-  mlp_pack_frag(L.params + MLP_OFF_W3, MLP_H, MLP_H, 16, 8, L.frag + MLP_F3, s);
-  mlp_pack_frag(L.params + MLP_OFF_W4, 3, MLP_H, 1, 8, L.frag + MLP_F4, s);
   mlp_pack_bias(L.params, L.bias, s);
-  ctx->launches += 6;
+  mlp_pack_tc(L.params, L.tc_img, s);
+  ctx->launches += 3;
 }
 
 // Loss and gradients (into L.grads) of the batch in scratch (X, T), current weights.
@@ -167,7 +164,7 @@ void forward_backward(FdfContext *ctx, const TrainScratch &S, int B, float *loss
 void locator_free(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
   cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf);
-  cfree(L.frag); cfree(L.bias); cfree(L.pending); cfree(L.guess); cfree(L.scratch); cfree(L.pflag);
+  cfree(L.bias); cfree(L.tc_img); cfree(L.pending); cfree(L.guess); cfree(L.scratch); cfree(L.pflag);
   cfree(L.scan_sums);
   L.pending_cap = 0;
   L.batch_cap = 0;
@@ -395,17 +392,20 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
   }
   cudaError_t e = cudaMemcpyAsync(d_pos, soa.data(), 24ull * n, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
-    mlp_guess(ctx->loc.frag, ctx->loc.bias, ctx->loc.norm, d_pos, d_pos + n, d_pos + 2 * n, 0, nullptr, nullptr,
-              (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, s, d_out);
+    mlp_guess_tc(ctx->loc.tc_img, ctx->loc.bias, ctx->loc.norm, d_pos, d_pos + n, d_pos + 2 * n, 0, nullptr,
+                 nullptr, (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, &ctx->cnt->err, s, d_out);
     ctx->launches += 1;
     e = cudaGetLastError();
   }
   std::vector<int> gh((size_t)n);
   if (e == cudaSuccess) e = cudaMemcpyAsync(gh.data(), d_guess, 4ull * n, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && outputs) e = cudaMemcpyAsync(outputs, d_out, 12ull * n, cudaMemcpyDeviceToHost, s);
+  unsigned int errw = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&errw, &ctx->cnt->err, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaFree(d_pos); cudaFree(d_guess); cudaFree(d_out);
   if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_LocatorPredict: ") + cudaGetErrorString(e));
+  if (errw & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "fdf_LocatorPredict: tensor-core wait timed out");
   const long long IM = ctx->g.IM, JM = ctx->g.JM;
   for (int64_t p = 0; p < n; ++p) {
     const long long c = gh[p];

@@ -1,19 +1,15 @@
-// fdf_mlp.cu -- the learned start-cell locator: a 3-128-128-128-3 SiLU MLP that maps a
-// particle's physical position to a predicted (i, j, k) cell, trained on location pairs
-// produced by the walking search itself.  The walk remains the judge: the prediction
-// is only a starting cell (see the learned walk in fdf_fp32.cu).
+// fdf_mlp.cu -- training of the learned start-cell locator: a 3-128-128-128-3 SiLU MLP
+// that maps a particle's physical position to a predicted (i, j, k) cell, trained on
+// location pairs produced by the walking search itself.  The walk remains the judge: the
+// prediction is only a starting cell (the learned walk in fdf_fp32.cu); inference runs on
+// tcgen05 (fdf_mlp_tc.cu).
 //
-// Tensor cores: every GEMM, in training and inference, is mma.sync m16n8k16 with
-// bfloat16 operands and FP32 accumulation.
-//   * training: a generic warp-tile GEMM (16x8 output tile per warp, operands read with
-//     arbitrary strides, so the same kernel serves X W^T, G W and G^T H), plus
-//     elementwise kernels for bias + SiLU, the loss, SiLU', bias sums and Adam (FP32
-//     master weights).  Each output is computed by one warp in a fixed k order, and the
-//     sums run in fixed order, so training is deterministic.
-//   * inference: one fused kernel; each warp carries 16 particles through the four
-//     layers with activations in registers (the FP32 accumulator fragment of two adjacent
-//     8-column tiles is exactly the bfloat16 A fragment of the next layer's 16-deep k
-//     tile), weights staged once per block in shared memory in fragment order.
+// Every training GEMM is mma.sync m16n8k16 with bfloat16 operands and FP32 accumulation: a
+// generic warp-tile GEMM (16x8 output tile per warp, operands read with arbitrary strides, so
+// the same kernel serves X W^T, G W and G^T H), plus elementwise kernels for bias + SiLU, the
+// loss, SiLU', bias sums and Adam (FP32 master weights).  Each output is computed by one warp
+// in a fixed k order, and the sums run in fixed order, so training is deterministic.  The
+// training matrices are small (batch x 128 x 128); the hot path is inference.
 //
 // Fragment layouts of mma.m16n8k16 (g = lane/4, c = lane%4):
 //   A (16x16, row): a0 = A[g][2c..2c+1], a1 = A[g+8][2c..2c+1], a2 = A[g][2c+8..9], a3 = A[g+8][2c+8..9]
@@ -235,19 +231,7 @@ __global__ void k_make_samples(const double *__restrict__ x, const double *__res
 }
 
 // ---------------------------------------------------------------- inference
-// Fragment order of a layer's weights W [N][K] (out x in): for n-tile nt, k-tile kt and
-// lane, (b0, b1) as one uint2 at frag[(nt * KT + kt) * 32 + lane].
-__global__ void k_pack_frag(const float *__restrict__ W, int N, int K, int NT, int KT, uint2 *__restrict__ frag) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= NT * KT * 32) return;
-  const int lane = q & 31, t = q >> 5, kt = t % KT, nt = t / KT;
-  const int g = lane >> 2, c = lane & 3;
-  const int n = nt * 8 + g;
-  auto w = [&](int k) -> float { return (n < N && k < K) ? W[n * K + k] : 0.f; };
-  const int k0 = kt * 16 + 2 * c;
-  frag[q] = make_uint2(pack_bf16(w(k0), w(k0 + 1)), pack_bf16(w(k0 + 8), w(k0 + 9)));
-}
-
+// Biases of the four layers in one vector (b1 | b2 | b3 | b4, padded to MLP_BIAS_WORDS).
 __global__ void k_pack_bias(const float *__restrict__ params, float *__restrict__ bias) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= MLP_BIAS_WORDS) return;
@@ -257,128 +241,6 @@ __global__ void k_pack_bias(const float *__restrict__ params, float *__restrict_
   else if (q < 384) v = params[MLP_OFF_B3 + q - 256];
   else if (q < 387) v = params[MLP_OFF_B4 + q - 384];
   bias[q] = v;
-}
-
-// SiLU for inference: x * sigmoid(x) with sigmoid(x) = 0.5 + 0.5 tanh(x / 2), one MUFU op.
-__device__ __forceinline__ float silu_fast(float x) {
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * x));
-  return x * fmaf(0.5f, t, 0.5f);
-}
-
-// One hidden layer for a 16-row tile: A fragments of KT k-tiles -> SiLU activations of the
-// 16 output n-tiles, packed as the next layer's A fragments (8 k-tiles): the accumulator
-// pair of n-tiles 2p and 2p+1 is exactly k-tile p of the next layer's A.
-template <int KT>
-__device__ __forceinline__ void hidden_layer(const unsigned (&a)[KT][4], const uint2 *__restrict__ frag,
-                                             const float *__restrict__ bias, int lane, unsigned (&out)[8][4]) {
-  const int c = lane & 3;
-#pragma unroll
-  for (int p = 0; p < 8; ++p) {
-    float acc[2][4];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int nt = 2 * p + h;
-      float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
-#pragma unroll
-      for (int kt = 0; kt < KT; ++kt) {
-        const uint2 bv = frag[(nt * KT + kt) * 32 + lane];
-        mma_bf16(d0, d1, d2, d3, a[kt][0], a[kt][1], a[kt][2], a[kt][3], bv.x, bv.y);
-      }
-      const float bi0 = bias[nt * 8 + 2 * c], bi1 = bias[nt * 8 + 2 * c + 1];
-      acc[h][0] = silu_fast(d0 + bi0);
-      acc[h][1] = silu_fast(d1 + bi1);
-      acc[h][2] = silu_fast(d2 + bi0);
-      acc[h][3] = silu_fast(d3 + bi1);
-    }
-    out[p][0] = pack_bf16(acc[0][0], acc[0][1]);   // row g,   cols 16p + 2c, +1
-    out[p][1] = pack_bf16(acc[0][2], acc[0][3]);   // row g+8, cols 16p + 2c, +1
-    out[p][2] = pack_bf16(acc[1][0], acc[1][1]);   // row g,   cols 16p + 8 + 2c, +1
-    out[p][3] = pack_bf16(acc[1][2], acc[1][3]);   // row g+8, cols 16p + 8 + 2c, +1
-  }
-}
-
-__device__ __forceinline__ float load_coord(const double *a, unsigned int r, int pairs) {
-  if (pairs) {
-    const float2 pr = *reinterpret_cast<const float2 *>(a + r);
-    return pr.x + pr.y;
-  }
-  return (float)a[r];
-}
-
-// Persistent: each warp takes 16 particles at a time through the four layers.
-__global__ void __launch_bounds__(256, 2) k_mlp_guess(const uint2 *__restrict__ frag_g,
-                                                      const float *__restrict__ bias_g, MlpNorm norm,
-                                                      const double *__restrict__ px, const double *__restrict__ py,
-                                                      const double *__restrict__ pz, int pairs,
-                                                      const unsigned int *__restrict__ list,
-                                                      const unsigned long long *__restrict__ list_count, int n_host,
-                                                      GridDims g, int *__restrict__ guess, float *__restrict__ yout) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint2 *frag = reinterpret_cast<uint2 *>(smem);
-  float *bias = reinterpret_cast<float *>(smem + MLP_FRAG_WORDS * sizeof(uint2));
-  for (int q = threadIdx.x; q < MLP_FRAG_WORDS; q += blockDim.x) frag[q] = frag_g[q];
-  for (int q = threadIdx.x; q < MLP_BIAS_WORDS; q += blockDim.x) bias[q] = bias_g[q];
-  __syncthreads();
-  const long long n = list_count ? (long long)*list_count : (long long)n_host;
-  const int lane = threadIdx.x & 31, gq = lane >> 2, c = lane & 3;
-  const long long warps_total = ((long long)gridDim.x * blockDim.x) >> 5;
-  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const uint2 *f1 = frag, *f2 = frag + MLP_F2, *f3 = frag + MLP_F3, *f4 = frag + MLP_F4;
-  for (long long tile = warp; tile * 16 < n; tile += warps_total) {
-    const long long r0 = tile * 16 + gq, r1 = r0 + 8;
-    float in0[3] = {0.f, 0.f, 0.f}, in1[3] = {0.f, 0.f, 0.f};
-    if (c < 2) {   // lanes c = 0, 1 hold columns (x, y) and (z, 0) of rows r0 and r1
-      if (r0 < n) {
-        const unsigned int p = list ? list[r0] : (unsigned int)r0;
-        in0[0] = (load_coord(px, p, pairs) - norm.centre[0]) * norm.inv_half[0];
-        in0[1] = (load_coord(py, p, pairs) - norm.centre[1]) * norm.inv_half[1];
-        in0[2] = (load_coord(pz, p, pairs) - norm.centre[2]) * norm.inv_half[2];
-      }
-      if (r1 < n) {
-        const unsigned int p = list ? list[r1] : (unsigned int)r1;
-        in1[0] = (load_coord(px, p, pairs) - norm.centre[0]) * norm.inv_half[0];
-        in1[1] = (load_coord(py, p, pairs) - norm.centre[1]) * norm.inv_half[1];
-        in1[2] = (load_coord(pz, p, pairs) - norm.centre[2]) * norm.inv_half[2];
-      }
-    }
-    unsigned a1[1][4];
-    a1[0][0] = c == 0 ? pack_bf16(in0[0], in0[1]) : (c == 1 ? pack_bf16(in0[2], 0.f) : 0u);
-    a1[0][1] = c == 0 ? pack_bf16(in1[0], in1[1]) : (c == 1 ? pack_bf16(in1[2], 0.f) : 0u);
-    a1[0][2] = 0u;
-    a1[0][3] = 0u;
-    unsigned h1[8][4], h2[8][4];
-    hidden_layer<1>(a1, f1, bias, lane, h1);
-    hidden_layer<8>(h1, f2, bias + 128, lane, h2);
-    hidden_layer<8>(h2, f3, bias + 256, lane, h1);
-    float y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f;
-#pragma unroll
-    for (int kt = 0; kt < 8; ++kt) {
-      const uint2 bv = f4[kt * 32 + lane];
-      mma_bf16(y0, y1, y2, y3, h1[kt][0], h1[kt][1], h1[kt][2], h1[kt][3], bv.x, bv.y);
-    }
-    // lane c holds outputs (2c, 2c+1) of rows r0 (y0, y1) and r1 (y2, y3); output 2 is in c = 1
-    const float o2_r0 = __shfl_sync(0xffffffffu, y0, (lane & ~3) | 1);
-    const float o2_r1 = __shfl_sync(0xffffffffu, y2, (lane & ~3) | 1);
-    if (c == 0) {
-      const float bb0 = bias[384], bb1 = bias[385], bb2 = bias[386];
-      const int N[3] = {g.IM, g.JM, g.KM};
-      const float ya[3] = {y0 + bb0, y1 + bb1, o2_r0 + bb2}, yb[3] = {y2 + bb0, y3 + bb1, o2_r1 + bb2};
-      for (int h = 0; h < 2; ++h) {
-        const long long r = h ? r1 : r0;
-        if (r >= n) continue;
-        const float *yy = h ? yb : ya;
-        if (yout) { yout[3 * r] = yy[0]; yout[3 * r + 1] = yy[1]; yout[3 * r + 2] = yy[2]; }
-        int idx[3];
-        for (int d = 0; d < 3; ++d) {
-          const float t = (yy[d] + 1.0f) * 0.5f * (float)N[d];
-          const int v = (t == t) ? (int)fminf(fmaxf(floorf(t), 0.f), (float)(N[d] - 1)) : 0;
-          idx[d] = v;
-        }
-        guess[r] = (idx[2] * g.JM + idx[1]) * g.IM + idx[0];
-      }
-    }
-  }
 }
 
 inline unsigned blocks_for(long long n, int th) { return (unsigned)(n > 0 ? (n + th - 1) / th : 1); }
@@ -427,9 +289,6 @@ void mlp_to_bf16(const float *in, __nv_bfloat16 *out, int n, cudaStream_t s) {
 void mlp_sum_partials(const float *part, int n, float *out, cudaStream_t s) {
   k_sum_partials<<<1, 32, 0, s>>>(part, n, out);
 }
-void mlp_pack_frag(const float *W, int N, int K, int NT, int KT, uint2 *frag, cudaStream_t s) {
-  k_pack_frag<<<blocks_for(NT * KT * 32, 256), 256, 0, s>>>(W, N, K, NT, KT, frag);
-}
 void mlp_pack_bias(const float *params, float *bias, cudaStream_t s) {
   k_pack_bias<<<blocks_for(MLP_BIAS_WORDS, 256), 256, 0, s>>>(params, bias);
 }
@@ -440,26 +299,6 @@ void mlp_make_samples(const double *x, const double *y, const double *z, const i
                       const unsigned int *keep, long long n, MlpNorm norm, GridDims g, float *xs, float *ts,
                       cudaStream_t s) {
   k_make_samples<<<blocks_for(n, 256), 256, 0, s>>>(x, y, z, cell, slot, keep, n, norm, g, xs, ts);
-}
-
-void mlp_guess(const uint2 *frag, const float *bias, const MlpNorm &norm, const double *x, const double *y,
-               const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count, int n_host,
-               int n_cap, GridDims g, int *guess, int num_sms, cudaStream_t s, float *yout) {
-  const int smem = (int)(MLP_FRAG_WORDS * sizeof(uint2) + MLP_BIAS_WORDS * sizeof(float));
-  static int attr_device = -1;   // the attribute is per device; set it once for the current one
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (attr_device != dev) {
-    cudaFuncSetAttribute(k_mlp_guess, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr_device = dev;
-  }
-  const long long tiles = ((long long)n_cap + 15) / 16;
-  long long blocks = (tiles + 7) / 8;
-  const long long cap_blocks = (long long)num_sms * 2;
-  if (blocks > cap_blocks) blocks = cap_blocks;
-  if (blocks < 1) blocks = 1;
-  k_mlp_guess<<<(unsigned)blocks, 256, smem, s>>>(frag, bias, norm, x, y, z, pairs, list, list_count, n_host, g,
-                                                  guess, yout);
 }
 
 namespace {

@@ -2,8 +2,7 @@
 //
 // Parameters, FP32 master copy, one contiguous vector (row-major W [out][in]):
 //   W1 [128][3] | b1 [128] | W2 [128][128] | b2 [128] | W3 [128][128] | b3 [128] | W4 [3][128] | b4 [3]
-// Inference weights, bfloat16 in mma B-fragment order (uint2 per lane per 16x8 tile):
-//   layer 1: 16 n-tiles x 1 k-tile, layers 2 and 3: 16 x 8, layer 4: 1 x 8.
+// Inference weights: the tcgen05 kernel's shared-memory image (fdf_mlp_tc.cu) and the biases.
 #pragma once
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -20,10 +19,6 @@
 #define MLP_OFF_B4 33920
 #define MLP_NPARAM 33923
 
-#define MLP_F2 512              // fragment offsets (uint2 units)
-#define MLP_F3 4608
-#define MLP_F4 8704
-#define MLP_FRAG_WORDS 8960
 #define MLP_BIAS_WORDS 392      // b1 | b2 | b3 | b4 (387 used)
 
 // Input normalisation xhat = (x - centre) * inv_half, in FP32.
@@ -46,7 +41,6 @@ void mlp_colsum(const float *G, int B, int N, float *db, cudaStream_t s);
 void mlp_adam(float *w, const float *g, float *m, float *v, int n, float lr, float c1, float c2, cudaStream_t s);
 void mlp_to_bf16(const float *in, __nv_bfloat16 *out, int n, cudaStream_t s);
 void mlp_sum_partials(const float *part, int n, float *out, cudaStream_t s);
-void mlp_pack_frag(const float *W, int N, int K, int NT, int KT, uint2 *frag, cudaStream_t s);
 void mlp_pack_bias(const float *params, float *bias, cudaStream_t s);
 
 // Training samples from located points: xs = normalised FP32 position, ts = cell-centre target.
@@ -56,14 +50,19 @@ void mlp_make_samples(const double *x, const double *y, const double *z, const i
                       cudaStream_t s);
 void mlp_flag_located(const int *cell, const unsigned char *status, long long n, unsigned int *flag, cudaStream_t s);
 
-// Inference: guess[t] = predicted cell of particle list[t] (t < *list_count), positions
-// read as float pairs (hi, lo) from the precision-form swarm arrays.  list == nullptr:
-// particles 0 .. n_host-1, positions read as FP64 from x, y, z.  yout (optional):
-// the network's outputs [n][3].
-void mlp_guess(const uint2 *frag, const float *bias, const MlpNorm &norm, const double *x, const double *y,
-               const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count, int n_host,
-               int n_cap, GridDims g, int *guess, int num_sms, cudaStream_t s, float *yout = nullptr);
-
 // Initial weights: W uniform in +-1/sqrt(fan_in) from the splitmix64 streams (seed, 100 + layer),
 // biases zero (host).
 void mlp_init_params_host(unsigned long long seed, float *params);
+
+// Inference on tcgen05 (fdf_mlp_tc.cu): guess[t] = predicted cell of particle list[t]
+// (t < *list_count), positions read as float pairs (hi, lo) from the precision-form swarm
+// arrays; list == nullptr: particles 0 .. n_host-1, positions read as FP64 from x, y, z.
+// yout (optional): the network's outputs [n][3].  The weights are packed once into the CTA's
+// shared-memory image (mlp_tc_image_bytes() bytes); a timed-out tensor-core wait sets
+// ERRBIT_TC_TIMEOUT in *err.
+size_t mlp_tc_image_bytes();
+void mlp_pack_tc(const float *params, unsigned char *img, cudaStream_t s);
+void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &norm, const double *x, const double *y,
+                  const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count,
+                  int n_host, int n_cap, GridDims g, int *guess, int num_sms, unsigned int *err, cudaStream_t s,
+                  float *yout = nullptr);

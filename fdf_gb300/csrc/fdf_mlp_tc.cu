@@ -1,0 +1,340 @@
+// fdf_mlp_tc.cu -- inference of the learned start-cell locator on the 5th-generation tensor
+// cores (tcgen05): one CTA holds the network's bfloat16 weights in shared memory and carries
+// tiles of 128 particles through the four layers; each layer is tcgen05.mma (M = 128,
+// kind::f16, bfloat16 operands from shared memory, FP32 accumulator in tensor memory),
+// issued by one thread and tracked by an mbarrier; the four warps then read the accumulator
+// rows back with tcgen05.ld (one particle per thread), add the bias, apply SiLU and store the
+// bfloat16 activations as the next layer's A operand.  One CTA per SM holds the weights once
+// and runs four independent tile pipelines (one per warpgroup, each with its own activation
+// buffers, mbarrier and 128 TMEM columns), so the tensor core serves one pipeline's MMAs while
+// the others run their epilogues; each pipeline prefetches its next tile's positions while
+// the current tile computes.
+//
+// Shared-memory operand layout (no swizzle, K-major): an R x K bfloat16 matrix is stored as
+// 8-row x 16-byte core matrices; element (r, k) sits at
+//     (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2
+// with SBO = 16 * K bytes (all K / 8 core matrices of an 8-row group side by side), so the
+// core matrices adjacent in K are 128 B apart (the descriptor's leading byte offset) and the
+// 8-row groups SBO apart (its stride byte offset).  The MMA of K-slice s (16 elements) starts
+// at byte 256 s.
+//
+// Every wait on an mbarrier is bounded: past the limit the CTA records ERRBIT_TC_TIMEOUT,
+// frees its tensor memory and returns.
+#include "fdf_internal.cuh"
+#include "fdf_mlp.cuh"
+#include <cuda_bf16.h>
+
+namespace {
+
+constexpr int TC_ROWS = 128;                 // particles per tile (MMA M)
+constexpr int TC_PIPES = 4;                  // warpgroups per CTA, one tile pipeline each
+constexpr int TC_THREADS = 128 * TC_PIPES;
+constexpr int TC_TMEM_COLS = 128 * TC_PIPES; // FP32 accumulator columns, 128 per pipeline
+// shared memory map (bytes)
+constexpr int SM_W1 = 0;                     // [128][16]  4096
+constexpr int SM_W2 = SM_W1 + 4096;          // [128][128] 32768
+constexpr int SM_W3 = SM_W2 + 32768;         // [128][128] 32768
+constexpr int SM_W4 = SM_W3 + 32768;         // [16][128]  4096
+constexpr int SM_PIPE = SM_W4 + 4096;        // per pipeline: A1 [128][16] 4096, A [128][128] 32768
+constexpr int PIPE_BYTES = 4096 + 32768;
+constexpr int SM_BIAS = SM_PIPE + TC_PIPES * PIPE_BYTES;   // 392 floats
+constexpr int SM_BAR = SM_BIAS + 1568;       // mbarriers (8 B each), TMEM base (4 B), time-out flags
+constexpr int SM_TOTAL = SM_BAR + 8 * TC_PIPES + 8 + 4 * TC_PIPES;
+constexpr int WIMG_BYTES = SM_PIPE;          // packed weight image in global memory (73,728 B)
+constexpr unsigned long long WAIT_LIMIT = 1ull << 22;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride (8-row) byte
+// offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ unsigned long long make_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+  return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)(lbo >> 4) << 16) |
+         ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, bfloat16 A and B, both K-major.
+__host__ __device__ constexpr unsigned make_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(unsigned tmem_d, unsigned long long adesc, unsigned long long bdesc,
+                                        unsigned idesc, unsigned accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      :
+      : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(unsigned bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n.reg .pred P1;\nmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\nselp.b32 %0, 1, 0, P1;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
+  unsigned r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+__device__ __forceinline__ unsigned pack2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<unsigned *>(&v);
+}
+
+__device__ __forceinline__ float silu_fast(float x) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * x));
+  return x * fmaf(0.5f, t, 0.5f);
+}
+
+// byte offset of element (r, k) in the operand layout with SBO = sbo
+__host__ __device__ constexpr unsigned op_off(int r, int k, unsigned sbo) {
+  return (unsigned)(r / 8) * sbo + (unsigned)(k / 8) * 128u + (unsigned)(r % 8) * 16u + (unsigned)(k % 8) * 2u;
+}
+
+// Packs the FP32 parameters into the shared-memory image of the weights (bfloat16).
+__global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__restrict__ img) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;   // one bfloat16 element of the image
+  if (q >= WIMG_BYTES / 2) return;
+  const int byte = 2 * q;
+  float v = 0.f;
+  if (byte < SM_W2) {                                   // W1 [128][16], K padded from 3
+    const int o = byte - SM_W1;
+    const int rg = o / 256, kc = (o % 256) / 128, rr = (o % 128) / 16, kk = (o % 16) / 2;
+    const int n = rg * 8 + rr, k = kc * 8 + kk;
+    if (k < 3) v = params[MLP_OFF_W1 + n * 3 + k];
+  } else if (byte < SM_W4) {                            // W2, W3 [128][128]
+    const bool second = byte >= SM_W3;
+    const int o = byte - (second ? SM_W3 : SM_W2);
+    const int rg = o / 2048, kc = (o % 2048) / 128, rr = (o % 128) / 16, kk = (o % 16) / 2;
+    const int n = rg * 8 + rr, k = kc * 8 + kk;
+    v = params[(second ? MLP_OFF_W3 : MLP_OFF_W2) + n * 128 + k];
+  } else {                                              // W4 [16][128], N padded from 3
+    const int o = byte - SM_W4;
+    const int rg = o / 2048, kc = (o % 2048) / 128, rr = (o % 128) / 16, kk = (o % 16) / 2;
+    const int n = rg * 8 + rr, k = kc * 8 + kk;
+    if (n < 3) v = params[MLP_OFF_W4 + n * 128 + k];
+  }
+  reinterpret_cast<__nv_bfloat16 *>(img)[q] = __float2bfloat16_rn(v);
+}
+
+__device__ __forceinline__ float load_coord(const double *a, unsigned int r, int pairs) {
+  if (pairs) {
+    const float2 pr = *reinterpret_cast<const float2 *>(a + r);
+    return pr.x + pr.y;
+  }
+  return (float)a[r];
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_mlp_guess_tc(const unsigned char *__restrict__ wimg, const float *__restrict__ bias_g, MlpNorm norm,
+                   const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ pz,
+                   int pairs, const unsigned int *__restrict__ list, const unsigned long long *__restrict__ list_count,
+                   int n_host, GridDims g, int *__restrict__ guess, float *__restrict__ yout,
+                   unsigned int *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int pipe = tid >> 7, row = tid & 127;     // warpgroup = pipeline; thread = tile row
+  float *bias = reinterpret_cast<float *>(smem + SM_BIAS);
+  unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + SM_BAR);
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(smem + SM_BAR + 8 * TC_PIPES);
+  volatile unsigned *tflag = reinterpret_cast<volatile unsigned *>(smem + SM_BAR + 8 * TC_PIPES + 8);
+  unsigned char *a1s = smem + SM_PIPE + pipe * PIPE_BYTES, *as = a1s + 4096;
+  // weights and biases, once per CTA
+  {
+    const uint4 *src = reinterpret_cast<const uint4 *>(wimg);
+    uint4 *dst = reinterpret_cast<uint4 *>(smem);
+    for (int q = tid; q < WIMG_BYTES / 16; q += TC_THREADS) dst[q] = src[q];
+    for (int q = tid; q < MLP_BIAS_WORDS; q += TC_THREADS) bias[q] = bias_g[q];
+    uint4 *a1 = reinterpret_cast<uint4 *>(a1s);
+    for (int q = row; q < 4096 / 16; q += 128) a1[q] = make_uint4(0, 0, 0, 0);
+  }
+  const unsigned bar_addr = smem_u32(bars + pipe);
+  if (row == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_addr) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    tflag[pipe] = 0u;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  // this pipeline's accumulator columns; this warp's TMEM lane quarter
+  const unsigned tmem = *tmem_slot + (unsigned)(128 * pipe);
+  const unsigned lane_base = (unsigned)((warp & 3) * 32) << 16;
+  const unsigned sbase = smem_u32(smem), a1_addr = smem_u32(a1s), a_addr = smem_u32(as);
+  const unsigned id_hidden = make_idesc(TC_ROWS, 128), id_out = make_idesc(TC_ROWS, 16);
+  const unsigned pipe_bar = 1 + pipe;   // named barrier of this warpgroup (0 is __syncthreads)
+
+  const long long n = list_count ? (long long)*list_count : (long long)n_host;
+  const long long ntiles = (n + TC_ROWS - 1) / TC_ROWS;
+  const long long tile0 = (long long)blockIdx.x * TC_PIPES + pipe, tstride = (long long)gridDim.x * TC_PIPES;
+  unsigned phase = 0;
+  bool timed_out = false;
+
+  auto pipe_sync = [&]() { asm volatile("bar.sync %0, 128;\n" ::"r"(pipe_bar) : "memory"); };
+  // waits for the MMAs this pipeline committed last; its 128 threads agree on a time-out
+  auto wait_mma = [&]() -> bool {
+    bool done = false;
+    for (unsigned long long it = 0; it < WAIT_LIMIT && !done; ++it) done = mbar_try_wait(bar_addr, phase);
+    phase ^= 1u;
+    if (!done) tflag[pipe] = 1u;
+    pipe_sync();
+    const bool bad = tflag[pipe] != 0u;
+    fence_after_sync();
+    return !bad;
+  };
+  // bias + SiLU of the 128 accumulator columns, stored as the next layer's A operand
+  auto epilogue = [&](const float *b) {
+#pragma unroll 1
+    for (int c = 0; c < 8; ++c) {
+      float v[16];
+      tmem_ld16(tmem + lane_base + (unsigned)(16 * c), v);
+      unsigned w[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        w[q] = pack2(silu_fast(v[2 * q] + b[16 * c + 2 * q]), silu_fast(v[2 * q + 1] + b[16 * c + 2 * q + 1]));
+      *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
+      *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+  };
+  auto load_inputs = [&](long long tile, float &x, float &y, float &z) {
+    const long long r = tile * TC_ROWS + row;
+    x = 0.f; y = 0.f; z = 0.f;
+    if (tile < ntiles && r < n) {
+      const unsigned int p = list ? list[r] : (unsigned int)r;
+      x = (load_coord(px, p, pairs) - norm.centre[0]) * norm.inv_half[0];
+      y = (load_coord(py, p, pairs) - norm.centre[1]) * norm.inv_half[1];
+      z = (load_coord(pz, p, pairs) - norm.centre[2]) * norm.inv_half[2];
+    }
+  };
+  // the MMAs of one layer, issued by the pipeline's first thread after its threads' stores
+  auto issue = [&](int layer) {
+    fence_async_smem();
+    fence_before_sync();
+    pipe_sync();
+    if (row == 0) {
+      fence_after_sync();
+      if (layer == 0) {
+        mma_f16(tmem, make_desc(a1_addr, 128, 256), make_desc(sbase + SM_W1, 128, 256), id_hidden, 0u);
+      } else {
+        const unsigned wb = layer == 1 ? SM_W2 : layer == 2 ? SM_W3 : SM_W4;
+        const unsigned id = layer == 3 ? id_out : id_hidden;
+#pragma unroll 1
+        for (int k = 0; k < 8; ++k)
+          mma_f16(tmem, make_desc(a_addr + 256 * k, 128, 2048), make_desc(sbase + wb + 256 * k, 128, 2048), id,
+                  k > 0 ? 1u : 0u);
+      }
+      mma_commit(bar_addr);
+    }
+  };
+
+  float cx, cy, cz;
+  load_inputs(tile0, cx, cy, cz);
+#pragma unroll 1
+  for (long long tile = tile0; tile < ntiles; tile += tstride) {
+    const long long r = tile * TC_ROWS + row;
+    *reinterpret_cast<uint4 *>(a1s + op_off(row, 0, 256)) = make_uint4(pack2(cx, cy), pack2(cz, 0.f), 0u, 0u);
+    issue(0);
+    load_inputs(tile + tstride, cx, cy, cz);   // the next tile's positions, while this one computes
+    if (!wait_mma()) { timed_out = true; break; }
+    epilogue(bias);
+    issue(1);
+    if (!wait_mma()) { timed_out = true; break; }
+    epilogue(bias + 128);
+    issue(2);
+    if (!wait_mma()) { timed_out = true; break; }
+    epilogue(bias + 256);
+    issue(3);
+    if (!wait_mma()) { timed_out = true; break; }
+    {
+      float v[16];
+      tmem_ld16(tmem + lane_base, v);
+      if (r < n) {
+        const float y0 = v[0] + bias[384], y1 = v[1] + bias[385], y2 = v[2] + bias[386];
+        if (yout) { yout[3 * r] = y0; yout[3 * r + 1] = y1; yout[3 * r + 2] = y2; }
+        const float ys[3] = {y0, y1, y2};
+        const int N[3] = {g.IM, g.JM, g.KM};
+        int idx[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const float t = (ys[d] + 1.0f) * 0.5f * (float)N[d];
+          idx[d] = (t == t) ? (int)fminf(fmaxf(floorf(t), 0.f), (float)(N[d] - 1)) : 0;
+        }
+        guess[r] = (idx[2] * g.JM + idx[1]) * g.IM + idx[0];
+      }
+    }
+    fence_before_sync();   // this tile's TMEM reads finish before the next tile's MMAs (ordered by issue(0))
+  }
+  if (timed_out && row == 0) atomicOr(err, (unsigned)ERRBIT_TC_TIMEOUT);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tmem_slot), "r"(TC_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+size_t mlp_tc_image_bytes() { return WIMG_BYTES; }
+
+void mlp_pack_tc(const float *params, unsigned char *img, cudaStream_t s) {
+  k_pack_tc<<<(WIMG_BYTES / 2 + 255) / 256, 256, 0, s>>>(params, img);
+}
+
+void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &norm, const double *x, const double *y,
+                  const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count,
+                  int n_host, int n_cap, GridDims g, int *guess, int num_sms, unsigned int *err, cudaStream_t s,
+                  float *yout) {
+  static int attr_device = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (attr_device != dev) {
+    cudaFuncSetAttribute(k_mlp_guess_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
+    attr_device = dev;
+  }
+  const long long tiles = ((long long)n_cap + TC_ROWS - 1) / TC_ROWS;
+  long long blocks = (tiles + TC_PIPES - 1) / TC_PIPES;
+  const long long cap_blocks = (long long)num_sms;
+  if (blocks > cap_blocks) blocks = cap_blocks;
+  if (blocks < 1) blocks = 1;
+  k_mlp_guess_tc<<<(unsigned)blocks, TC_THREADS, SM_TOTAL, s>>>(img, bias, norm, x, y, z, pairs, list, list_count,
+                                                                 n_host, g, guess, yout, err);
+}
