@@ -31,7 +31,9 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300: learned+FP32 vs plain FP64 walk, exact cells"
 UNIT = "particle-steps/s"
 
-# Algorithmic bytes ("Roofline accounting").
+# Algorithmic bytes: particle state per particle, plus
+# one plane-table row per walk evaluation beyond the first (the first evaluation's row is the
+# particle's own cell, shared by the cell's particles in the cell-sorted order).
 ROW_BYTES = 296          # 36 plane doubles + threshold read per walk evaluation
 LOCATE_PER_PARTICLE = 53 + 61
 GATHER_PER_PARTICLE = 8 + 64 + 93
@@ -269,13 +271,25 @@ def prepare(ctx, wl, form, args):
 
 
 def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_step: float, Nc: int, Nn: int,
-                      Nf: int, momentum: bool = False) -> dict:
-    """Algorithmic bytes per launch of each stage (the accounting of the design doc 3.3); the
-    momentum deposit adds the particles' velocities and three components per face."""
-    if form in ("fp32", "learned_fp32"):
+                      Nf: int, momentum: bool = False, pending: float = 0.0) -> dict:
+    """Algorithmic bytes per launch of each stage; the momentum deposit adds the particles'
+    velocities and three components per face."""
+    if form == "learned_fp32":
+        # first pass: one evaluation per particle, pending flags and their scan; walk from the
+        # guess: the pending particles' state and the remaining evaluations
         return {
             "center_to_corner": 24 * nodes_per_step,
-            "advect_locate": 86 * n_avg + 176 * evals_per_step,
+            "advect_locate": 86 * n_avg + 16 * n_avg,
+            "guess_walk": 57 * pending + 176 * max(evals_per_step - n_avg, 0.0),
+            "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
+            "wait_corner": 0,
+            "gather_interpolate": 121 * n_avg + 12 * Nn,
+            "deposit": 4 * (Nc + 1) + 16 * n_avg + 8 * Nn + 4 * Nf + (12 * n_avg + 12 * Nf if momentum else 0),
+        }
+    if form == "fp32":
+        return {
+            "center_to_corner": 24 * nodes_per_step,
+            "advect_locate": 86 * n_avg + 176 * max(evals_per_step - n_avg, 0.0),
             "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
             "wait_corner": 0,
             "gather_interpolate": 121 * n_avg + 12 * Nn,
@@ -283,7 +297,7 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
         }
     return {
         "center_to_corner": 48 * nodes_per_step,
-        "advect_locate": LOCATE_PER_PARTICLE * n_avg + ROW_BYTES * evals_per_step,
+        "advect_locate": LOCATE_PER_PARTICLE * n_avg + ROW_BYTES * max(evals_per_step - n_avg, 0.0),
         "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
         "wait_corner": 0,
         "gather_interpolate": GATHER_PER_PARTICLE * n_avg + 24 * Nn,
@@ -328,12 +342,14 @@ def time_form(ctx, wl, form, args, dist, local, with_clocks):
     psteps, evals = ps1 - ps0, e1 - e0
     K = max(args.steps, 1)
     n_avg = psteps / K
-    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf, momentum_on(wl))
     runs = max(stages["sort_by_cell"][1], 1)     # one span per pipeline run
     per = {k: (v[0] / runs) for k, v in stages.items() if v[1] > 0}
     learned = None
+    asked = taken = gev = 0
     if form == "learned_fp32":
         asked, taken, gev = (b - a for a, b in zip(guess0, ctx.locator_stats()))
+    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf, momentum_on(wl), asked / K)
+    if form == "learned_fp32":
         mlp_ms = per.get("learned_guess", 0.0)
         tfl = MLP_FLOPS * asked / K / (mlp_ms / 1000.0) / 1e12 if mlp_ms > 0 else None
         learned = {"guesses_per_step": asked / K, "guess_fraction": asked / max(psteps, 1),

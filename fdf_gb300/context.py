@@ -245,7 +245,7 @@ class PicContext:
         return int(self.lib.fdf_GetLaunchCount(self.h))
 
     STAGES = ("center_to_corner", "advect_locate", "sort_by_cell", "wait_corner", "gather_interpolate",
-              "deposit", "learned_guess")
+              "deposit", "learned_guess", "guess_walk")
 
     def counters(self) -> tuple[int, int, int]:
         """(particle-steps advanced, walk evaluations made, corner nodes computed) since the swarm was set."""

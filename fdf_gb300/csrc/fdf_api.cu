@@ -25,7 +25,7 @@ constexpr long long FDF_MAX_PARTICLES = 512LL * 1024 * 1024;
 
 // Stage ids reported by fdf_GetStageTimes.
 enum { STAGE_CORNER = 0, STAGE_LOCATE = 1, STAGE_SORT = 2, STAGE_WAIT = 3, STAGE_GATHER_INTERP = 4,
-       STAGE_DEPOSIT = 5, STAGE_GUESS = 6, NUM_STAGES = 7 };
+       STAGE_DEPOSIT = 5, STAGE_GUESS = 6, STAGE_GUESS_WALK = 7, NUM_STAGES = 8 };
 
 size_t record_event(FdfContext *ctx, cudaStream_t stream) {
   if (ctx->ev_used == ctx->ev_pool.size()) {
@@ -500,7 +500,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   if (prof && learned) {
     ctx->ev_spans.push_back({STAGE_LOCATE, {e0, eg0}});
     ctx->ev_spans.push_back({STAGE_GUESS, {eg0, eg1}});
-    ctx->ev_spans.push_back({STAGE_LOCATE, {eg1, e1}});
+    ctx->ev_spans.push_back({STAGE_GUESS_WALK, {eg1, e1}});
   } else if (prof) {
     ctx->ev_spans.push_back({STAGE_LOCATE, {e0, e1}});
   }

@@ -1,6 +1,6 @@
 // fdf_mlp.cu -- training of the learned start-cell locator: a 3-128-128-128-3 SiLU MLP
 // that maps a particle's physical position to a predicted (i, j, k) cell, trained on
-// location pairs produced by the walking search itself.  The walk remains the judge: the
+// location pairs produced by the walking search itself.  The walk still decides the cell: the
 // prediction is only a starting cell (the learned walk in fdf_fp32.cu); inference runs on
 // tcgen05 (fdf_mlp_tc.cu).
 //

@@ -207,9 +207,9 @@ int64_t fdf_GetLaunchCount(FdfContext *ctx);
 /* Stage timing with CUDA events on the context stream (enable resets the record).
  * Stages: 0 center->corner (on a second stream, concurrent with 2), 1 advect+locate,
  * 2 sort by cell (histogram scan, slots, per-cell PID order), 3 wait for stage 0,
- * 4 gather+interpolate, 5 deposits, 6 learned guesses (learned form; its stage 1 is the
- * first evaluation plus the walk from the guess).  ms_total[s] sums the stage over all
- * pipeline runs since enabling; launches[s] counts the timed spans. */
+ * 4 gather+interpolate, 5 deposits; learned form: 6 network inference, 7 walk from the
+ * guess (its stage 1 is the first evaluation and the pending list).  ms_total[s] sums the
+ * stage over all pipeline runs since enabling; launches[s] counts the timed spans. */
 int fdf_SetProfiling(FdfContext *ctx, int enable);
 /* Running totals since fdf_SetSwarm: particles advanced (sum over steps of the live
  * particles at step start), walking-search cell evaluations actually made, and

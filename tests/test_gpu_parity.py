@@ -60,7 +60,7 @@ def run_parity(ctx, wl, steps, check_every=1, faces=True):
 
 
 def test_config1_full_size_parity(ctx):
-    """configs[0] of the workload list at its full size: 20x20x280 uniform grid, 10,000 particles
+    """The uniform configuration at its full size: 20x20x280 grid, 10,000 particles
     located from the corner cell like the reference, 10 steps."""
     wl = W.config1()
     out = run_parity(ctx, wl, wl.steps)
