@@ -53,6 +53,8 @@ def workload(name: str):
         return W.config_bent_pipe(n=8_000_000, materialize=False)
     if name == "bent_pipe_small":      # profiling case: 885K cells, 2M particles (> L2)
         return W.config_bent_pipe(48, 48, 384, n=2_000_000, materialize=False)
+    if name.startswith("bent_pipe_8m_cfl"):   # displacement sweep: bent_pipe_8m_cfl<C>
+        return W.config_bent_pipe(n=8_000_000, cfl=float(name[len("bent_pipe_8m_cfl"):]), materialize=False)
     if name == "curved_pipe":
         return W.config_curved_pipe(materialize=False)
     if name == "sinusoidal_medium":
@@ -255,6 +257,8 @@ def prepare(ctx, wl, form, args):
         ctx.set_momentum_deposit(True)
     if form != "learned_fp32":
         return
+    if args.guess_min_cells is not None:
+        ctx.locator_min_distance(args.guess_min_cells)
     if wl.name not in _TRAINED:
         import torch
         torch.cuda.synchronize()
@@ -565,6 +569,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=16000)
     ap.add_argument("--train-batch", type=int, default=8192)
     ap.add_argument("--train-lr", type=float, default=2e-3)
+    ap.add_argument("--guess-min-cells", type=float, default=None,
+                    help="learned form: particles at least this many cells past their cell get a guess")
     ap.add_argument("--identity-steps", type=int, default=3,
                     help="steps of the learned-vs-FP32-form identity check on the full workload (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -66,6 +66,7 @@ _SIGS = {
     "fdf_LocatorPredict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_void_p]),
     "fdf_LocatorGetStats": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p]),
+    "fdf_LocatorSetMinDistance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
 }
 
 

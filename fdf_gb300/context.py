@@ -306,6 +306,10 @@ class PicContext:
         self._check(self.lib.fdf_LocatorPredict(self.h, _ptr(p), len(p), _ptr(cells), _ptr(out)))
         return cells, out
 
+    def locator_min_distance(self, cells: float):
+        """Particles at least `cells` cells past their previous cell get a network guess."""
+        self._check(self.lib.fdf_LocatorSetMinDistance(self.h, float(cells)))
+
     def locator_stats(self) -> tuple[int, int, int]:
         """(particles given a guess, guesses kept, evaluations of the walks from the guesses)."""
         a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -444,7 +444,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     // start cell and walk from there (k_locate32_guess)
     LocatorState &L = ctx->loc;
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
-                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, L.pflag, s);
+                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, L.pflag, L.far_cells, s);
     exclusive_scan_u32(L.pflag, (long long)ctx->cap + 1, L.scan_sums, s);
     launch_compact_pending(L.pflag, ctx->cap, L.pending, ctx->cnt, s);
     eg0 = prof ? record_event(ctx, s) : 0;
@@ -453,10 +453,10 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     eg1 = prof ? record_event(ctx, s) : 0;
     launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
                           ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
-    ctx->launches += 2 + 3 + 1;   // guess, walk from the guess, flag scan, compaction
+    ctx->launches += 3 + 3 + 1;   // guess, walk from the guess, fallback walk, flag scan, compaction
   } else if (f32) {
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
-                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, nullptr, s);
+                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, nullptr, 0.f, s);
   } else {
     launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys,
                   ctx->cell_start, ctx->sentinel, s);

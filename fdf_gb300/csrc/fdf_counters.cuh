@@ -46,10 +46,14 @@ __device__ __forceinline__ void block_flush_counts(const LocCounts &m, DevCounte
       unsigned long long t = 0;
       for (int k = 0; k < nw; ++k) t += red[k][q];
       if (t) {
-        unsigned long long *dst[6] = {&cnt->removed_lost, &cnt->removed_oob, &cnt->evals, &cnt->evals_total,
-                                      &cnt->lost_total, &cnt->fallbacks};
-        atomicAdd(dst[q], t);
-        if (q == 5) atomicAdd(&cnt->fallbacks_total, t);
+        switch (q) {
+          case 0: atomicAdd(&cnt->removed_lost, t); break;
+          case 1: atomicAdd(&cnt->removed_oob, t); break;
+          case 2: atomicAdd(&cnt->evals, t); break;
+          case 3: atomicAdd(&cnt->evals_total, t); break;
+          case 4: atomicAdd(&cnt->lost_total, t); break;
+          default: atomicAdd(&cnt->fallbacks, t); atomicAdd(&cnt->fallbacks_total, t); break;
+        }
       }
     } else {
       unsigned int t = 0;

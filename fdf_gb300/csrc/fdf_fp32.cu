@@ -308,11 +308,29 @@ __device__ __forceinline__ unsigned int settle_key32(bool lost, int cell, float2
   return key;
 }
 
+// How far past the previous cell a particle is, in cells, from the first evaluation's
+// distances: for each index direction with a negative face, -d_neg / (d_lower + d_upper)
+// (the two planes' distances add up to the cell's width there).  Only steers which exact path
+// the learned form takes, so it may be approximate; a degenerate width gives +inf.
+__device__ __forceinline__ float beyond_cells(const float (&dv)[6]) {
+  float far = 0.f;
+  const int lo[3] = {F_LEFT, F_BOTTOM, F_BACK}, hi[3] = {F_RIGHT, F_TOP, F_FRONT};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float dl = dv[lo[a]], dh = dv[hi[a]], width = dl + dh;
+    const float neg = dl < 0.f ? -dl : (dh < 0.f ? -dh : 0.f);
+    if (neg > 0.f) far = fmaxf(far, width > 0.f ? __fdividef(neg, width) : INFINITY);
+  }
+  return far;
+}
+
 // Advect + locate, one thread per particle.
 //   FIRST == false: the reference walk from the previous cell (or cell (0,0,0)).
-//   FIRST == true:  the reference's first evaluation only, in the previous cell; a particle
-//                   that it does not conclude is flagged in `pending` (n_cap + 1 flags) and
-//                   finished by k_locate32_guess (its key and histogram entry are written there).
+//   FIRST == true:  the reference's first evaluation, in the previous cell; a particle that it
+//                   does not conclude and that lies at least far_cells past that cell is
+//                   flagged in `pending` (n_cap + 1 flags) and finished by k_locate32_guess (its
+//                   key and histogram entry are written there); a nearer one continues the
+//                   reference walk here.
 template <bool FIRST>
 __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
@@ -320,7 +338,7 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
                                                   const float *__restrict__ fbox, int drop_removed,
                                                   DevCounters *cnt, unsigned int *__restrict__ keys,
                                                   unsigned int *__restrict__ count, unsigned int sentinel,
-                                                  unsigned int *__restrict__ pending, int n_cap) {
+                                                  unsigned int *__restrict__ pending, int n_cap, float far_cells) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
@@ -349,7 +367,18 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
       // learned form: the walk's next cell (w.i, w.j, k) is where the reference continues;
       // outside the grid it ends there as LOST, as the reference's next loop test does
       const bool next_inside = w.i >= 0 && w.i < g.IM && w.j >= 0 && w.j < g.JM && w.k >= 0 && w.k < g.KM;
-      if (FIRST && !w.concluded && !w.lost && next_inside) {
+      if (FIRST && !w.concluded && !w.lost && next_inside && !(far_cells <= beyond_cells(w.e.dv))) {
+        // close to the previous cell: the reference walk continues here from its second cell
+        Walk32 w2;
+        w2.i = w.i; w2.j = w.j; w2.k = w.k; w2.err = 0u;
+        walk_ref32(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w2, m.fb);
+        m.err |= w2.err;
+        m.done += (unsigned long long)w2.evaluated;
+        m.evals += (unsigned long long)(w.evaluated + w2.evaluated);
+        lost = w2.lost || !w2.concluded;
+        store_located32(b, s, g, lost, w2.i, w2.j, w2.k, w2.e.dv);
+        cell = lost ? -1 : (int)(((long long)w2.k * g.JM + w2.j) * g.IM + w2.i);
+      } else if (FIRST && !w.concluded && !w.lost && next_inside) {
         wait = true;
         m.evals += (unsigned long long)w.evaluated;
         b.cell[s] = (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
@@ -396,9 +425,9 @@ __global__ void k_compact_pending(const unsigned int *__restrict__ scan, int n_c
 // learned guess and runs for at most FDF_GUESS_WALK evaluations.  Its cell C is taken
 // when C == P1 (the reference evaluates P1 next and concludes there with the same exact
 // decisions), or when it ends with every face positive by more than thr + C's overlap
-// margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise the reference
-// walk continues from P1 as its second evaluation.  Grid-stride over the list,
-// warp-uniform trip count.
+// margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise guess[t] becomes
+// -1 and k_locate32_fallback continues the reference walk from P1.  Grid-stride over the
+// list, warp-uniform trip count.
 __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                         const double *__restrict__ planes,
                                                         const double *__restrict__ bbox,
@@ -406,23 +435,20 @@ __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, 
                                                         DevCounters *cnt, unsigned int *__restrict__ keys,
                                                         unsigned int *__restrict__ count, unsigned int sentinel,
                                                         const unsigned int *__restrict__ pending,
-                                                        const int *__restrict__ guess) {
+                                                        int *__restrict__ guess) {
   const long long npend = (long long)cnt->pending;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
   unsigned long long acc = 0, gev = 0;
-  LocCounts mt;   // this thread's counters over all its list entries
+  LocCounts m;   // this thread's counters over all its list entries
   for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < npend; base += stride) {
     const long long t = base + lane;
-    LocCounts &m = mt;
     unsigned int hkey = 0xffffffffu;
     if (t < npend) {
       const int s = (int)pending[t];
       const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
-      const int prev = b.cell[s];
-      int pi = 0, pj = 0, pk = 0;
-      if (prev >= 0 && (long long)prev < g.Nc) cell_ijk(g, (unsigned int)prev, pi, pj, pk);
-      // walk from the guess
+      int pi, pj, pk;
+      cell_ijk(g, (unsigned int)b.cell[s], pi, pj, pk);
       Eval32 e;
       int gi, gj, gk;
       cell_ijk(g, (unsigned int)guess[t], gi, gj, gk);
@@ -445,36 +471,83 @@ __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, 
         if (ng & (1u << F_LEFT)) gi -= 1; else if (ng & (1u << F_RIGHT)) gi += 1;
         if (ng & (1u << F_BOTTOM)) gj -= 1; else if (ng & (1u << F_TOP)) gj += 1;
       }
-      bool lost;
-      int cell;
       if (taken) {
         ++acc;
-        lost = false;
         store_located32(b, s, g, false, gi, gj, gk, e.dv);
-        cell = (int)(((long long)gk * g.JM + gj) * g.IM + gi);
+        const int cell = (int)(((long long)gk * g.JM + gj) * g.IM + gi);
+        const unsigned int key =
+            settle_key32(false, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
+        keys[s] = key;
+        if (key < sentinel) hkey = key;
+        else if (!drop_removed) hkey = sentinel;
       } else {
-        Walk32 w;   // the reference walk from its second evaluation on (one step already made)
-        w.i = pi; w.j = pj; w.k = pk; w.err = 0u;
+        guess[t] = -1;   // the reference walk from P1 decides (k_locate32_fallback)
+      }
+    }
+    warp_histogram(hkey, count);
+  }
+  block_flush_counts(m, cnt);
+  block_add_u64(acc, &cnt->guess_taken_total);
+  block_add_u64(gev, &cnt->guess_evals_total);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->guess_asked_total, (unsigned long long)npend);
+}
+
+// The pending particles whose guess was not taken (guess[t] < 0): the reference walk from its
+// second cell P1 (b.cell[s]), the remaining MAX_TRAVERSAL - 1 evaluations allowed.  Each warp
+// scans a chunk of 32 x 32 list entries, queues the failed ones in shared memory and walks
+// them 32 at a time, so every lane has a particle.
+constexpr int FB_CHUNK = 1024;
+__global__ void __launch_bounds__(256) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
+                                                           const double *__restrict__ planes,
+                                                           const double *__restrict__ bbox,
+                                                           const float *__restrict__ fbox, int drop_removed,
+                                                           DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                           unsigned int *__restrict__ count, unsigned int sentinel,
+                                                           const unsigned int *__restrict__ pending,
+                                                           const int *__restrict__ guess) {
+  __shared__ unsigned int queue[8][FB_CHUNK];
+  const long long npend = (long long)cnt->pending;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  LocCounts m;
+  unsigned int *q = queue[wib];
+  for (long long chunk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk * FB_CHUNK < npend;
+       chunk += warps) {
+    int nq = 0;
+    for (int i = 0; i < FB_CHUNK / 32; ++i) {
+      const long long t = chunk * FB_CHUNK + i * 32 + lane;
+      const bool fail = t < npend && guess[t] < 0;
+      const unsigned int bal = __ballot_sync(0xffffffffu, fail);
+      if (fail) q[nq + __popc(bal & ((1u << lane) - 1u))] = (unsigned int)t;
+      nq += __popc(bal);
+    }
+    __syncwarp();
+    for (int base = 0; base < nq; base += 32) {
+      unsigned int hkey = 0xffffffffu;
+      if (base + lane < nq) {
+        const int s = (int)pending[q[base + lane]];
+        const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
+        Walk32 w;
+        w.err = 0u;
+        cell_ijk(g, (unsigned int)b.cell[s], w.i, w.j, w.k);
         walk_ref32(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w, m.fb);
         m.err |= w.err;
         m.done += (unsigned long long)w.evaluated;
         m.evals += (unsigned long long)w.evaluated;
-        lost = w.lost || !w.concluded;
+        const bool lost = w.lost || !w.concluded;
         store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
-        cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
+        const int cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
+        const unsigned int key =
+            settle_key32(lost, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
+        keys[s] = key;
+        if (key < sentinel) hkey = key;
+        else if (!drop_removed) hkey = sentinel;
       }
-      const unsigned int key =
-          settle_key32(lost, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
-      keys[s] = key;
-      if (key < sentinel) hkey = key;
-      else if (!drop_removed) hkey = sentinel;
+      warp_histogram(hkey, count);
     }
-    warp_histogram(hkey, count);
+    __syncwarp();
   }
-  block_flush_counts(mt, cnt);
-  block_add_u64(acc, &cnt->guess_taken_total);
-  block_add_u64(gev, &cnt->guess_evals_total);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->guess_asked_total, (unsigned long long)npend);
+  block_flush_counts(m, cnt);
 }
 
 // Corner field in FP32: mean of the valid adjacent cells (nodes next to occupied cells).
@@ -699,15 +772,15 @@ void launch_build_table32(const double *planes, const double *coor, GridDims g, 
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                      unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
-                     cudaStream_t s) {
+                     float far_cells, cudaStream_t s) {
   if (pending)
     k_locate32<true><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox,
                                                             fbox, drop_removed, cnt, keys, count, sentinel, pending,
-                                                            n_cap);
+                                                            n_cap, far_cells);
   else
     k_locate32<false><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed,
                                                              bbox, fbox, drop_removed, cnt, keys, count, sentinel,
-                                                             nullptr, n_cap);
+                                                             nullptr, n_cap, 0.f);
 }
 
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
@@ -718,13 +791,15 @@ void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *l
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
                            const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                            unsigned int *keys, unsigned int *count, unsigned int sentinel,
-                           const unsigned int *pending, const int *guess, int num_sms, cudaStream_t s) {
+                           const unsigned int *pending, int *guess, int num_sms, cudaStream_t s) {
   long long blocks = ((long long)n_cap + 255) / 256;
   const long long cap = (long long)num_sms * 8;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   k_locate32_guess<<<(unsigned)blocks, 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
                                                     sentinel, pending, guess);
+  k_locate32_fallback<<<(unsigned)blocks, 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
+                                                       sentinel, pending, guess);
 }
 
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,

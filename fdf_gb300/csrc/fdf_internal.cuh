@@ -24,7 +24,7 @@
 #define FDF_DISTANCE_THRESHOLD 1e-11
 #define FDF_INTERP_DIST_TOL 1e-14
 #define FDF_BBOX_TOL 1e-6
-#define FDF_GUESS_WALK 8      // evaluations allowed to the walk from a learned guess
+#define FDF_GUESS_WALK 4      // evaluations allowed to the walk from a learned guess
 #define FDF_GUESS_REACH 16    // largest index distance from the previous cell a guess may settle at
 
 // Face order of the reference (common.h Face enum).
@@ -156,19 +156,22 @@ void launch_build_table32(const double *planes, const double *coor, GridDims g, 
 // fbox: 12 floats, (x, y, z, -) lower and (x, y, z, -) upper bounds strictly inside the
 // bounding box by more than any lo part of a position inside it, then 4 unused.
 // pending != nullptr: the learned form's first pass (one evaluation in the previous cell;
-// pending[s] = 1 for the particles that leave it, 0 otherwise, for s <= n_cap).
+// pending[s] = 1 for the particles that leave it by at least far_cells cells, 0 otherwise,
+// for s <= n_cap; the others are located here).
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                      unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
-                     cudaStream_t s);
+                     float far_cells, cudaStream_t s);
 // The learned form's pending list from the scanned flags (sets cnt->pending).
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
                             cudaStream_t s);
-// The learned form's second pass over pending[0 .. cnt->pending), guess[t] = start cell.
+// The learned form's second pass over pending[0 .. cnt->pending), guess[t] = start cell:
+// the walk from the guess, then the reference walk for the guesses not taken (guess[t] set
+// to -1 in between).
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
                            const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                            unsigned int *keys, unsigned int *count, unsigned int sentinel,
-                           const unsigned int *pending, const int *guess, int num_sms, cudaStream_t s);
+                           const unsigned int *pending, int *guess, int num_sms, cudaStream_t s);
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
                                unsigned long long *nodes_done, cudaStream_t s);
 void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,

@@ -416,6 +416,13 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
   return FDF_SUCCESS;
 }
 
+int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!(cells >= 0.0)) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorSetMinDistance: cells must be >= 0");
+  ctx->loc.far_cells = (float)cells;
+  return FDF_SUCCESS;
+}
+
 int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals) {
   if (!ctx || !asked || !taken || !guess_evals) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));

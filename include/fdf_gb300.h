@@ -75,8 +75,10 @@ typedef struct {
  * threshold plus the cell's overlap margin (the largest gap between the cell's face planes
  * and the planes of the same grid surfaces on the neighbouring patches), within
  * FDF_GUESS_REACH = 16 cells of the previous cell in each index; otherwise the reference
- * walk from the previous cell decides.  Cells, weights and statuses are then those of the
- * FP32 form except where the reference's own result depends on where its walk starts. */
+ * walk from the previous cell decides.  Particles that stay within about a cell of their
+ * previous cell skip the network (fdf_LocatorSetMinDistance).  Cells, weights and statuses are
+ * then those of the FP32 form except where the reference's own result depends on where its
+ * walk starts. */
 #define FDF_FORM_LEARNED_FP32 2
 
 /* ---- context, grid and fields (replace UserCtx set-up: setup.c:197-290, grid.c:34-160) ---- */
@@ -193,6 +195,11 @@ int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target
                          float *loss);
 /* Predicted cells (i, j, k) of n host positions [n][3]; outputs (optional) [n][3] = y. */
 int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs);
+/* Which particles the learned form asks the network: after the reference's first evaluation
+ * (in the previous cell), a particle estimated at least `cells` cells past that cell (from the
+ * evaluation's face distances) gets a guess; a nearer one continues the reference walk at once.
+ * Default 1.0; 0 asks for every particle that left its cell.  Results do not depend on it. */
+int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells);
 /* Running totals of the learned form: particles given a guess, guesses whose walk was
  * kept, and evaluations made by the walks from the guesses. */
 int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals);

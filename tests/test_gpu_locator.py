@@ -8,7 +8,8 @@
   0.02 (outputs are O(1)), and its cells are floor((y + 1) N / 2) of its outputs.
 * Training on walk-produced pairs is deterministic and reduces the loss.
 * The learned form gives the FP32 form's swarm, fields and deposits bit for bit, with a
-  trained and with an untrained network, and the trained network reduces the walk.
+  trained and with an untrained network, with either guess policy, and the trained network
+  reduces the walk.
 """
 import numpy as np
 import pytest
@@ -116,15 +117,23 @@ def test_training_deterministic_and_learns(small):
     assert np.mean(cheb <= 1) >= 0.6
 
 
-def _run(form, wl, steps, train=None):
+def _run(form, wl, steps, params=None, train=None, min_cells=None):
+    """Initial setup + steps in one form; the learned form gets trained (train), given (params)
+    or untrained (neither) weights.  Returns (swarm, faces, fields, psteps, evals, stats, params)."""
     ctx = PicContext(0)
     try:
         ctx.load_workload(wl, form=form)
+        p = None
         if form == FORM_LEARNED_FP32:   # the locator belongs to the grid set by load_workload
-            if train is None:
-                ctx.locator_init(seed=0)
-            else:
+            if train is not None:
                 ctx.locator_train(**train)
+            elif params is not None:
+                ctx.locator_set_params(params)
+            else:
+                ctx.locator_init(seed=0)
+            if min_cells is not None:
+                ctx.locator_min_distance(min_cells)
+            p = ctx.locator_get_params()
         ctx.initial_setup()
         for _ in range(steps):
             ctx.step(info=False)
@@ -134,7 +143,7 @@ def _run(form, wl, steps, train=None):
         sc = ctx.get_scattered()
         psteps, evals, _ = ctx.counters()
         stats = ctx.locator_stats() if form == FORM_LEARNED_FP32 else None
-        return s, faces, sc, psteps, evals, stats
+        return s, faces, sc, psteps, evals, stats, p
     finally:
         ctx.close()
 
@@ -143,10 +152,12 @@ def _run(form, wl, steps, train=None):
 def pipe_runs(require_gpu):
     wl = W.config_bent_pipe(24, 24, 192, n=300_000, cfl=4.0, materialize=False)
     train = dict(n_samples=1_000_000, seed=7, steps=3000, batch=8192, lr=2e-3)
+    learned = _run(FORM_LEARNED_FP32, wl, 4, train=train)
     return wl, {
         "fp32": _run(FORM_FP32, wl, 4),
-        "learned": _run(FORM_LEARNED_FP32, wl, 4, train),
-        "untrained": _run(FORM_LEARNED_FP32, wl, 4, None),
+        "learned": learned,                                                         # default policy
+        "learned_all": _run(FORM_LEARNED_FP32, wl, 4, params=learned[6], min_cells=0.0),   # every mover
+        "untrained": _run(FORM_LEARNED_FP32, wl, 4, min_cells=0.0),
     }
 
 
@@ -161,18 +172,23 @@ def _same(a, b):
 
 def test_learned_form_identical_to_fp32_form(pipe_runs):
     _, r = pipe_runs
-    _same(r["fp32"], r["learned"])
-    _same(r["fp32"], r["untrained"])
+    for key in ("learned", "learned_all", "untrained"):
+        _same(r["fp32"], r[key])
 
 
 def test_trained_locator_shortens_walk(pipe_runs):
+    """Asking the network for every particle that left its cell: the trained network needs far
+    fewer walk evaluations than the untrained one; the default policy asks only for particles
+    a cell or more away."""
     _, r = pipe_runs
     ps = r["fp32"][3]
-    e_fp32, e_learn, e_untr = r["fp32"][4], r["learned"][4], r["untrained"][4]
-    asked, taken, gev = r["learned"][5]
-    asked_u, taken_u, gev_u = r["untrained"][5]
-    print(f"[gain] walk evaluations per particle-step: FP32 form {e_fp32 / ps:.3f}, learned {e_learn / ps:.3f}, "
-          f"untrained {e_untr / ps:.3f}; guesses kept {taken}/{asked} (untrained {taken_u}/{asked_u}), "
-          f"evaluations per kept-or-tried guess {gev / max(asked, 1):.2f}")
+    e = {k: r[k][4] / ps for k in ("fp32", "learned", "learned_all", "untrained")}
+    st = {k: r[k][5] for k in ("learned", "learned_all", "untrained")}
+    print("[gain] walk evaluations per particle-step: " + ", ".join(f"{k} {v:.3f}" for k, v in e.items()))
+    for k, (asked, taken, gev) in st.items():
+        print(f"[gain] {k}: guesses {asked}, kept {taken / max(asked, 1):.3f}, "
+              f"evaluations per guess {gev / max(asked, 1):.2f}")
+    asked, taken, _ = st["learned_all"]
     assert taken > 0.5 * asked
-    assert e_learn < e_untr
+    assert e["learned_all"] < e["untrained"]
+    assert st["learned"][0] < st["learned_all"][0]
