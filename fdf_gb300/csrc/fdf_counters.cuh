@@ -10,8 +10,9 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
   return v;
 }
 
+// Per-thread counts stay far below 2^32 within one launch; the block sums are 64-bit.
 struct LocCounts {
-  unsigned long long lost = 0, oob = 0, evals = 0, done = 0, lost_total = 0, fb = 0;
+  unsigned int lost = 0, oob = 0, evals = 0, done = 0, lost_total = 0, fb = 0;
   unsigned int err = 0;
 };
 
@@ -30,7 +31,7 @@ __device__ __forceinline__ void block_flush_counts(const LocCounts &m, DevCounte
   __shared__ unsigned int rerr[32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   __syncthreads();   // a previous call's readers are done with the shared words
-  unsigned long long v[6] = {m.lost, m.oob, m.evals, m.done, m.lost_total, m.fb};
+  unsigned long long v[6] = {m.lost, m.oob, m.evals, m.done, m.lost_total, m.fb};   // widened before the sums
 #pragma unroll
   for (int q = 0; q < 6; ++q) v[q] = warp_sum_u64(v[q]);
   const unsigned int e = __reduce_or_sync(0xffffffffu, m.err);

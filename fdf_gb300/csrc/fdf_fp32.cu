@@ -172,7 +172,7 @@ struct Eval32 {
 template <bool CERT>
 __device__ __forceinline__ void eval_cell32(const float *__restrict__ table, const double *__restrict__ planes,
                                             long long cur, float2 px, float2 py, float2 pz, float sx, float sy,
-                                            float sz, Eval32 &e, unsigned long long &fb) {
+                                            float sz, Eval32 &e, unsigned int &fb) {
   const float4 *row = reinterpret_cast<const float4 *>(table + cur * FDF_ROW32);
   const float4 h0 = __ldg(row), h1 = __ldg(row + 1);
   e.neg = 0u;
@@ -234,7 +234,7 @@ struct Walk32 {
 
 __device__ __forceinline__ void walk_ref32(const float *__restrict__ table, const double *__restrict__ planes,
                                            const GridDims &g, float2 px, float2 py, float2 pz, int limit, Walk32 &w,
-                                           unsigned long long &fb) {
+                                           unsigned int &fb) {
   const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
   long long saved = -1;
   int power = 1, lam = 0;
@@ -286,8 +286,8 @@ __device__ __forceinline__ void store_located32(const SwarmBuf &b, int s, const 
 __device__ __forceinline__ unsigned int settle_key32(bool lost, int cell, float2 px, float2 py, float2 pz,
                                                      int drop_removed, const double *__restrict__ bbox,
                                                      const float *__restrict__ fbox, unsigned int sentinel,
-                                                     unsigned long long &my_lost, unsigned long long &my_oob,
-                                                     unsigned long long &my_lost_total) {
+                                                     unsigned int &my_lost, unsigned int &my_oob,
+                                                     unsigned int &my_lost_total) {
   unsigned int key = lost ? sentinel : (unsigned int)cell;
   if (lost) my_lost_total += 1;
   if (drop_removed) {
@@ -332,7 +332,7 @@ __device__ __forceinline__ float beyond_cells(const float (&dv)[6]) {
 //                   key and histogram entry are written there); a nearer one continues the
 //                   reference walk here.
 template <bool FIRST>
-__global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(256, 3) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
                                                   int reset_first, const double *__restrict__ bbox,
                                                   const float *__restrict__ fbox, int drop_removed,
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
       if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, w.i, w.j, w.k);
       walk_ref32(table, planes, g, px, py, pz, FIRST ? 1 : FDF_MAX_TRAVERSAL, w, m.fb);
       m.err |= w.err;
-      m.done += (unsigned long long)w.evaluated;
+      m.done += (unsigned int)w.evaluated;
       // learned form: the walk's next cell (w.i, w.j, k) is where the reference continues;
       // outside the grid it ends there as LOST, as the reference's next loop test does
       const bool next_inside = w.i >= 0 && w.i < g.IM && w.j >= 0 && w.j < g.JM && w.k >= 0 && w.k < g.KM;
@@ -373,18 +373,17 @@ __global__ void __launch_bounds__(256) k_locate32(SwarmBuf b, GridDims g, const 
         w2.i = w.i; w2.j = w.j; w2.k = w.k; w2.err = 0u;
         walk_ref32(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w2, m.fb);
         m.err |= w2.err;
-        m.done += (unsigned long long)w2.evaluated;
-        m.evals += (unsigned long long)(w.evaluated + w2.evaluated);
+        m.done += (unsigned int)w2.evaluated;
+        m.evals += (unsigned int)(w.evaluated + w2.evaluated);
         lost = w2.lost || !w2.concluded;
         store_located32(b, s, g, lost, w2.i, w2.j, w2.k, w2.e.dv);
         cell = lost ? -1 : (int)(((long long)w2.k * g.JM + w2.j) * g.IM + w2.i);
       } else if (FIRST && !w.concluded && !w.lost && next_inside) {
         wait = true;
-        m.evals += (unsigned long long)w.evaluated;
+        m.evals += (unsigned int)w.evaluated;
         b.cell[s] = (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
       } else {
-        m.evals += FIRST ? (unsigned long long)w.evaluated
-                         : (unsigned long long)(w.cycle ? FDF_MAX_TRAVERSAL : w.steps);
+        m.evals += FIRST ? (unsigned int)w.evaluated : (unsigned int)(w.cycle ? FDF_MAX_TRAVERSAL : w.steps);
         lost = w.lost || !w.concluded;
         store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
         cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
@@ -428,7 +427,7 @@ __global__ void k_compact_pending(const unsigned int *__restrict__ scan, int n_c
 // margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise guess[t] becomes
 // -1 and k_locate32_fallback continues the reference walk from P1.  Grid-stride over the
 // list, warp-uniform trip count.
-__global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(256, 3) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                         const double *__restrict__ planes,
                                                         const double *__restrict__ bbox,
                                                         const float *__restrict__ fbox, int drop_removed,
@@ -439,7 +438,7 @@ __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, 
   const long long npend = (long long)cnt->pending;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
-  unsigned long long acc = 0, gev = 0;
+  unsigned int acc = 0, gev = 0;
   LocCounts m;   // this thread's counters over all its list entries
   for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < npend; base += stride) {
     const long long t = base + lane;
@@ -497,7 +496,7 @@ __global__ void __launch_bounds__(256) k_locate32_guess(SwarmBuf b, GridDims g, 
 // scans a chunk of 32 x 32 list entries, queues the failed ones in shared memory and walks
 // them 32 at a time, so every lane has a particle.
 constexpr int FB_CHUNK = 1024;
-__global__ void __launch_bounds__(256) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                            const double *__restrict__ planes,
                                                            const double *__restrict__ bbox,
                                                            const float *__restrict__ fbox, int drop_removed,
@@ -532,8 +531,8 @@ __global__ void __launch_bounds__(256) k_locate32_fallback(SwarmBuf b, GridDims 
         cell_ijk(g, (unsigned int)b.cell[s], w.i, w.j, w.k);
         walk_ref32(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w, m.fb);
         m.err |= w.err;
-        m.done += (unsigned long long)w.evaluated;
-        m.evals += (unsigned long long)w.evaluated;
+        m.done += (unsigned int)w.evaluated;
+        m.evals += (unsigned int)w.evaluated;
         const bool lost = w.lost || !w.concluded;
         store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
         const int cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const do
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
-  unsigned long long my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0;
+  unsigned int my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0;
   unsigned int my_err = 0;
   unsigned int hkey = 0xffffffffu;   // histogram bucket of this particle (none = all ones)
   if (s < n) {
