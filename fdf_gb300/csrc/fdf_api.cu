@@ -80,6 +80,8 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
   cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
   locator_free(ctx);
+  for (auto &gx : ctx->step_graph)
+    if (gx) cudaGraphExecDestroy(gx);
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->ev_scan) cudaEventDestroy(ctx->ev_scan);
   if (ctx->ev_corner) cudaEventDestroy(ctx->ev_corner);
@@ -172,6 +174,7 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   ctx->sentinel = (unsigned int)Nc;
   ctx->loc.has_params = false;   // a locator is trained for one grid
   ctx->has_grid = true;
+  ctx->gen++;
   ctx->has_ucat = false;
   ctx->swarm_set = false;
   return FDF_SUCCESS;
@@ -198,6 +201,7 @@ int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized) {
   ctx->launches += 1;
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->has_ucat = true;
+  ctx->gen++;
   return FDF_SUCCESS;
 }
 
@@ -206,18 +210,21 @@ int fdf_SetForm(FdfContext *ctx, int form) {
   if (form != FDF_FORM_PLAIN_FP64 && form != FDF_FORM_FP32 && form != FDF_FORM_LEARNED_FP32)
     return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetForm: unknown form");
   ctx->form = form;
+  ctx->gen++;
   return FDF_SUCCESS;
 }
 
 int fdf_SetTimeStep(FdfContext *ctx, double dt) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   ctx->dt = dt;
+  ctx->gen++;
   return FDF_SUCCESS;
 }
 
 int fdf_SetParticleVolume(FdfContext *ctx, double volume) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   ctx->volume = volume;
+  ctx->gen++;
   return FDF_SUCCESS;
 }
 
@@ -240,6 +247,7 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   ctx->staging_bytes = (size_t)cap * 120 + 1024;
   CU(cudaMalloc(&ctx->staging, ctx->staging_bytes));
   ctx->cap = cap;
+  ctx->gen++;
   ctx->swarm_set = false;
   return FDF_SUCCESS;
 }
@@ -282,6 +290,7 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->cur = 0;
   ctx->swarm_set = true;
+  ctx->gen++;
   ctx->swarm_form = ctx->form;
   return FDF_SUCCESS;
 }
@@ -307,6 +316,7 @@ int fdf_SeedParticles(FdfContext *ctx, int64_t n, uint64_t seed, int start_in_ge
   CU(cudaMemcpyAsync(ctx->cnt, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->swarm_set = true;
+  ctx->gen++;
   ctx->swarm_form = ctx->form;
   return FDF_SUCCESS;
 }
@@ -411,6 +421,13 @@ int fdf_GetFaceDeposits(FdfContext *ctx, double *fi, double *fj, double *fk) {
 
 namespace {
 
+// Kernels one pipeline run launches: locate, 3 scan kernels, corner, slots, order, gather,
+// deposit; the learned form adds the flag scan (3), the compaction, the network, the walk
+// from the guess and the fallback walk.
+long long launches_per_step(const FdfContext *ctx) {
+  return 9 + (ctx->swarm_form == FDF_FORM_LEARNED_FP32 ? 7 : 0);
+}
+
 // The shared pipeline of the initial setup (advect=0, drop=0) and a step (1, 1).
 int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no grid: call fdf_SetGrid first");
@@ -453,7 +470,6 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     eg1 = prof ? record_event(ctx, s) : 0;
     launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
                           ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
-    ctx->launches += 3 + 3 + 1;   // guess, walk from the guess, fallback walk, flag scan, compaction
   } else if (f32) {
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
                     ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, nullptr, 0.f, s);
@@ -513,7 +529,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   }
   CHECK_LAUNCH();
   ctx->cur = 1 - ctx->cur;
-  ctx->launches += 9;   // locate, 3 scan kernels, corner, slots, order, gather, deposit
+  ctx->launches += launches_per_step(ctx);
   if (info) {
     DevCounters c{};
     CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
@@ -546,11 +562,43 @@ int fdf_AdvanceStep(FdfContext *ctx, FdfStepInfo *info) {
   return run_pipeline(ctx, 1, 1, info);
 }
 
+// nsteps steps without host round trips.  Unless stage timing is on, each step replays a
+// CUDA graph of the step captured for the current swarm buffer parity (the first step after
+// any change runs eagerly, then the graph is captured from the next one); a launch-bound
+// small swarm then pays one graph launch per step instead of a dozen kernel launches.
 int fdf_AdvanceSteps(FdfContext *ctx, int nsteps) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   for (int q = 0; q < nsteps; ++q) {
-    int r = run_pipeline(ctx, 1, 1, nullptr);
-    if (r) return r;
+    const int parity = ctx->cur;
+    if (ctx->profiling || ctx->eager_gen != ctx->gen) {
+      // eager: stage timing, or the first step after a change (one-time set-up stays out of capture)
+      int r = run_pipeline(ctx, 1, 1, nullptr);
+      if (r) return r;
+      ctx->eager_gen = ctx->gen;
+      continue;
+    }
+    if (ctx->graph_gen[parity] != ctx->gen || !ctx->step_graph[parity]) {
+      CU(cudaSetDevice(ctx->device));
+      if (ctx->step_graph[parity]) { cudaGraphExecDestroy(ctx->step_graph[parity]); ctx->step_graph[parity] = nullptr; }
+      const long long launches0 = ctx->launches;
+      CU(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+      const int r = run_pipeline(ctx, 1, 1, nullptr);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+      ctx->cur = parity;                 // the capture ran nothing: restore the host state
+      ctx->launches = launches0;
+      if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+      if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("step capture: ") + cudaGetErrorString(e));
+      const cudaError_t ei = cudaGraphInstantiate(&ctx->step_graph[parity], graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("step graph: ") + cudaGetErrorString(ei));
+      ctx->graph_gen[parity] = ctx->gen;
+    }
+    CU(cudaGraphLaunch(ctx->step_graph[parity], ctx->stream));
+    ctx->cur = 1 - parity;
+    ctx->out_form = ctx->swarm_form;
+    ctx->out_momentum = ctx->momentum;
+    ctx->launches += launches_per_step(ctx);
   }
   return FDF_SUCCESS;
 }
@@ -609,6 +657,7 @@ int fdf_SetProfiling(FdfContext *ctx, int enable) {
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->profiling = enable != 0;
+  ctx->gen++;
   ctx->ev_used = 0;
   ctx->ev_spans.clear();
   return FDF_SUCCESS;
@@ -628,6 +677,7 @@ int fdf_SetMomentumDeposit(FdfContext *ctx, int enable) {
     CU(cudaMemset(ctx->mom32, 0, 12ull * nf));
   }
   ctx->momentum = enable != 0;
+  ctx->gen++;
   return FDF_SUCCESS;
 }
 

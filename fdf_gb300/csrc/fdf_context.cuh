@@ -74,6 +74,12 @@ struct FdfContext {
   std::string last_error;
   int num_sms = 0;
   LocatorState loc;
+  // fdf_AdvanceSteps replays one captured step per swarm buffer parity; `gen` counts the
+  // changes of anything a captured step bakes in (pointers, kernel arguments, form)
+  long long gen = 1;
+  cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+  long long graph_gen[2] = {0, 0};
+  long long eager_gen = 0;   // generation of the last eager step
 };
 
 

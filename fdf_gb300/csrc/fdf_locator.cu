@@ -420,6 +420,7 @@ int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   if (!(cells >= 0.0)) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorSetMinDistance: cells must be >= 0");
   ctx->loc.far_cells = (float)cells;
+  ctx->gen++;   // a captured step holds the value
   return FDF_SUCCESS;
 }
 

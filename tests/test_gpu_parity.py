@@ -113,6 +113,31 @@ def test_momentum_deposit_parity(ctx):
     ctx.set_momentum_deposit(False)
 
 
+@pytest.mark.parametrize("form", [0, 1])
+def test_graph_steps_match_eager_steps(ctx, form):
+    """fdf_AdvanceSteps replays a captured CUDA graph of the step (per swarm buffer parity):
+    the result is bit-identical to the same steps issued one by one."""
+    wl = W.config1(n=5000, steps=7)
+    outs = []
+    for graph in (False, True):
+        ctx.load_workload(wl, form=form)
+        ctx.initial_setup()
+        if graph:
+            ctx.steps(wl.steps)
+        else:
+            for _ in range(wl.steps):
+                ctx.step(info=False)
+        ctx.synchronize()
+        outs.append((ctx.get_swarm(), ctx.get_faces(), ctx.get_scattered(), ctx.counters()[:2]))
+    (sa, fa, ca, na), (sb, fb, cb, nb) = outs
+    for f in ("position", "velocity", "weight", "P", "cell", "pid", "status"):
+        assert np.array_equal(getattr(sa, f), getattr(sb, f)), f
+    for x, y in zip(fa + ca, fb + cb):
+        assert np.array_equal(x, y)
+    assert na == nb
+    ctx.set_form(0)
+
+
 def test_lost_beyond_max_traversal_and_out_of_bounds(ctx):
     """Corner-start walks that need more than 1000 evaluations are LOST at set-up, kept with
     velocity 0, and removed in step 1; particles pushed out of the domain are removed as
