@@ -241,6 +241,28 @@ FORM_DTYPE = {"plain_fp64": "f64", "fp32": "f32 (positions and walk decisions f6
               "learned_fp32": "f32 (positions and walk decisions f64; bf16 MLP, f32 accumulate)"}
 MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, one inference
 
+# DRAM bytes (read + write) per launch of a stage's kernels, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on this workload at full size, with the
+# units the stage processed then: live particles, or guessed particles for the network and
+# the walk from the guess.
+TRAFFIC = {
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (8.100e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (1.168e9, "guesses", 29.64e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (8.844e9, "guesses", 29.64e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.839e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (8.045e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.838e9, "particles", 63.81e6),
+}
+
+
+def stage_traffic(wl, form: str, stage: str, n_avg: float, guesses: float):
+    """Measured DRAM bytes per launch of the stage, scaled to this run's units, or None."""
+    t = TRAFFIC.get((wl.name, form, stage))
+    if t is None:
+        return None
+    total, unit, units = t
+    return total * ((guesses if unit == "guesses" else n_avg) / units)
+
 _TRAINED = {}   # workload name -> (trained parameters, training report)
 
 
@@ -275,7 +297,7 @@ def prepare(ctx, wl, form, args):
 
 
 def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_step: float, Nc: int, Nn: int,
-                      Nf: int, momentum: bool = False, pending: float = 0.0) -> dict:
+                      Nf: int, momentum: bool = False, pending: float = 0.0, pending_evals: float = 0.0) -> dict:
     """Algorithmic bytes per launch of each stage; the momentum deposit adds the particles'
     velocities and three components per face."""
     if form == "learned_fp32":
@@ -283,8 +305,8 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
         # guess: the pending particles' state and the remaining evaluations
         return {
             "center_to_corner": 24 * nodes_per_step,
-            "advect_locate": 86 * n_avg + 16 * n_avg,
-            "guess_walk": 57 * pending + 176 * max(evals_per_step - n_avg, 0.0),
+            "advect_locate": 86 * n_avg + 16 * n_avg + 176 * max(evals_per_step - n_avg - pending_evals, 0.0),
+            "guess_walk": 57 * pending + 176 * pending_evals,
             "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
             "wait_corner": 0,
             "gather_interpolate": 121 * n_avg + 12 * Nn,
@@ -354,19 +376,23 @@ def time_form(ctx, wl, form, args, dist, local, with_clocks):
     runs = max(stages["sort_by_cell"][1], 1)     # one span per pipeline run
     per = {k: (v[0] / runs) for k, v in stages.items() if v[1] > 0}
     learned = None
-    asked = taken = gev = 0
+    asked = taken = gev = fev = 0
     if form == "learned_fp32":
-        asked, taken, gev = (b - a for a, b in zip(guess0, guess1))
-    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf, momentum_on(wl), asked / K)
+        asked, taken, gev, fev = (b - a for a, b in zip(guess0, guess1))
+    alg = algorithmic_bytes(form, n_avg, evals / K, (nd1 - nd0) / K, Nc, Nn, Nf, momentum_on(wl), asked / K,
+                            (gev + fev) / K)
     if form == "learned_fp32":
         mlp_ms = per.get("learned_guess", 0.0)
         tfl = MLP_FLOPS * asked / K / (mlp_ms / 1000.0) / 1e12 if mlp_ms > 0 else None
         learned = {"guesses_per_step": asked / K, "guess_fraction": asked / max(psteps, 1),
                    "guesses_kept": taken / max(asked, 1), "guess_walk_evals_per_guess": gev / max(asked, 1),
+                   "fallback_evals_per_guess": fev / max(asked, 1),
                    "mlp_tflops": tfl, "mlp_flops_per_particle": MLP_FLOPS,
                    "training": _TRAINED[wl.name][1]}
+    traffic = {k: stage_traffic(wl, form, k, n_avg, asked / K) for k in per}
     return dict(form=form, psteps=psteps, evals=evals, ms=ms_max, launches=launches, clocks=clk, per=per, alg=alg,
-                learned=learned, value=psteps * int(os.environ.get("WORLD_SIZE", "1")) / (ms_max / 1000.0))
+                learned=learned, traffic=traffic,
+                value=psteps * int(os.environ.get("WORLD_SIZE", "1")) / (ms_max / 1000.0))
 
 
 def learned_identity(ctx, wl, args, steps: int) -> dict:
@@ -461,16 +487,21 @@ def run_gpu(args, rank, ws, local, dist):
     per, alg = prim["per"], prim["alg"]
     dom = max((k for k in per if alg.get(k)), key=per.get)
     achieved = alg[dom] / (per[dom] / 1000.0) / 1e9
+    tr = prim["traffic"].get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_launch": alg[dom], "traffic": None,
+                "algorithmic_bytes_per_launch": alg[dom], "traffic": tr,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum at this configuration, "
+                                   "scaled to this run's particles" if tr is not None else None),
+                "dram_gbs": (tr / (per[dom] / 1000.0) / 1e9 if tr is not None else None),
                 "stage_ms_per_step": {k: round(v, 4) for k, v in per.items()},
                 "stage_gbs": {k: round(alg[k] / (per[k] / 1000.0) / 1e9, 1) for k in per if per[k] > 0 and alg.get(k)}}
     lp = prim.get("learned")
     if lp and lp["mlp_tflops"] and per.get("learned_guess", 0.0) > per[dom]:
         # the network inference dominates: its roofline is the tensor one
         tf, tf_kind = bf16_peak()
-        roofline.update({"bound": "tensor", "kernel": "learned_guess (k_mlp_guess)", "achieved": lp["mlp_tflops"],
+        roofline.update({"bound": "tensor", "kernel": "learned_guess (k_mlp_guess_tc)", "achieved": lp["mlp_tflops"],
+                         "traffic": prim["traffic"].get("learned_guess"),
                          "peak": tf, "unit": "TFLOP/s", "frac": lp["mlp_tflops"] / tf,
                          "peak_source": f"{tf_kind} (MEASURED_PEAKS.json bf16_tflops)",
                          "algorithmic_flops_per_launch": MLP_FLOPS * lp["guesses_per_step"],

@@ -65,7 +65,7 @@ _SIGS = {
                                             ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_LocatorPredict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                           ctypes.c_void_p]),
-    "fdf_LocatorGetStats": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p]),
+    "fdf_LocatorGetStats": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p, c_int64_p]),
     "fdf_LocatorSetMinDistance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
 }
 

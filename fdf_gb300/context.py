@@ -310,8 +310,10 @@ class PicContext:
         """Particles at least `cells` cells past their previous cell get a network guess."""
         self._check(self.lib.fdf_LocatorSetMinDistance(self.h, float(cells)))
 
-    def locator_stats(self) -> tuple[int, int, int]:
-        """(particles given a guess, guesses kept, evaluations of the walks from the guesses)."""
-        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
-        self._check(self.lib.fdf_LocatorGetStats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return a.value, b.value, c.value
+    def locator_stats(self) -> tuple[int, int, int, int]:
+        """(particles given a guess, guesses kept, evaluations of the walks from the guesses,
+        evaluations of the reference walks that finished the guesses not kept)."""
+        a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.fdf_LocatorGetStats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                 ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value

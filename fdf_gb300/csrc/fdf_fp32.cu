@@ -509,6 +509,7 @@ __global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDi
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
   LocCounts m;
+  unsigned int fev = 0;
   unsigned int *q = queue[wib];
   for (long long chunk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk * FB_CHUNK < npend;
        chunk += warps) {
@@ -533,6 +534,7 @@ __global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDi
         m.err |= w.err;
         m.done += (unsigned int)w.evaluated;
         m.evals += (unsigned int)w.evaluated;
+        fev += (unsigned int)w.evaluated;
         const bool lost = w.lost || !w.concluded;
         store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
         const int cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
@@ -547,6 +549,7 @@ __global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDi
     __syncwarp();
   }
   block_flush_counts(m, cnt);
+  block_add_u64(fev, &cnt->fallback_evals_total);
 }
 
 // Corner field in FP32: mean of the valid adjacent cells (nodes next to occupied cells).

@@ -57,6 +57,7 @@ struct DevCounters {
   unsigned long long guess_asked_total;   // learned form: particles given a learned start cell
   unsigned long long guess_taken_total;   // ... whose walk from the guess was accepted
   unsigned long long guess_evals_total;   // ... evaluations made by the walks from the guess
+  unsigned long long fallback_evals_total;   // ... by the reference walks of the guesses not taken
 };
 
 struct SwarmBuf {

@@ -424,8 +424,9 @@ int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells) {
   return FDF_SUCCESS;
 }
 
-int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals) {
-  if (!ctx || !asked || !taken || !guess_evals) return FDF_ERR_ARG_NULL;
+int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals,
+                        int64_t *fallback_evals) {
+  if (!ctx || !asked || !taken || !guess_evals || !fallback_evals) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));
   DevCounters c{};
   CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
@@ -433,6 +434,7 @@ int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t
   *asked = (int64_t)c.guess_asked_total;
   *taken = (int64_t)c.guess_taken_total;
   *guess_evals = (int64_t)c.guess_evals_total;
+  *fallback_evals = (int64_t)c.fallback_evals_total;
   return FDF_SUCCESS;
 }
 

@@ -201,8 +201,10 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
  * Default 1.0; 0 asks for every particle that left its cell.  Results do not depend on it. */
 int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells);
 /* Running totals of the learned form: particles given a guess, guesses whose walk was
- * kept, and evaluations made by the walks from the guesses. */
-int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals);
+ * kept, evaluations made by the walks from the guesses, and by the reference walks that
+ * finished the guesses not kept. */
+int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals,
+                        int64_t *fallback_evals);
 
 /* ---- utilities ---- */
 int fdf_Synchronize(FdfContext *ctx);

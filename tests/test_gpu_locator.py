@@ -185,10 +185,10 @@ def test_trained_locator_shortens_walk(pipe_runs):
     e = {k: r[k][4] / ps for k in ("fp32", "learned", "learned_all", "untrained")}
     st = {k: r[k][5] for k in ("learned", "learned_all", "untrained")}
     print("[gain] walk evaluations per particle-step: " + ", ".join(f"{k} {v:.3f}" for k, v in e.items()))
-    for k, (asked, taken, gev) in st.items():
+    for k, (asked, taken, gev, _) in st.items():
         print(f"[gain] {k}: guesses {asked}, kept {taken / max(asked, 1):.3f}, "
               f"evaluations per guess {gev / max(asked, 1):.2f}")
-    asked, taken, _ = st["learned_all"]
+    asked, taken, _, _ = st["learned_all"]
     assert taken > 0.5 * asked
     assert e["learned_all"] < e["untrained"]
     assert st["learned"][0] < st["learned_all"][0]
