@@ -207,6 +207,14 @@ class PicContext:
         self._check(self.lib.fdf_GetFaceDeposits(self.h, _ptr(fi), _ptr(fj), _ptr(fk)))
         return fi, fj, fk
 
+    def write_swarm_field(self, field: str, path: str, int64_indices: bool = True):
+        """WriteSwarmField: the field as a PETSc binary Vec file."""
+        self._check(self.lib.fdf_WriteSwarmField(self.h, field.encode(), path.encode(), 1 if int64_indices else 0))
+
+    def read_swarm_field(self, field: str, path: str, int64_indices: bool = True):
+        """ReadSwarmField: replaces the field from a PETSc binary Vec file of the swarm's length."""
+        self._check(self.lib.fdf_ReadSwarmField(self.h, field.encode(), path.encode(), 1 if int64_indices else 0))
+
     def set_momentum_deposit(self, on: bool = True):
         self._check(self.lib.fdf_SetMomentumDeposit(self.h, 1 if on else 0))
 

@@ -206,6 +206,26 @@ int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells);
 int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals,
                         int64_t *fallback_evals);
 
+/* ---- the reference's on-disk formats (host-side; no GPU work except the swarm transfers) ----
+ * FDFGRID grid file (io.c:101-170 ReadGridFile, grid.c:356-383 AssignGridCoordinates): an
+ * optional "FDFGRID" line, the number of blocks, "IM JM KM" (cells) per block, then one "x y z"
+ * line per node, i fastest, then j, then k.  The first block is read; coor == NULL returns the
+ * sizes only; coor_len counts doubles.  The writer emits one block with 17 significant digits. */
+int fdf_ReadGridFile(const char *path, int64_t *IM, int64_t *JM, int64_t *KM, double *coor, int64_t coor_len);
+int fdf_WriteGridFile(const char *path, int64_t IM, int64_t JM, int64_t KM, const double *coor);
+/* PETSc binary Vec file as VecView writes it on one rank (WriteFieldData, io.c:653-700):
+ * big-endian {VEC_FILE_CLASSID 1211214, N} as PetscInt (8 bytes when int64_indices, as in the
+ * reference's PETSc 3.19.2-64bit build), then N big-endian doubles; bs > 1 also writes
+ * "<path>.info" with "-vecload_block_size <bs>".  values == NULL reads the length only. */
+int fdf_WritePetscVec(const char *path, const double *values, int64_t n, int bs, int int64_indices);
+int fdf_ReadPetscVec(const char *path, double *values, int64_t n_max, int64_t *n, int int64_indices);
+/* A real swarm field ("position", "velocity", "weight", "P") of the context written to, or read
+ * from, such a file: WriteSwarmField (io.c:1023-1070) and ReadSwarmField (io.c:1924-1950) of the
+ * reference, whose files are results/<field><step %05d>_0.dat.  Reading needs a swarm of the
+ * file's length and replaces that field (the particles keep the swarm's current order). */
+int fdf_WriteSwarmField(FdfContext *ctx, const char *field, const char *path, int int64_indices);
+int fdf_ReadSwarmField(FdfContext *ctx, const char *field, const char *path, int int64_indices);
+
 /* ---- utilities ---- */
 int fdf_Synchronize(FdfContext *ctx);
 /* The context's cudaStream_t, for callers that time or order work around it. */
