@@ -160,3 +160,65 @@ def test_fp32_conservation_and_determinism(ctx):
     assert abs(tot - s1.n) <= 1e-4 * s1.n
     assert c1[0].sum() == s1.n
     ctx.set_form(FORM_PLAIN_FP64)
+
+
+def _ksum(vals):
+    """Neumaier-compensated float32 sum in the given order (the deposit kernel's KSum)."""
+    f = np.float32
+    s, c = f(0.0), f(0.0)
+    for v in vals:
+        t = f(s + v)
+        c = f(c + (f(f(s - t) + v) if abs(s) >= abs(v) else f(f(v - t) + s)))
+        s = t
+    return f(s + c)
+
+
+def test_fp32_deposit_matches_host_restatement(ctx):
+    """The FP32 deposit (warp-staged kernel) against the same float32 arithmetic on the host:
+    particles in the swarm's (cell, PID) order, each face summing its lower cell's a V/3 then
+    its own cell's (1 - a) V/3 with Neumaier compensation; count and P average per cell.  Every
+    value must be bit-identical."""
+    wl = W.config_sinusoidal(IM=32, JM=6, KM=12, n=20_000, cfl=1.0, steps=3)   # 33 nodes per row: a warp starts at i = IM
+    ctx.load_workload(wl, form=FORM_FP32)
+    ctx.initial_setup()
+    ctx.steps(wl.steps)
+    s = ctx.get_swarm()
+    fi, fj, fk = ctx.get_faces()
+    cnt, avg = ctx.get_scattered()
+    IM, JM, KM = wl.dims
+    lin = (s.cell[:, 2] * JM + s.cell[:, 1]) * IM + s.cell[:, 0]
+    assert np.all(np.diff(lin) >= 0), "the swarm is held in cell order"
+    seg = {}
+    for c in np.unique(lin):
+        idx = np.nonzero(lin == c)[0]
+        seg[int(c)] = idx
+    a = s.weight.astype(np.float32)
+    P = s.P.astype(np.float32)
+    third = np.float32(wl.volume / 3.0)
+    cid = lambda i, j, k: (k * JM + j) * IM + i
+    empty = np.zeros(0, dtype=np.int64)
+
+    def face(d, lower, upper):
+        vals = [np.float32(a[p, d] * third) for p in (seg.get(lower, empty) if lower is not None else empty)]
+        vals += [np.float32(np.float32(1.0 - a[p, d]) * third) for p in (seg.get(upper, empty) if upper is not None else empty)]
+        return _ksum(vals)
+
+    for k in range(KM):
+        for j in range(JM):
+            for i in range(IM + 1):
+                want = face(0, cid(i - 1, j, k) if i > 0 else None, cid(i, j, k) if i < IM else None)
+                assert np.float32(fi[k, j, i]) == want, ("fi", i, j, k)
+    for k in range(KM):
+        for j in range(JM + 1):
+            for i in range(IM):
+                want = face(1, cid(i, j - 1, k) if j > 0 else None, cid(i, j, k) if j < JM else None)
+                assert np.float32(fj[k, j, i]) == want, ("fj", i, j, k)
+    for k in range(KM + 1):
+        for j in range(JM):
+            for i in range(IM):
+                want = face(2, cid(i, j, k - 1) if k > 0 else None, cid(i, j, k) if k < KM else None)
+                assert np.float32(fk[k, j, i]) == want, ("fk", i, j, k)
+    for c, idx in seg.items():
+        i, j, k = c % IM, (c // IM) % JM, c // (IM * JM)
+        assert cnt[k, j, i] == len(idx)
+        assert np.float32(avg[k, j, i]) == np.float32(_ksum([P[p] for p in idx]) / np.float32(len(idx)))
