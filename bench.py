@@ -149,6 +149,27 @@ def bf16_peak():
         return 1900.0, "fallback"
 
 
+def host_link_gbs(device: int) -> dict:
+    """Raw copy rate between pinned host memory and the GPU (1 GiB each way, best of 3)."""
+    import torch
+    n = 1 << 27
+    x = torch.empty(n, dtype=torch.float64, device=f"cuda:{device}")
+    hbuf = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    best = {"h2d": 0.0, "d2h": 0.0}
+    for _ in range(3):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        x.copy_(hbuf, non_blocking=True)
+        torch.cuda.synchronize()
+        b = time.perf_counter()
+        hbuf.copy_(x, non_blocking=True)
+        torch.cuda.synchronize()
+        c = time.perf_counter()
+        best["h2d"] = max(best["h2d"], 8 * n / (b - a) / 1e9)
+        best["d2h"] = max(best["d2h"], 8 * n / (c - b) / 1e9)
+    return {k: round(v, 1) for k, v in best.items()}
+
+
 def pinned_like(a: np.ndarray) -> np.ndarray:
     try:
         import torch
@@ -543,25 +564,37 @@ def run_gpu(args, rank, ws, local, dist):
         t0 = time.perf_counter()
         ps = 0
         n_cur = n0
+        split = {"set_swarm": 0.0, "step": 0.0, "get_swarm": 0.0, "get_fields": 0.0}
         for _ in range(k_e2e):
+            ta = time.perf_counter()
             ctx._check(lib.fdf_SetSwarm(h, n_cur, _ptr(bufs.position), _ptr(bufs.velocity), _ptr(bufs.weight),
                                         _ptr(bufs.P), _ptr(bufs.cell), _ptr(bufs.pid), _ptr(bufs.status)))
+            tb = time.perf_counter()
             ctx._check(lib.fdf_AdvanceStep(h, None))
+            ctx._check(lib.fdf_Synchronize(h))
+            tc = time.perf_counter()
             ctx._check(lib.fdf_GetSwarm(h, n0, ctypes.byref(got), _ptr(bufs.position), _ptr(bufs.velocity),
                                         _ptr(bufs.weight), _ptr(bufs.P), _ptr(bufs.cell), _ptr(bufs.pid),
                                         _ptr(bufs.status)))
+            td = time.perf_counter()
             ctx._check(lib.fdf_GetScatteredFields(h, _ptr(count), _ptr(avg)))
             ctx._check(lib.fdf_GetFaceDeposits(h, _ptr(fi), _ptr(fj), _ptr(fk)))
             if mom is not None:
                 ctx._check(lib.fdf_GetFaceMomentum(h, _ptr(mom[0]), _ptr(mom[1]), _ptr(mom[2])))
+            te = time.perf_counter()
+            for key, v in zip(split, (tb - ta, tc - tb, td - tc, te - td)):
+                split[key] += v
             ps += n_cur
             n_cur = got.value
         el = reduce_max(dist, time.perf_counter() - t0)
+        link = host_link_gbs(local)
         e2e = {"value": ps * ws / el, "unit": UNIT, "h2d_bytes_per_step": int(120 * n0),
                "d2h_bytes_per_step": int(120 * n0 + 16 * Nn + 8 * Nf + (24 * Nf if mom is not None else 0)),
                "steps": k_e2e,
                "path": "fdf_SetSwarm + fdf_AdvanceStep + fdf_GetSwarm/GetScatteredFields/GetFaceDeposits, "
-                       "pinned host DMSwarm-layout arrays"}
+                       "pinned host DMSwarm-layout arrays",
+               "ms_per_step": {k: round(1000.0 * v / k_e2e, 2) for k, v in split.items()},
+               "host_link_gbs": link}
 
     accuracy = None
     if rank == 0 and ws == 1 and args.accuracy_steps > 0 and ("fp32" in forms or "learned_fp32" in forms):
