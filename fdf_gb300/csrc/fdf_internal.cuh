@@ -34,7 +34,7 @@ enum { ST_NEEDS_LOCATION = 0, ST_ACTIVE_AND_LOCATED = 1, ST_MIGRATING_OUT = 2, S
        ST_UNINITIALIZED = 4 };
 
 // Device error word bits.
-enum { ERRBIT_DEGENERATE = 1u, ERRBIT_BAD_CELL = 2u, ERRBIT_TC_TIMEOUT = 4u };
+enum { ERRBIT_DEGENERATE = 1u, ERRBIT_TC_TIMEOUT = 4u };
 
 // Counters kept on the device so that a step needs no host round trip.
 struct DevCounters {
