@@ -486,6 +486,43 @@ def fp32_accuracy(ctx, wl, steps: int, nthreads: int) -> dict:
             "P_avg_rel": stats(np.abs(gavg[occupied] - sim.avg[occupied]) / np.abs(sim.avg[occupied]))}
 
 
+def time_contra2cart(ctx, wl, calls: int) -> dict:
+    """Contra2Cart (setup.c:1294-1420) on the workload's grid: the face fluxes of a uniform
+    flow are uploaded once, the first call builds the metric table (timed on the host), then
+    `calls` calls are timed with CUDA events on the context stream.  Inputs (face velocity,
+    table) are larger than L2."""
+    from fdf_gb300.workloads import uniform_flow_fluxes
+    IM, JM, KM = wl.dims
+    Nc, Nn = IM * JM * KM, (IM + 1) * (JM + 1) * (KM + 1)
+    n_int = (IM - 1) * (JM - 1) * (KM - 1)
+    ctx.set_grid(wl.coor)
+    ctx.set_ucat(wl.ucat)
+    csi, eta, zet, _, flipped = ctx.grid_metrics()
+    u = np.array([0.3, -0.2, 1.1])
+    ctx.set_ucont(uniform_flow_fluxes(u, csi, eta, zet))
+    del csi, eta, zet
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    ctx.contra2cart()
+    ctx.synchronize()
+    table_ms = 1000.0 * (time.perf_counter() - t0)
+    ctx.set_profiling(True)
+    for _ in range(calls):
+        ctx.contra2cart()
+    ms_total, runs = ctx.stage_times()["contra2cart"]
+    ctx.set_profiling(False)
+    ms = ms_total / max(runs, 1)
+    err = float(np.abs(ctx.get_ucat(node_sized=False)[1:, 1:, 1:] - u).max())
+    alg = 116 * n_int + 24 * Nn        # table 80 + ucat 24 + ucat32 12 per interior cell, face velocity per node
+    hbm, peak_kind = peaks()
+    gbs = alg / (ms / 1000.0) / 1e9
+    return {"ms_per_call": ms, "calls": runs, "table_build_ms": table_ms, "interior_cells": n_int,
+            "algorithmic_bytes_per_call": alg, "achieved_gbs": gbs, "hbm_frac": gbs / hbm,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "fp64_ops_per_cell": 24, "fp64_gflops": 24 * n_int / (ms / 1000.0) / 1e9,
+            "uniform_flow_max_abs_error": err, "grid_flipped": flipped}
+
+
 def run_gpu(args, rank, ws, local, dist):
     from fdf_gb300.context import PicContext, SwarmArrays
     import torch
@@ -608,6 +645,10 @@ def run_gpu(args, rank, ws, local, dist):
         v, st, el, sample = time_oracle(wl, budget_s=float(args.cpu_seconds), max_steps=1000, nthreads=nthreads)
         cpu = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample}
 
+    c2c = None
+    if rank == 0 and not args.no_contra2cart:
+        c2c = time_contra2cart(ctx, wl, max(args.steps, 5))
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -624,7 +665,7 @@ def run_gpu(args, rank, ws, local, dist):
                            "deposits": "face volume" + (" and momentum" if momentum_on(wl) else "")},
                 "roofline": roofline, "forms": form_lines, "fp32_accuracy_vs_fp64_oracle": accuracy,
                 "learned_vs_fp32_form": identity,
-                "cpu_baseline": cpu, "e2e": e2e,
+                "cpu_baseline": cpu, "e2e": e2e, "contra2cart": c2c,
                 "gpu_launches": launches, "clocks": clk}
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -650,6 +691,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-contra2cart", action="store_true",
+                    help="skip timing the Eulerian input (Contra2Cart on the workload's grid)")
     ap.add_argument("--accuracy-steps", type=int, default=10,
                     help="steps of the FP32-form vs FP64-oracle comparison on the full workload (0 = skip)")
     args = ap.parse_args()

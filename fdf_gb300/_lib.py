@@ -27,6 +27,10 @@ _SIGS = {
     "fdf_ContextDestroy": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_SetGrid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]),
     "fdf_SetUcat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "fdf_GetUcat": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "fdf_GetGridMetrics": (ctypes.c_int, [ctypes.c_void_p] * 6),
+    "fdf_SetUcont": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_Contra2Cart": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTimeStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_SetParticleVolume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),

@@ -19,6 +19,7 @@ from ._lib import FdfStepInfo
 
 ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG", 63: "PETSC_ERR_ARG_OUTOFRANGE",
              73: "PETSC_ERR_ARG_WRONGSTATE", 76: "PETSC_ERR_LIB", 83: "PETSC_ERR_USER", 85: "PETSC_ERR_ARG_NULL",
+             90: "PETSC_ERR_FLOP_COUNT",
              97: "PETSC_ERR_GPU"}
 NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
 FORM_PLAIN_FP64, FORM_FP32, FORM_LEARNED_FP32 = 0, 1, 2
@@ -131,6 +132,38 @@ class PicContext:
         else:
             raise ValueError(f"ucat shape {ucat.shape} matches neither the cell nor the node layout")
         self._check(self.lib.fdf_SetUcat(self.h, _ptr(ucat), node_sized))
+
+    def get_ucat(self, node_sized: bool = True) -> np.ndarray:
+        """The context's cell-centred ucat, node-sized [KM+1][JM+1][IM+1][3] (or [KM][JM][IM][3])."""
+        IM, JM, KM = self.dims
+        shp = (KM + 1, JM + 1, IM + 1, 3) if node_sized else (KM, JM, IM, 3)
+        out = np.empty(shp)
+        self._check(self.lib.fdf_GetUcat(self.h, _ptr(out), 1 if node_sized else 0))
+        return out
+
+    # -- Eulerian input: face velocity -> ucat (Contra2Cart, setup.c:1294-1420)
+    def grid_metrics(self):
+        """(csi, eta, zet, aj, flipped) of the grid after the orientation check (Metric.c)."""
+        IM, JM, KM = self.dims
+        shp = (KM + 1, JM + 1, IM + 1)
+        csi, eta, zet = (np.empty(shp + (3,)) for _ in range(3))
+        aj = np.empty(shp)
+        fl = ctypes.c_int(0)
+        self._check(self.lib.fdf_GetGridMetrics(self.h, _ptr(csi), _ptr(eta), _ptr(zet), _ptr(aj),
+                                                ctypes.byref(fl)))
+        return csi, eta, zet, aj, bool(fl.value)
+
+    def set_ucont(self, ucont: np.ndarray):
+        """Contravariant face velocity, node-sized [KM+1][JM+1][IM+1][3] (the reference's lUcont)."""
+        ucont = np.ascontiguousarray(ucont, dtype=np.float64)
+        IM, JM, KM = self.dims
+        if ucont.shape != (KM + 1, JM + 1, IM + 1, 3):
+            raise ValueError(f"ucont shape {ucont.shape} is not the node-sized [KM+1][JM+1][IM+1][3]")
+        self._check(self.lib.fdf_SetUcont(self.h, _ptr(ucont)))
+
+    def contra2cart(self):
+        """ucat of the interior cells from the face velocity, on the device (stream-ordered)."""
+        self._check(self.lib.fdf_Contra2Cart(self.h))
 
     def set_form(self, form: int):
         """FORM_PLAIN_FP64 (bit-exact), FORM_FP32 (precision form) or FORM_LEARNED_FP32 (precision
@@ -253,7 +286,7 @@ class PicContext:
         return int(self.lib.fdf_GetLaunchCount(self.h))
 
     STAGES = ("center_to_corner", "advect_locate", "sort_by_cell", "wait_corner", "gather_interpolate",
-              "deposit", "learned_guess", "guess_walk")
+              "deposit", "learned_guess", "guess_walk", "contra2cart")
 
     def counters(self) -> tuple[int, int, int]:
         """(particle-steps advanced, walk evaluations made, corner nodes computed) since the swarm was set."""

@@ -23,21 +23,6 @@ namespace {
 constexpr long long FDF_MAX_PARTICLES = 512LL * 1024 * 1024;
 
 
-// Stage ids reported by fdf_GetStageTimes.
-enum { STAGE_CORNER = 0, STAGE_LOCATE = 1, STAGE_SORT = 2, STAGE_WAIT = 3, STAGE_GATHER_INTERP = 4,
-       STAGE_DEPOSIT = 5, STAGE_GUESS = 6, STAGE_GUESS_WALK = 7, NUM_STAGES = 8 };
-
-size_t record_event(FdfContext *ctx, cudaStream_t stream) {
-  if (ctx->ev_used == ctx->ev_pool.size()) {
-    cudaEvent_t e;
-    if (cudaEventCreate(&e) != cudaSuccess) return (size_t)-1;
-    ctx->ev_pool.push_back(e);
-  }
-  size_t id = ctx->ev_used++;
-  cudaEventRecord(ctx->ev_pool[id], stream);
-  return id;
-}
-
 }  // namespace
 
 extern "C" {
@@ -76,6 +61,7 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk);
   cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
   cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox); cfree(ctx->mom); cfree(ctx->mom32);
+  eulerian_free(ctx);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
   cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
   cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
@@ -106,6 +92,7 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   cfree(ctx->cursor); cfree(ctx->scan_sums);
   cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
   cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->mom); cfree(ctx->mom32);
+  eulerian_free(ctx);
   ctx->momentum = false;
   GridDims g{};
   g.IM = (int)IM; g.JM = (int)JM; g.KM = (int)KM; g.Nc = Nc; g.Nn = Nn;
@@ -514,18 +501,18 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   ctx->out_form = ctx->swarm_form;
   size_t e5 = prof ? record_event(ctx, s) : 0;
   if (prof && learned) {
-    ctx->ev_spans.push_back({STAGE_LOCATE, {e0, eg0}});
-    ctx->ev_spans.push_back({STAGE_GUESS, {eg0, eg1}});
-    ctx->ev_spans.push_back({STAGE_GUESS_WALK, {eg1, e1}});
+    ctx->ev_spans.push_back({FDF_STAGE_LOCATE, {e0, eg0}});
+    ctx->ev_spans.push_back({FDF_STAGE_GUESS, {eg0, eg1}});
+    ctx->ev_spans.push_back({FDF_STAGE_GUESS_WALK, {eg1, e1}});
   } else if (prof) {
-    ctx->ev_spans.push_back({STAGE_LOCATE, {e0, e1}});
+    ctx->ev_spans.push_back({FDF_STAGE_LOCATE, {e0, e1}});
   }
   if (prof) {
-    ctx->ev_spans.push_back({STAGE_SORT, {e1, e2}});
-    ctx->ev_spans.push_back({STAGE_CORNER, {c0, c1}});
-    ctx->ev_spans.push_back({STAGE_WAIT, {e2, e3}});
-    ctx->ev_spans.push_back({STAGE_GATHER_INTERP, {e3, e4}});
-    ctx->ev_spans.push_back({STAGE_DEPOSIT, {e4, e5}});
+    ctx->ev_spans.push_back({FDF_STAGE_SORT, {e1, e2}});
+    ctx->ev_spans.push_back({FDF_STAGE_CORNER, {c0, c1}});
+    ctx->ev_spans.push_back({FDF_STAGE_WAIT, {e2, e3}});
+    ctx->ev_spans.push_back({FDF_STAGE_GATHER_INTERP, {e3, e4}});
+    ctx->ev_spans.push_back({FDF_STAGE_DEPOSIT, {e4, e5}});
   }
   CHECK_LAUNCH();
   ctx->cur = 1 - ctx->cur;

@@ -74,6 +74,12 @@ struct FdfContext {
   std::string last_error;
   int num_sms = 0;
   LocatorState loc;
+  // Eulerian input (fdf_eulerian.cu): face velocity and the per-cell Contra2Cart table
+  double *ucont = nullptr;       // [Nn][3] node-sized, as the reference's lUcont
+  double *c2c_table = nullptr;   // [10][Nc], built on the first fdf_Contra2Cart of a grid
+  int c2c_rc = FDF_SUCCESS;      // the table build's error (a near-zero determinant)
+  std::string c2c_msg;
+  int c2c_flipped = 0;
   // fdf_AdvanceSteps replays one captured step per swarm buffer parity; `gen` counts the
   // changes of anything a captured step bakes in (pointers, kernel arguments, form)
   long long gen = 1;
@@ -85,6 +91,26 @@ struct FdfContext {
 
 // forms whose swarm is held in the precision-form arrays
 inline bool form_is32(int form) { return form == FDF_FORM_FP32 || form == FDF_FORM_LEARNED_FP32; }
+
+// Stage ids reported by fdf_GetStageTimes.
+enum { FDF_STAGE_CORNER = 0, FDF_STAGE_LOCATE = 1, FDF_STAGE_SORT = 2, FDF_STAGE_WAIT = 3,
+       FDF_STAGE_GATHER_INTERP = 4, FDF_STAGE_DEPOSIT = 5, FDF_STAGE_GUESS = 6, FDF_STAGE_GUESS_WALK = 7,
+       FDF_STAGE_CONTRA2CART = 8, FDF_NUM_STAGES = 9 };
+
+// Records a pooled timing event on `stream`; returns its index in ctx->ev_pool.
+inline size_t record_event(FdfContext *ctx, cudaStream_t stream) {
+  if (ctx->ev_used == ctx->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return (size_t)-1;
+    ctx->ev_pool.push_back(e);
+  }
+  size_t id = ctx->ev_used++;
+  cudaEventRecord(ctx->ev_pool[id], stream);
+  return id;
+}
+
+// Frees the Eulerian-input buffers (face velocity, Contra2Cart table) of the context's grid.
+void eulerian_free(FdfContext *ctx);
 
 inline int fail(FdfContext *ctx, int code, const std::string &msg) {
   if (ctx) ctx->last_error = msg;

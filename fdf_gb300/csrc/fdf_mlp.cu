@@ -235,10 +235,10 @@ __global__ void k_make_samples(const double *__restrict__ x, const double *__res
 __global__ void k_pack_bias(const float *__restrict__ params, float *__restrict__ bias) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= MLP_BIAS_WORDS) return;
-  float v = 0.f;
-  if (q < 128) v = params[MLP_OFF_B1 + q];
-  else if (q < 256) v = params[MLP_OFF_B2 + q - 128];
-  else if (q < 384) v = params[MLP_OFF_B3 + q - 256];
+  float v = 0.f;   // hidden layers: b/2 (the epilogue works on z/2); output layer: b
+  if (q < 128) v = 0.5f * params[MLP_OFF_B1 + q];
+  else if (q < 256) v = 0.5f * params[MLP_OFF_B2 + q - 128];
+  else if (q < 384) v = 0.5f * params[MLP_OFF_B3 + q - 256];
   else if (q < 387) v = params[MLP_OFF_B4 + q - 384];
   bias[q] = v;
 }

@@ -19,7 +19,7 @@
 #define MLP_OFF_B4 33920
 #define MLP_NPARAM 33923
 
-#define MLP_BIAS_WORDS 392      // b1 | b2 | b3 | b4 (387 used)
+#define MLP_BIAS_WORDS 392      // b1/2 | b2/2 | b3/2 | b4 (387 used; hidden biases halved for the SiLU epilogue)
 
 // Input normalisation xhat = (x - centre) * inv_half, in FP32.
 struct MlpNorm {

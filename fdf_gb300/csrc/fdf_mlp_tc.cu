@@ -111,10 +111,13 @@ __device__ __forceinline__ unsigned pack2(float lo, float hi) {
   return *reinterpret_cast<unsigned *>(&v);
 }
 
-__device__ __forceinline__ float silu_fast(float x) {
+// SiLU(z) = z * sigmoid(z) = h + h * tanh(h) with h = z / 2; takes the accumulator v and the
+// half-bias hb, so that h = v/2 + hb is one FMA (scaling by 1/2 is exact).
+__device__ __forceinline__ float silu_half(float v, float hb) {
+  const float h = fmaf(v, 0.5f, hb);
   float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * x));
-  return x * fmaf(0.5f, t, 0.5f);
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
 }
 
 // byte offset of element (r, k) in the operand layout with SBO = sbo
@@ -219,7 +222,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     fence_after_sync();
     return !bad;
   };
-  // bias + SiLU of the 128 accumulator columns, stored as the next layer's A operand
+  // bias + SiLU of the 128 accumulator columns (b: half-biases), stored as the next layer's A operand
   auto epilogue = [&](const float *b) {
 #pragma unroll 1
     for (int c = 0; c < 8; ++c) {
@@ -228,7 +231,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       unsigned w[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        w[q] = pack2(silu_fast(v[2 * q] + b[16 * c + 2 * q]), silu_fast(v[2 * q + 1] + b[16 * c + 2 * q + 1]));
+        w[q] = pack2(silu_half(v[2 * q], b[16 * c + 2 * q]), silu_half(v[2 * q + 1], b[16 * c + 2 * q + 1]));
       *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
       *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
     }

@@ -123,6 +123,17 @@ def _make_right_handed(g: np.ndarray) -> np.ndarray:
     return g
 
 
+def uniform_flow_fluxes(u, csi: np.ndarray, eta: np.ndarray, zet: np.ndarray) -> np.ndarray:
+    """Contravariant face velocity (the reference's ucont layout, node-sized [..][3]) of the
+    constant velocity u through the face metric vectors: (csi . u, eta . u, zet . u)."""
+    u = np.asarray(u, dtype=np.float64)
+    out = np.empty(csi.shape)
+    out[..., 0] = csi[..., 0] * u[0] + csi[..., 1] * u[1] + csi[..., 2] * u[2]
+    out[..., 1] = eta[..., 0] * u[0] + eta[..., 1] * u[1] + eta[..., 2] * u[2]
+    out[..., 2] = zet[..., 0] * u[0] + zet[..., 1] * u[1] + zet[..., 2] * u[2]
+    return out
+
+
 def cell_centroids(coor: np.ndarray) -> np.ndarray:
     c = (coor[:-1, :-1, :-1] + coor[:-1, :-1, 1:] + coor[:-1, 1:, :-1] + coor[:-1, 1:, 1:]
          + coor[1:, :-1, :-1] + coor[1:, :-1, 1:] + coor[1:, 1:, :-1] + coor[1:, 1:, 1:])

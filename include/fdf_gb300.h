@@ -36,6 +36,7 @@ extern "C" {
 #define FDF_ERR_ARG_WRONGSTATE 73
 #define FDF_ERR_LIB 76
 #define FDF_ERR_USER 83          /* degenerate cell face met by the walk (walkingsearch.c:147-155) */
+#define FDF_ERR_FLOP_COUNT 90    /* near-zero Jacobian or Contra2Cart determinant (Metric.c:560, setup.c:1389) */
 #define FDF_ERR_ARG_NULL 85
 #define FDF_ERR_GPU 97
 
@@ -90,6 +91,31 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
 /* Cell-centred Cartesian velocity.  node_sized=1: the reference's DMDA layout
  * [KM+1][JM+1][IM+1][3] with cell (i,j,k) at [k][j][i]; node_sized=0: [KM][JM][IM][3]. */
 int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized);
+/* Reads the context's cell-centred ucat back, in either layout of fdf_SetUcat (node_sized=1:
+ * the extra i=IM, j=JM, k=KM entries are zero). */
+int fdf_GetUcat(FdfContext *ctx, double *ucat, int node_sized);
+
+/* ---- Eulerian input: contravariant face velocity -> ucat, on the device ---- */
+/* Face metrics Csi, Eta, Zet (ComputeFaceMetrics, Metric.c:286-460) and Aj = 1/J
+ * (ComputeCellCenteredJacobianInverse, Metric.c:491-600) of the grid, after the orientation
+ * check (CheckAndFixGridOrientation, Metric.c:195-260), node-sized [KM+1][JM+1][IM+1][3]
+ * (aj: [KM+1][JM+1][IM+1]); any output may be NULL.  *flipped = 1 when every Aj was negative
+ * and all four were negated (the reference's GridOrientation is +1 afterwards either way).
+ * Errors: FDF_ERR_FLOP_COUNT (|J| < 1e-12 at a node), FDF_ERR_USER (Aj of mixed signs). */
+int fdf_GetGridMetrics(FdfContext *ctx, double *csi, double *eta, double *zet, double *aj, int *flipped);
+/* Contravariant face velocity, the reference's lUcont: node-sized [KM+1][JM+1][IM+1][3] with
+ * .x the flux through i-face i, .y through j-face j, .z through k-face k at node (i,j,k). */
+int fdf_SetUcont(FdfContext *ctx, const double *ucont);
+/* Contra2Cart(UserCtx*) (setup.c:1294-1420): ucat of the cells i in 1..IM-1, j in 1..JM-1,
+ * k in 1..KM-1 (the reference's interior loop on one rank) from the face velocity and the
+ * orientation-fixed metrics, bit-identical to the reference; the other cells keep their
+ * ucat (the reference leaves them to its boundary conditions).  The metrics and the grid-only
+ * part of Cramer's rule are built on the first call for a grid.  Stream-ordered: the next
+ * step, fdf_GetUcat and fdf_Synchronize see the result.  Errors: FDF_ERR_ARG_WRONGSTATE
+ * without fdf_SetUcont, the errors of fdf_GetGridMetrics, FDF_ERR_FLOP_COUNT (a cell's
+ * |det| < 1e-18; ucat is then left unchanged). */
+int fdf_Contra2Cart(FdfContext *ctx);
+
 /* Selects the form used by the next fdf_SetSwarm (default PLAIN_FP64). */
 int fdf_SetForm(FdfContext *ctx, int form);
 int fdf_SetTimeStep(FdfContext *ctx, double dt);                 /* user->dt            */
@@ -237,7 +263,8 @@ int64_t fdf_GetLaunchCount(FdfContext *ctx);
  * Stages: 0 center->corner (on a second stream, concurrent with 2), 1 advect+locate,
  * 2 sort by cell (histogram scan, slots, per-cell PID order), 3 wait for stage 0,
  * 4 gather+interpolate, 5 deposits; learned form: 6 network inference, 7 walk from the
- * guess (its stage 1 is the first evaluation and the pending list).  ms_total[s] sums the
+ * guess (its stage 1 is the first evaluation and the pending list); 8 fdf_Contra2Cart
+ * (outside the steps, one span per call).  ms_total[s] sums the
  * stage over all pipeline runs since enabling; launches[s] counts the timed spans. */
 int fdf_SetProfiling(FdfContext *ctx, int enable);
 /* Running totals since fdf_SetSwarm: particles advanced (sum over steps of the live

@@ -31,6 +31,7 @@ NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2
 LEFT, RIGHT, BOTTOM, TOP, FRONT, BACK = 0, 1, 2, 3, 4, 5
 ERR_USER = 83
 ERR_ARG_NULL = 85
+ERR_FLOP_COUNT = 90
 
 
 def build(force: bool = False) -> str:
@@ -111,6 +112,11 @@ def lib():
                                     D, D, ctypes.c_int, ctypes.POINTER(OStepInfo)]
         L.o_InitialSetup.argtypes = [ctypes.POINTER(OGrid), D, D, ctypes.POINTER(OSwarm), D, D, ctypes.c_int,
                                      ctypes.POINTER(OStepInfo)]
+        L.o_ComputeFaceMetrics.argtypes = [ctypes.POINTER(OGrid), D, D, D]
+        L.o_ComputeFaceMetrics.restype = None
+        L.o_ComputeCellCenteredJacobianInverse.argtypes = [ctypes.POINTER(OGrid), D]
+        L.o_CheckAndFixGridOrientation.argtypes = [ctypes.POINTER(OGrid), D, D, D, D, ctypes.POINTER(ctypes.c_int)]
+        L.o_Contra2Cart.argtypes = [ctypes.POINTER(OGrid), D, D, D, D, D]
         _lib = L
     return _lib
 
@@ -313,3 +319,42 @@ class Simulation:
         if err:
             raise RuntimeError(f"oracle step failed with PETSc error {err}")
         return info
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: PETSc error {code}")
+        self.code = code
+
+
+def grid_metrics(g: Grid):
+    """Metric.c:286-460, 491-600 and 195-260 in the reference's order (face metrics, Jacobian
+    inverse, orientation check).  Returns (csi, eta, zet, aj, flipped); csi/eta/zet are
+    node-sized [KM+1][JM+1][IM+1][3], aj [KM+1][JM+1][IM+1].  Raises OracleError with the
+    PETSc code on a near-zero Jacobian (90) or a grid of mixed orientation (83)."""
+    L = lib()
+    shp = g.node_shape
+    csi, eta, zet = (np.zeros(shp + (3,)) for _ in range(3))
+    aj = np.zeros(shp)
+    L.o_ComputeFaceMetrics(ctypes.byref(g.c), _dp(csi), _dp(eta), _dp(zet))
+    rc = L.o_ComputeCellCenteredJacobianInverse(ctypes.byref(g.c), _dp(aj))
+    if rc:
+        raise OracleError(rc, "ComputeCellCenteredJacobianInverse")
+    flipped = ctypes.c_int(0)
+    rc = L.o_CheckAndFixGridOrientation(ctypes.byref(g.c), _dp(csi), _dp(eta), _dp(zet), _dp(aj),
+                                        ctypes.byref(flipped))
+    if rc:
+        raise OracleError(rc, "CheckAndFixGridOrientation")
+    return csi, eta, zet, aj, bool(flipped.value)
+
+
+def contra2cart(g: Grid, ucont: np.ndarray, csi, eta, zet, ucat: np.ndarray | None = None) -> np.ndarray:
+    """setup.c:1294-1420: node-sized ucat of the interior cells from ucont (node-sized [..][3]);
+    entries of `ucat` (zeros when None) outside the interior cells are left as given."""
+    L = lib()
+    ucont = np.ascontiguousarray(ucont, dtype=np.float64)
+    out = np.zeros(g.node_shape + (3,)) if ucat is None else np.array(ucat, dtype=np.float64, copy=True)
+    rc = L.o_Contra2Cart(ctypes.byref(g.c), _dp(ucont), _dp(csi), _dp(eta), _dp(zet), _dp(out))
+    if rc:
+        raise OracleError(rc, "Contra2Cart")
+    return out

@@ -519,3 +519,196 @@ int o_InitialSetup(const OGrid *g, const double *ucat, double *corner, OSwarm *s
   if (info) *info = loc;
   return 0;
 }
+
+/* ======================================================================== */
+/* The Eulerian input of the path: face metrics, the Jacobian, Contra2Cart.  */
+/* ======================================================================== */
+
+static inline int64_t o_nidx(const OGrid *g, int64_t i, int64_t j, int64_t k) {
+  return (k * (g->JM + 1) + j) * (g->IM + 1) + i;
+}
+
+/* copy one node's 3-vector */
+static inline void o_cp3(double *a, int64_t dst, int64_t src) {
+  a[3 * dst] = a[3 * src]; a[3 * dst + 1] = a[3 * src + 1]; a[3 * dst + 2] = a[3 * src + 2];
+}
+
+/* Metric.c:286-460.  One rank owns every node: xs = ys = zs = 0, xe = mx, ye = my, ze = mz. */
+void o_ComputeFaceMetrics(const OGrid *g, double *csi, double *eta, double *zet) {
+  const int64_t mx = g->IM + 1, my = g->JM + 1, mz = g->KM + 1, nn = mx * my * mz;
+  memset(csi, 0, (size_t)(3 * nn) * sizeof(double));
+  memset(eta, 0, (size_t)(3 * nn) * sizeof(double));
+  memset(zet, 0, (size_t)(3 * nn) * sizeof(double));
+#define P_(c, ii, jj, kk) (node_at(g, (ii), (jj), (kk))[c])
+  for (int64_t k = 1; k < mz; ++k)            /* Csi :325-341 */
+    for (int64_t j = 1; j < my; ++j)
+      for (int64_t i = 0; i < mx; ++i) {
+        double de[3], dz[3];
+        for (int c = 0; c < 3; ++c) {
+          de[c] = 0.5 * (P_(c, i, j, k) + P_(c, i, j, k - 1) - P_(c, i, j - 1, k) - P_(c, i, j - 1, k - 1));
+          dz[c] = 0.5 * (P_(c, i, j - 1, k) + P_(c, i, j, k) - P_(c, i, j - 1, k - 1) - P_(c, i, j, k - 1));
+        }
+        double *o = csi + 3 * o_nidx(g, i, j, k);
+        o[0] = de[1] * dz[2] - de[2] * dz[1];
+        o[1] = de[2] * dz[0] - de[0] * dz[2];
+        o[2] = de[0] * dz[1] - de[1] * dz[0];
+      }
+  for (int64_t k = 1; k < mz; ++k)            /* Eta :344-360 */
+    for (int64_t j = 0; j < my; ++j)
+      for (int64_t i = 1; i < mx; ++i) {
+        double dx[3], dz[3];
+        for (int c = 0; c < 3; ++c) {
+          dx[c] = 0.5 * (P_(c, i, j, k) + P_(c, i, j, k - 1) - P_(c, i - 1, j, k) - P_(c, i - 1, j, k - 1));
+          dz[c] = 0.5 * (P_(c, i, j, k) + P_(c, i - 1, j, k) - P_(c, i, j, k - 1) - P_(c, i - 1, j, k - 1));
+        }
+        double *o = eta + 3 * o_nidx(g, i, j, k);
+        o[0] = dz[1] * dx[2] - dz[2] * dx[1];
+        o[1] = dz[2] * dx[0] - dz[0] * dx[2];
+        o[2] = dz[0] * dx[1] - dz[1] * dx[0];
+      }
+  for (int64_t k = 0; k < mz; ++k)            /* Zet :363-379 */
+    for (int64_t j = 1; j < my; ++j)
+      for (int64_t i = 1; i < mx; ++i) {
+        double dx[3], de[3];
+        for (int c = 0; c < 3; ++c) {
+          dx[c] = 0.5 * (P_(c, i, j, k) + P_(c, i, j - 1, k) - P_(c, i - 1, j, k) - P_(c, i - 1, j - 1, k));
+          de[c] = 0.5 * (P_(c, i, j, k) + P_(c, i - 1, j, k) - P_(c, i, j - 1, k) - P_(c, i - 1, j - 1, k));
+        }
+        double *o = zet + 3 * o_nidx(g, i, j, k);
+        o[0] = dx[1] * de[2] - dx[2] * de[1];
+        o[1] = dx[2] * de[0] - dx[0] * de[2];
+        o[2] = dx[0] * de[1] - dx[1] * de[0];
+      }
+#undef P_
+  /* boundary extrapolation :383-452, in the reference's order: i, then j, then k */
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t j = 0; j < my; ++j)
+      if (1 < mx) { o_cp3(eta, o_nidx(g, 0, j, k), o_nidx(g, 1, j, k)); o_cp3(zet, o_nidx(g, 0, j, k), o_nidx(g, 1, j, k)); }
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t j = 0; j < my; ++j)
+      if (mx - 2 >= 0) {
+        o_cp3(eta, o_nidx(g, mx - 1, j, k), o_nidx(g, mx - 2, j, k));
+        o_cp3(zet, o_nidx(g, mx - 1, j, k), o_nidx(g, mx - 2, j, k));
+      }
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t i = 0; i < mx; ++i)
+      if (1 < my) { o_cp3(csi, o_nidx(g, i, 0, k), o_nidx(g, i, 1, k)); o_cp3(zet, o_nidx(g, i, 0, k), o_nidx(g, i, 1, k)); }
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t i = 0; i < mx; ++i)
+      if (my - 2 >= 0) {
+        o_cp3(csi, o_nidx(g, i, my - 1, k), o_nidx(g, i, my - 2, k));
+        o_cp3(zet, o_nidx(g, i, my - 1, k), o_nidx(g, i, my - 2, k));
+      }
+  for (int64_t j = 0; j < my; ++j)
+    for (int64_t i = 0; i < mx; ++i)
+      if (1 < mz) { o_cp3(csi, o_nidx(g, i, j, 0), o_nidx(g, i, j, 1)); o_cp3(eta, o_nidx(g, i, j, 0), o_nidx(g, i, j, 1)); }
+  for (int64_t j = 0; j < my; ++j)
+    for (int64_t i = 0; i < mx; ++i)
+      if (mz - 2 >= 0) {
+        o_cp3(csi, o_nidx(g, i, j, mz - 1), o_nidx(g, i, j, mz - 2));
+        o_cp3(eta, o_nidx(g, i, j, mz - 1), o_nidx(g, i, j, mz - 2));
+      }
+}
+
+/* Metric.c:491-600. */
+int o_ComputeCellCenteredJacobianInverse(const OGrid *g, double *aj) {
+  const int64_t mx = g->IM + 1, my = g->JM + 1, mz = g->KM + 1, nn = mx * my * mz;
+  memset(aj, 0, (size_t)nn * sizeof(double));
+#define P_(c, ii, jj, kk) (node_at(g, (ii), (jj), (kk))[c])
+  for (int64_t k = 1; k < mz; ++k)
+    for (int64_t j = 1; j < my; ++j)
+      for (int64_t i = 1; i < mx; ++i) {
+        double dxi[3], deta[3], dzeta[3];
+        for (int c = 0; c < 3; ++c) {
+          dxi[c] = 0.25 * ((P_(c, i, j, k) + P_(c, i, j - 1, k) + P_(c, i, j, k - 1) + P_(c, i, j - 1, k - 1)) -
+                           (P_(c, i - 1, j, k) + P_(c, i - 1, j - 1, k) + P_(c, i - 1, j, k - 1) + P_(c, i - 1, j - 1, k - 1)));
+          deta[c] = 0.25 * ((P_(c, i, j, k) + P_(c, i - 1, j, k) + P_(c, i, j, k - 1) + P_(c, i - 1, j, k - 1)) -
+                            (P_(c, i, j - 1, k) + P_(c, i - 1, j - 1, k) + P_(c, i, j - 1, k - 1) + P_(c, i - 1, j - 1, k - 1)));
+          dzeta[c] = 0.25 * ((P_(c, i, j, k) + P_(c, i, j - 1, k) + P_(c, i - 1, j, k) + P_(c, i - 1, j - 1, k)) -
+                             (P_(c, i, j, k - 1) + P_(c, i, j - 1, k - 1) + P_(c, i - 1, j, k - 1) + P_(c, i - 1, j - 1, k - 1)));
+        }
+        const double J = dxi[0] * (deta[1] * dzeta[2] - deta[2] * dzeta[1]) -
+                         dxi[1] * (deta[0] * dzeta[2] - deta[2] * dzeta[0]) +
+                         dxi[2] * (deta[0] * dzeta[1] - deta[1] * dzeta[0]);
+        if (fabs(J) < 1.0e-12) return O_ERR_FLOP_COUNT;
+        aj[o_nidx(g, i, j, k)] = 1.0 / J;
+      }
+#undef P_
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t j = 0; j < my; ++j)
+      if (1 < mx) aj[o_nidx(g, 0, j, k)] = aj[o_nidx(g, 1, j, k)];
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t j = 0; j < my; ++j)
+      if (mx - 2 >= 0) aj[o_nidx(g, mx - 1, j, k)] = aj[o_nidx(g, mx - 2, j, k)];
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t i = 0; i < mx; ++i)
+      if (1 < my) aj[o_nidx(g, i, 0, k)] = aj[o_nidx(g, i, 1, k)];
+  for (int64_t k = 0; k < mz; ++k)
+    for (int64_t i = 0; i < mx; ++i)
+      if (my - 2 >= 0) aj[o_nidx(g, i, my - 1, k)] = aj[o_nidx(g, i, my - 2, k)];
+  for (int64_t j = 0; j < my; ++j)
+    for (int64_t i = 0; i < mx; ++i)
+      if (1 < mz) aj[o_nidx(g, i, j, 0)] = aj[o_nidx(g, i, j, 1)];
+  for (int64_t j = 0; j < my; ++j)
+    for (int64_t i = 0; i < mx; ++i)
+      if (mz - 2 >= 0) aj[o_nidx(g, i, j, mz - 1)] = aj[o_nidx(g, i, j, mz - 2)];
+  return 0;
+}
+
+/* Metric.c:195-260 (VecMin / VecMax over every node). */
+int o_CheckAndFixGridOrientation(const OGrid *g, double *csi, double *eta, double *zet, double *aj,
+                                 int *flipped) {
+  const int64_t nn = (g->IM + 1) * (g->JM + 1) * (g->KM + 1);
+  double lo = aj[0], hi = aj[0];
+  for (int64_t q = 1; q < nn; ++q) {
+    if (aj[q] < lo) lo = aj[q];
+    if (aj[q] > hi) hi = aj[q];
+  }
+  if (flipped) *flipped = 0;
+  if (lo < 0.0 && hi > 0.0) return O_ERR_USER;
+  if (hi < 0.0) {
+    for (int64_t q = 0; q < 3 * nn; ++q) { csi[q] = -csi[q]; eta[q] = -eta[q]; zet[q] = -zet[q]; }
+    for (int64_t q = 0; q < nn; ++q) aj[q] = -aj[q];
+    if (flipped) *flipped = 1;
+  }
+  return 0;
+}
+
+/* setup.c:1294-1420, one rank: cells 1 .. IM-1 (x), 1 .. JM-1 (y), 1 .. KM-1 (z). */
+int o_Contra2Cart(const OGrid *g, const double *ucont, const double *csi, const double *eta,
+                  const double *zet, double *ucat) {
+  for (int64_t k = 1; k < g->KM; ++k)
+    for (int64_t j = 1; j < g->JM; ++j)
+      for (int64_t i = 1; i < g->IM; ++i) {
+        const int64_t n = o_nidx(g, i, j, k);
+        const int64_t ni = o_nidx(g, i - 1, j, k), nj = o_nidx(g, i, j - 1, k), nk = o_nidx(g, i, j, k - 1);
+        double m[3][3];
+        for (int c = 0; c < 3; ++c) {
+          m[0][c] = 0.5 * (csi[3 * ni + c] + csi[3 * n + c]);
+          m[1][c] = 0.5 * (eta[3 * nj + c] + eta[3 * n + c]);
+          m[2][c] = 0.5 * (zet[3 * nk + c] + zet[3 * n + c]);
+        }
+        double q[3];
+        q[0] = 0.5 * (ucont[3 * ni] + ucont[3 * n]);
+        q[1] = 0.5 * (ucont[3 * nj + 1] + ucont[3 * n + 1]);
+        q[2] = 0.5 * (ucont[3 * nk + 2] + ucont[3 * n + 2]);
+        const double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                           m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                           m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        if (fabs(det) < 1.0e-18) return O_ERR_FLOP_COUNT;
+        const double det_inv = 1.0 / det;
+        const double det0 = q[0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                            q[1] * (m[0][1] * m[2][2] - m[0][2] * m[2][1]) +
+                            q[2] * (m[0][1] * m[1][2] - m[0][2] * m[1][1]);
+        const double det1 = -q[0] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                            q[1] * (m[0][0] * m[2][2] - m[0][2] * m[2][0]) -
+                            q[2] * (m[0][0] * m[1][2] - m[0][2] * m[1][0]);
+        const double det2 = q[0] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]) -
+                            q[1] * (m[0][0] * m[2][1] - m[0][1] * m[2][0]) +
+                            q[2] * (m[0][0] * m[1][1] - m[0][1] * m[1][0]);
+        ucat[3 * n] = det0 * det_inv;
+        ucat[3 * n + 1] = det1 * det_inv;
+        ucat[3 * n + 2] = det2 * det_inv;
+      }
+  return 0;
+}

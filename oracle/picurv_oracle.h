@@ -107,6 +107,24 @@ int o_AdvanceStep(const OGrid *g, const double *ucat, double *corner_scratch, OS
 int o_InitialSetup(const OGrid *g, const double *ucat, double *corner_scratch, OSwarm *s,
                    double *count, double *avg, int nthreads, OStepInfo *info);
 
+/* ---- the Eulerian input of the path: metrics and Contra2Cart ------------ */
+#define O_ERR_FLOP_COUNT 90
+/* Metric.c:286-460 ComputeFaceMetrics: Csi, Eta, Zet at every node, node-sized
+ * [KM+1][JM+1][IM+1][3]; outputs are zeroed first (fresh PETSc Vecs are zero). */
+void o_ComputeFaceMetrics(const OGrid *g, double *csi, double *eta, double *zet);
+/* Metric.c:491-600 ComputeCellCenteredJacobianInverse: Aj = 1/J, node-sized; returns
+ * O_ERR_FLOP_COUNT at the first node with |J| < 1e-12. */
+int o_ComputeCellCenteredJacobianInverse(const OGrid *g, double *aj);
+/* Metric.c:195-260 CheckAndFixGridOrientation: Aj of mixed signs -> O_ERR_USER; all negative
+ * -> Csi, Eta, Zet and Aj negated (*flipped = 1). */
+int o_CheckAndFixGridOrientation(const OGrid *g, double *csi, double *eta, double *zet, double *aj,
+                                 int *flipped);
+/* setup.c:1294-1420 Contra2Cart: ucat (node-sized [..][3]) of the cells i in 1..IM-1,
+ * j in 1..JM-1, k in 1..KM-1 from ucont (node-sized [..][3]) and the face metrics; other
+ * entries are left alone.  Returns O_ERR_FLOP_COUNT at the first cell with |det| < 1e-18. */
+int o_Contra2Cart(const OGrid *g, const double *ucont, const double *csi, const double *eta,
+                  const double *zet, double *ucat);
+
 #ifdef __cplusplus
 }
 #endif
