@@ -332,7 +332,7 @@ __device__ __forceinline__ float beyond_cells(const float (&dv)[6]) {
 //                   key and histogram entry are written there); a nearer one continues the
 //                   reference walk here.
 template <bool FIRST>
-__global__ void __launch_bounds__(256, 3) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(FDF_LOC_THREADS, 768 / FDF_LOC_THREADS) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
                                                   int reset_first, const double *__restrict__ bbox,
                                                   const float *__restrict__ fbox, int drop_removed,
@@ -775,14 +775,15 @@ void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *tabl
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                      unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
                      float far_cells, cudaStream_t s) {
+  constexpr int th = FDF_LOC_THREADS;
   if (pending)
-    k_locate32<true><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox,
-                                                            fbox, drop_removed, cnt, keys, count, sentinel, pending,
-                                                            n_cap, far_cells);
+    k_locate32<true><<<blocks_for(n_cap, th), th, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox,
+                                                          fbox, drop_removed, cnt, keys, count, sentinel, pending,
+                                                          n_cap, far_cells);
   else
-    k_locate32<false><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed,
-                                                             bbox, fbox, drop_removed, cnt, keys, count, sentinel,
-                                                             nullptr, n_cap, 0.f);
+    k_locate32<false><<<blocks_for(n_cap, th), th, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed,
+                                                           bbox, fbox, drop_removed, cnt, keys, count, sentinel,
+                                                           nullptr, n_cap, 0.f);
 }
 
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,

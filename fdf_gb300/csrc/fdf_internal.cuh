@@ -113,6 +113,12 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
   k = (int)kk;
 }
 
+// Threads per block of the advect + locate kernels.  A block keeps its SM slot until its
+// slowest walk ends, so smaller blocks waste fewer warp slots on the walk-length tail.
+#ifndef FDF_LOC_THREADS
+#define FDF_LOC_THREADS 128
+#endif
+
 // ---------------------------------------------------------------- kernels (launchers)
 void launch_build_planes(const double *coor_aos, GridDims g, double *planes, unsigned int *err, cudaStream_t s);
 // cell_start == nullptr: every node; else only nodes adjacent to an occupied cell.

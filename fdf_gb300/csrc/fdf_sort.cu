@@ -134,9 +134,15 @@ __global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__res
 }
 
 // Orders every cell's slots by (PID, previous slot) -- or by previous slot alone when
-// pid is null.  Segments are short (the mean occupancy is a few particles per cell);
-// up to 32 entries are sorted in registers and longer ones in place in global memory.
-constexpr int SEG_LOCAL = 32;
+// pid is null.  Segments are short (a few particles per cell on average): up to 8 entries
+// are checked and, when out of order, sorted in registers by a 19-comparator sorting
+// network; longer ones are insertion-sorted in place in global memory.
+constexpr int SEG_NET = 8;
+
+__device__ __forceinline__ bool key_gt(long long ka, unsigned int va, long long kb, unsigned int vb) {
+  return ka > kb || (ka == kb && va > vb);
+}
+
 __global__ void __launch_bounds__(256) k_order_segments(const unsigned int *__restrict__ cell_start, int nseg,
                                                        const long long *__restrict__ pid,
                                                        unsigned int *__restrict__ perm) {
@@ -145,22 +151,37 @@ __global__ void __launch_bounds__(256) k_order_segments(const unsigned int *__re
   const unsigned int s0 = cell_start[c], s1 = cell_start[c + 1];
   const unsigned int L = s1 - s0;
   if (L < 2) return;
-  if (L <= SEG_LOCAL) {
-    long long kp[SEG_LOCAL];
-    unsigned int ix[SEG_LOCAL];
-    for (unsigned int q = 0; q < L; ++q) {
-      unsigned int v = perm[s0 + q];
-      long long kv = pid ? pid[v] : (long long)v;
-      unsigned int r = q;
-      while (r > 0 && (kp[r - 1] > kv || (kp[r - 1] == kv && ix[r - 1] > v))) {
-        kp[r] = kp[r - 1];
-        ix[r] = ix[r - 1];
-        --r;
+  if (L <= SEG_NET) {
+    long long kp[SEG_NET];
+    unsigned int ix[SEG_NET];
+    bool sorted = true;
+#pragma unroll
+    for (int q = 0; q < SEG_NET; ++q) {
+      // padding (max, max) sorts after every real entry (slots are below 2^31)
+      kp[q] = 0x7fffffffffffffffLL;
+      ix[q] = 0xffffffffu;
+      if (q < (int)L) {
+        ix[q] = perm[s0 + q];
+        kp[q] = pid ? pid[ix[q]] : (long long)ix[q];
+        if (q > 0 && key_gt(kp[q - 1], ix[q - 1], kp[q], ix[q])) sorted = false;
       }
-      kp[r] = kv;
-      ix[r] = v;
     }
-    for (unsigned int q = 0; q < L; ++q) perm[s0 + q] = ix[q];
+    if (sorted) return;
+    auto cx = [&](int a, int b) {
+      const bool sw = key_gt(kp[a], ix[a], kp[b], ix[b]);
+      const long long ka = sw ? kp[b] : kp[a], kb = sw ? kp[a] : kp[b];
+      const unsigned int va = sw ? ix[b] : ix[a], vb = sw ? ix[a] : ix[b];
+      kp[a] = ka; kp[b] = kb; ix[a] = va; ix[b] = vb;
+    };
+    cx(0, 2); cx(1, 3); cx(4, 6); cx(5, 7);
+    cx(0, 4); cx(1, 5); cx(2, 6); cx(3, 7);
+    cx(0, 1); cx(2, 3); cx(4, 5); cx(6, 7);
+    cx(2, 4); cx(3, 5);
+    cx(1, 4); cx(3, 6);
+    cx(1, 2); cx(3, 4); cx(5, 6);
+#pragma unroll
+    for (int q = 0; q < SEG_NET; ++q)
+      if (q < (int)L) perm[s0 + q] = ix[q];
   } else {
     for (unsigned int q = 1; q < L; ++q) {
       unsigned int v = perm[s0 + q];

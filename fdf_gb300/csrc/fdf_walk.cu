@@ -34,7 +34,7 @@ using fdfx::add;
 using fdfx::sub;
 using fdfx::mul;
 
-__global__ void __launch_bounds__(256) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
+__global__ void __launch_bounds__(FDF_LOC_THREADS) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
                                                 double dt, int advect, int reset_first, const double *__restrict__ bbox,
                                                 int drop_removed, DevCounters *cnt, unsigned int *__restrict__ keys,
                                                 unsigned int *__restrict__ count, unsigned int sentinel) {
@@ -147,7 +147,7 @@ void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *plane
                    unsigned int sentinel, cudaStream_t s) {
   // advect and drop_removed are both set by the fused step, which also resets statuses first.
   int reset_first = drop_removed;
-  int th = 256;
+  constexpr int th = FDF_LOC_THREADS;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
   k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, count,
