@@ -80,6 +80,7 @@ struct FdfContext {
   int c2c_rc = FDF_SUCCESS;      // the table build's error (a near-zero determinant)
   std::string c2c_msg;
   int c2c_flipped = 0;
+  bool c2c_half = false;         // every tabled value mid-range: the halved Contra2Cart applies
   // fdf_AdvanceSteps replays one captured step per swarm buffer parity; `gen` counts the
   // changes of anything a captured step bakes in (pointers, kernel arguments, form)
   long long gen = 1;

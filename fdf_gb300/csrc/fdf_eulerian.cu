@@ -12,10 +12,12 @@
 //
 // Design: the metrics depend only on the grid, and so do the Cramer's-rule determinant and
 // the nine 2x2 minors it shares with det0..det2.  They are computed once per grid into a
-// per-cell table [10][Nc] (1/det, then the minors of det0, det1, det2); a Contra2Cart call
-// then reads 80 B of table and the face velocities per cell and does 25 FP64 operations
-// instead of ~90 plus a division.  The table's values are the reference's intermediate
-// values exactly, so the result is unchanged.
+// per-cell table [11][Nc] (1/det, the minors of det0, det1, det2, then 1/(2 det)); a
+// Contra2Cart call reads 80 B of table and the face velocities per cell and does 21 FP64
+// operations (3 face sums, 9 products, 6 sums, 3 scalings) instead of ~90 plus a division, and
+// converts its FP32 copy on the integer pipe.  The table holds the reference's intermediate
+// values exactly, and the halved form is exact in the range it is used, so every bit of ucat is
+// the reference's.  The kernel is bound by GB300's FP64 pipe, not HBM.
 #include "fdf_context.cuh"
 
 #include <algorithm>
@@ -25,9 +27,36 @@
 
 namespace {
 
-constexpr int C2C_SLOTS = 10;            // 1/det | A0 A1 A2 | B0 B1 B2 | C0 C1 C2
+constexpr int C2C_SLOTS = 11;            // 1/det | A0 A1 A2 | B0 B1 B2 | C0 C1 C2 | 1/(2 det)
 constexpr unsigned ERR_JACOBIAN = 1u;    // |J| < 1e-12 at a node (Metric.c:560)
 constexpr unsigned ERR_DET = 2u;         // |det| < 1e-18 in a cell (setup.c:1389-1391)
+constexpr unsigned ERR_WIDE = 4u;        // a tabled value outside [2^-400, 2^400] (not an error)
+
+// |x| in [2^-400, 2^400], or x == +-0: products of two such values neither overflow nor leave
+// the normal range, so halving them (and their sums) is exact.
+__device__ __forceinline__ bool mid_range(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) << 1;   // sign dropped
+  const unsigned int e = (unsigned int)(b >> 53);
+  return b == 0ull || (e - (1023u - 400u)) <= 800u;
+}
+
+// The hardware conversion, out of line so that it is not if-converted into every lane.
+__device__ __noinline__ float d2f_hw(double x) { return __double2float_rn(x); }
+
+// double -> float, round to nearest even, on the integer pipe for results in the normal
+// float range (the FP64 pipe is this path's bound); the rest takes the hardware conversion.
+// The low 29 mantissa bits round into bit 29 (ties to even), a carry moves into the exponent,
+// and the exponent is rebased from 1023 to 127.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long mag = b & 0x7fffffffffffffffull;
+  if (mag >= 0x3810000000000000ull && mag < 0x47efffffe0000000ull) {   // [2^-126, FLT_MAX)
+    const unsigned long long r = mag + 0x0fffffffull + ((mag >> 29) & 1ull);
+    const unsigned int f = (unsigned int)(r >> 29) - ((1023u - 127u) << 23);
+    return __uint_as_float(f | ((unsigned int)(b >> 32) & 0x80000000u));
+  }
+  return d2f_hw(x);
+}
 
 __device__ __forceinline__ long long nid(const GridDims &g, int i, int j, int k) {
   return ((long long)k * (g.JM + 1) + j) * (g.IM + 1) + i;
@@ -192,6 +221,11 @@ __global__ void k_c2c_table(const double *__restrict__ csi, const double *__rest
     t[1] = A0; t[2] = A1; t[3] = A2;
     t[4] = B0; t[5] = B1; t[6] = B2;
     t[7] = C0; t[8] = C1; t[9] = C2;
+    t[10] = 0.5 * t[0];
+    bool mid = t[0] != 0.0 && mid_range(t[0]);
+#pragma unroll
+    for (int q = 1; q < 10; ++q) mid = mid && mid_range(t[q]);
+    if (!mid) atomicOr(err, ERR_WIDE);
   }
 #pragma unroll
   for (int s = 0; s < C2C_SLOTS; ++s) table[s * g.Nc + c] = t[s];
@@ -200,6 +234,25 @@ __global__ void k_c2c_table(const double *__restrict__ csi, const double *__rest
 // Contra2Cart (setup.c:1374-1409) of the interior cells: the face-averaged contravariant
 // velocity q, det0..det2 from the tabled minors, ucat = det_q / det.  Writes the FP64 ucat
 // (SoA [3][Nc]) and its FP32 copy; boundary cells keep their values.
+//
+// HALF (every tabled value in [2^-400, 2^400]): with s = a + b, the reference's q = s/2 and
+// det0 = q0 A0 - q1 A1 + q2 A2 are exactly half of s0 A0 - s1 A1 + s2 A2 whenever the face
+// sums s lie in [2^-400, 2^400] too (products and sums stay normal, so halving commutes with
+// every rounding), and det0 * (1/det) then rounds the same real number as
+// (s0 A0 - s1 A1 + s2 A2) * (1/(2 det)).  Three FP64 multiplications per cell fewer; a cell
+// whose face sums fall outside that range takes the reference's literal sequence.
+// The reference's literal sequence (setup.c:1374-1409) from the face sums; out of line so that
+// the compiler does not if-convert its halvings into the common path.
+__device__ __noinline__ void c2c_literal(double s0, double s1, double s2, const double *__restrict__ table,
+                                         long long c, long long N, double &u, double &v, double &w) {
+  const double q0 = 0.5 * s0, q1 = 0.5 * s1, q2 = 0.5 * s2;
+  const double di = table[c];
+  u = (q0 * table[N + c] - q1 * table[2 * N + c] + q2 * table[3 * N + c]) * di;
+  v = (-q0 * table[4 * N + c] + q1 * table[5 * N + c] - q2 * table[6 * N + c]) * di;
+  w = (q0 * table[7 * N + c] - q1 * table[8 * N + c] + q2 * table[9 * N + c]) * di;
+}
+
+template <bool HALF>
 __global__ void __launch_bounds__(256) k_contra2cart(const double *__restrict__ ucont, const double *__restrict__ table,
                                                      GridDims g, double *__restrict__ ucat, float *__restrict__ ucat32) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -209,17 +262,21 @@ __global__ void __launch_bounds__(256) k_contra2cart(const double *__restrict__ 
   if (i == 0 || j == 0 || k == 0) return;
   const long long n = nid(g, i, j, k);
   const long long sj = g.IM + 1, sk = (long long)(g.IM + 1) * (g.JM + 1);
-  const double q0 = 0.5 * (ucont[3 * (n - 1)] + ucont[3 * n]);
-  const double q1 = 0.5 * (ucont[3 * (n - sj) + 1] + ucont[3 * n + 1]);
-  const double q2 = 0.5 * (ucont[3 * (n - sk) + 2] + ucont[3 * n + 2]);
+  const double s0 = ucont[3 * (n - 1)] + ucont[3 * n];
+  const double s1 = ucont[3 * (n - sj) + 1] + ucont[3 * n + 1];
+  const double s2 = ucont[3 * (n - sk) + 2] + ucont[3 * n + 2];
   const long long N = g.Nc;
-  const double di = table[c];
-  const double det0 = q0 * table[N + c] - q1 * table[2 * N + c] + q2 * table[3 * N + c];
-  const double det1 = -q0 * table[4 * N + c] + q1 * table[5 * N + c] - q2 * table[6 * N + c];
-  const double det2 = q0 * table[7 * N + c] - q1 * table[8 * N + c] + q2 * table[9 * N + c];
-  const double u = det0 * di, v = det1 * di, w = det2 * di;
+  double u, v, w;
+  if (HALF && mid_range(s0) && mid_range(s1) && mid_range(s2)) {
+    const double hdi = table[10 * N + c];
+    u = (s0 * table[N + c] - s1 * table[2 * N + c] + s2 * table[3 * N + c]) * hdi;
+    v = (-s0 * table[4 * N + c] + s1 * table[5 * N + c] - s2 * table[6 * N + c]) * hdi;
+    w = (s0 * table[7 * N + c] - s1 * table[8 * N + c] + s2 * table[9 * N + c]) * hdi;
+  } else {
+    c2c_literal(s0, s1, s2, table, c, N, u, v, w);
+  }
   ucat[c] = u; ucat[N + c] = v; ucat[2 * N + c] = w;
-  ucat32[c] = (float)u; ucat32[N + c] = (float)v; ucat32[2 * N + c] = (float)w;
+  ucat32[c] = d2f_rn(u); ucat32[N + c] = d2f_rn(v); ucat32[2 * N + c] = d2f_rn(w);
 }
 
 inline unsigned blocks_of(long long n, int th) { return (unsigned)((n + th - 1) / th); }
@@ -320,6 +377,7 @@ int ensure_c2c_table(FdfContext *ctx) {
                 std::string("Contra2Cart table: ") + cudaGetErrorString(e));
   }
   ctx->c2c_flipped = flipped;
+  ctx->c2c_half = (err_h & ERR_WIDE) == 0u;
   ctx->c2c_rc = FDF_SUCCESS;
   if (err_h & ERR_DET) {
     ctx->c2c_rc = FDF_ERR_FLOP_COUNT;
@@ -380,8 +438,12 @@ int fdf_Contra2Cart(FdfContext *ctx) {
   if (r) return r;
   const bool prof = ctx->profiling;
   const size_t e0 = prof ? record_event(ctx, ctx->stream) : 0;
-  k_contra2cart<<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ctx->ucont, ctx->c2c_table, ctx->g, ctx->ucat,
-                                                                    ctx->ucat32);
+  if (ctx->c2c_half)
+    k_contra2cart<true><<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ctx->ucont, ctx->c2c_table, ctx->g,
+                                                                          ctx->ucat, ctx->ucat32);
+  else
+    k_contra2cart<false><<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ctx->ucont, ctx->c2c_table, ctx->g,
+                                                                           ctx->ucat, ctx->ucat32);
   CHECK_LAUNCH();
   ctx->launches += 1;
   if (prof) {

@@ -332,7 +332,7 @@ __device__ __forceinline__ float beyond_cells(const float (&dv)[6]) {
 //                   key and histogram entry are written there); a nearer one continues the
 //                   reference walk here.
 template <bool FIRST>
-__global__ void __launch_bounds__(FDF_LOC_THREADS, 768 / FDF_LOC_THREADS) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_LOC_MIN_BLOCKS) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
                                                   int reset_first, const double *__restrict__ bbox,
                                                   const float *__restrict__ fbox, int drop_removed,
@@ -427,7 +427,7 @@ __global__ void k_compact_pending(const unsigned int *__restrict__ scan, int n_c
 // margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise guess[t] becomes
 // -1 and k_locate32_fallback continues the reference walk from P1.  Grid-stride over the
 // list, warp-uniform trip count.
-__global__ void __launch_bounds__(256, 3) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                         const double *__restrict__ planes,
                                                         const double *__restrict__ bbox,
                                                         const float *__restrict__ fbox, int drop_removed,
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256, 3) k_locate32_guess(SwarmBuf b, GridDims 
 // scans a chunk of 32 x 32 list entries, queues the failed ones in shared memory and walks
 // them 32 at a time, so every lane has a particle.
 constexpr int FB_CHUNK = 1024;
-__global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                            const double *__restrict__ planes,
                                                            const double *__restrict__ bbox,
                                                            const float *__restrict__ fbox, int drop_removed,

@@ -118,6 +118,16 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_LOC_THREADS
 #define FDF_LOC_THREADS 128
 #endif
+// Resident blocks per SM the FP32 locate kernels are compiled for.  The walk is bound by load
+// latency, so 1024 resident threads (64 registers, a few spilled to L1) beat 768 (80, none
+// spilled): 3.9 against 4.8 ms per 64M-particle step; 1280 (48 registers) spills too much.
+#ifndef FDF_LOC_MIN_BLOCKS
+#define FDF_LOC_MIN_BLOCKS (1024 / FDF_LOC_THREADS)
+#endif
+// Resident 256-thread blocks per SM the learned form's guess and fallback walks are compiled for.
+#ifndef FDF_GUESS_MIN_BLOCKS
+#define FDF_GUESS_MIN_BLOCKS 3
+#endif
 
 // ---------------------------------------------------------------- kernels (launchers)
 void launch_build_planes(const double *coor_aos, GridDims g, double *planes, unsigned int *err, cudaStream_t s);

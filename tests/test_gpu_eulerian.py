@@ -34,9 +34,10 @@ GRIDS = {
 
 
 def assert_bitwise(a, b, what):
+    """Bit for bit, except that any two NaNs match (their payloads are the machine's)."""
     a, b = np.asarray(a), np.asarray(b)
     assert a.shape == b.shape, what
-    bad = a.view(np.int64) != b.view(np.int64)
+    bad = (a.view(np.int64) != b.view(np.int64)) & ~(np.isnan(a) & np.isnan(b))
     assert not bad.any(), f"{what}: {int(bad.sum())} values differ, first at {np.argwhere(bad)[0]}"
 
 
@@ -78,6 +79,38 @@ def test_contra2cart_bitwise(ctx, name):
     ctx.contra2cart()
     ref2 = O.contra2cart(g, ucont2, csi, eta, zet, ucat0)
     assert_bitwise(_ucat_cells(ctx), ref2[:KM, :JM, :IM], f"{name} ucat, second call")
+
+
+def _check_c2c(ctx, coor, ucont, what):
+    KM, JM, IM = (s - 1 for s in coor.shape[:3])
+    ctx.set_grid(coor)
+    ctx.set_ucont(ucont)
+    ctx.contra2cart()
+    g = O.Grid(coor)
+    csi, eta, zet, _, _ = O.grid_metrics(g)
+    ref = O.contra2cart(g, ucont, csi, eta, zet)
+    assert_bitwise(_ucat_cells(ctx)[1:, 1:, 1:], ref[1:KM, 1:JM, 1:IM], what)
+
+
+def test_contra2cart_extreme_face_velocities(ctx):
+    """Face sums outside [2^-400, 2^400] (zeros of both signs, subnormals, huge values, inf)
+    take the literal sequence; the rest the halved one: both bit for bit."""
+    coor = W.sinusoidal_grid(10, 9, 12)
+    rng = np.random.default_rng(21)
+    ucont = rng.uniform(-1.0, 1.0, size=coor.shape)
+    pick = rng.integers(0, 8, size=coor.shape)
+    specials = [0.0, -0.0, 5e-324, -3e-310, 1e-300, -2e280, 1e300, np.inf]
+    for q, v in enumerate(specials):
+        ucont[pick == q] = np.where(rng.uniform(size=coor.shape) < 0.3, v, ucont)[pick == q]
+    _check_c2c(ctx, coor, ucont, "extreme face velocities")
+
+
+def test_contra2cart_wide_table(ctx):
+    """A grid scaled by 2^110: tabled minors above 2^400 and 1/det below 2^-400, so the whole
+    grid takes the literal sequence."""
+    coor = W.sinusoidal_grid(6, 5, 7) * 2.0 ** 110
+    ucont = np.random.default_rng(22).uniform(-1.0, 1.0, size=coor.shape) * 2.0 ** 216
+    _check_c2c(ctx, coor, ucont, "wide table")
 
 
 def test_errors(ctx):
