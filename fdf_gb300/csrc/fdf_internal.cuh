@@ -124,6 +124,15 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_LOC_MIN_BLOCKS
 #define FDF_LOC_MIN_BLOCKS (1024 / FDF_LOC_THREADS)
 #endif
+// Resident blocks per SM of the plain FP64 walk (FP64-bound: occupancy barely matters) and of
+// the per-cell PID ordering (latency-bound: 2048 resident threads at 32 registers, 1.59 -> 1.24 ms
+// for the 64M-particle sort stage).
+#ifndef FDF_PLAIN_MIN_BLOCKS
+#define FDF_PLAIN_MIN_BLOCKS 12
+#endif
+#ifndef FDF_ORDER_MIN_BLOCKS
+#define FDF_ORDER_MIN_BLOCKS 8
+#endif
 // Resident 256-thread blocks per SM the learned form's guess and fallback walks are compiled for.
 #ifndef FDF_GUESS_MIN_BLOCKS
 #define FDF_GUESS_MIN_BLOCKS 3

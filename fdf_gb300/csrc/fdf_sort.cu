@@ -143,7 +143,7 @@ __device__ __forceinline__ bool key_gt(long long ka, unsigned int va, long long 
   return ka > kb || (ka == kb && va > vb);
 }
 
-__global__ void __launch_bounds__(256) k_order_segments(const unsigned int *__restrict__ cell_start, int nseg,
+__global__ void __launch_bounds__(256, FDF_ORDER_MIN_BLOCKS) k_order_segments(const unsigned int *__restrict__ cell_start, int nseg,
                                                        const long long *__restrict__ pid,
                                                        unsigned int *__restrict__ perm) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;

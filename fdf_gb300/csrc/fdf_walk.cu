@@ -34,7 +34,7 @@ using fdfx::add;
 using fdfx::sub;
 using fdfx::mul;
 
-__global__ void __launch_bounds__(FDF_LOC_THREADS) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
+__global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
                                                 double dt, int advect, int reset_first, const double *__restrict__ bbox,
                                                 int drop_removed, DevCounters *cnt, unsigned int *__restrict__ keys,
                                                 unsigned int *__restrict__ count, unsigned int sentinel) {
