@@ -267,12 +267,12 @@ MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, on
 # units the stage processed then: live particles, or guessed particles for the network and
 # the walk from the guess.
 TRAFFIC = {
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (8.100e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (8.168e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (1.168e9, "guesses", 29.64e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (8.844e9, "guesses", 29.64e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.839e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (8.045e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.838e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (8.816e9, "guesses", 29.64e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.842e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (8.069e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.842e9, "particles", 63.81e6),
 }
 
 
@@ -486,6 +486,10 @@ def fp32_accuracy(ctx, wl, steps: int, nthreads: int) -> dict:
             "P_avg_rel": stats(np.abs(gavg[occupied] - sim.avg[occupied]) / np.abs(sim.avg[occupied]))}
 
 
+FP64_OPS_C2C = 21      # 3 face sums, 9 products, 6 sums, 3 scalings per interior cell
+CLOCK_MAX_MHZ = 2070   # GB300 maximum SM clock
+
+
 def time_contra2cart(ctx, wl, calls: int) -> dict:
     """Contra2Cart (setup.c:1294-1420) on the workload's grid: the face fluxes of a uniform
     flow are uploaded once, the first call builds the metric table (timed on the host), then
@@ -516,10 +520,18 @@ def time_contra2cart(ctx, wl, calls: int) -> dict:
     alg = 116 * n_int + 24 * Nn        # table 80 + ucat 24 + ucat32 12 per interior cell, face velocity per node
     hbm, peak_kind = peaks()
     gbs = alg / (ms / 1000.0) / 1e9
+    # the bound: GB300's FP64 pipe, two lanes per clock per SM (ncu: sm__pipe_fp64_cycles_active
+    # 83 % with 21 FP64 instructions per cell)
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    fp64_peak = 2.0 * sms * CLOCK_MAX_MHZ * 1e6 / 1e9
+    gops = FP64_OPS_C2C * n_int / (ms / 1000.0) / 1e9
     return {"ms_per_call": ms, "calls": runs, "table_build_ms": table_ms, "interior_cells": n_int,
+            "bound": "fp64", "fp64_ops_per_cell": FP64_OPS_C2C, "achieved_fp64_gops": gops,
+            "fp64_pipe_peak_gops": fp64_peak, "fp64_frac": gops / fp64_peak,
+            "fp64_peak_source": f"2 FP64 lanes per clock x {sms} SMs x {CLOCK_MAX_MHZ} MHz",
             "algorithmic_bytes_per_call": alg, "achieved_gbs": gbs, "hbm_frac": gbs / hbm,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-            "fp64_ops_per_cell": 24, "fp64_gflops": 24 * n_int / (ms / 1000.0) / 1e9,
             "uniform_flow_max_abs_error": err, "grid_flipped": flipped}
 
 
