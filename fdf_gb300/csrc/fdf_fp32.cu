@@ -795,14 +795,25 @@ void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float
                            const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                            unsigned int *keys, unsigned int *count, unsigned int sentinel,
                            const unsigned int *pending, int *guess, int num_sms, cudaStream_t s) {
-  long long blocks = ((long long)n_cap + 255) / 256;
-  const long long cap = (long long)num_sms * 8;
-  if (blocks > cap) blocks = cap;
-  if (blocks < 1) blocks = 1;
-  k_locate32_guess<<<(unsigned)blocks, 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
-                                                    sentinel, pending, guess);
-  k_locate32_fallback<<<(unsigned)blocks, 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
-                                                       sentinel, pending, guess);
+  // grid-stride kernels: one wave of resident blocks, so that no SM runs a partial last wave
+  static int resident[2] = {0, 0}, res_device = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (res_device != dev) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_locate32_guess, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_locate32_fallback, 256, 0);
+    res_device = dev;
+  }
+  const long long need = ((long long)n_cap + 255) / 256;
+  auto wave = [&](int r) {
+    long long blocks = (long long)num_sms * (r > 0 ? r : 1);
+    if (blocks > need) blocks = need;
+    return (unsigned)(blocks < 1 ? 1 : blocks);
+  };
+  k_locate32_guess<<<wave(resident[0]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
+                                                     sentinel, pending, guess);
+  k_locate32_fallback<<<wave(resident[1]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys,
+                                                        count, sentinel, pending, guess);
 }
 
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
