@@ -669,41 +669,48 @@ __global__ void __launch_bounds__(256) k_deposit32(SwarmBuf b, GridDims g, const
   const long long c = ((long long)k * JM + j) * IM + i;
   int s0 = 0, s1 = 0;
   if (is_cell) { s0 = (int)__ldg(cs + c); s1 = (int)__ldg(cs + c + 1); }
+  // per face the lower cell's segment first, then this cell's; the three lower segments run
+  // first and this cell's segment then feeds the P sum and the three upper parts in one pass
+  // (every accumulator receives its values in the same order as face by face)
+  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
+  const bool face_i = j < JM && k < KM, face_j = i < IM && k < KM, face_k = i < IM && j < JM;
+  KSum acc[3], mm[3][3];
+  auto lower = [&](int f, const float *__restrict__ wgt, long long lc) {
+    const int l0 = (int)__ldg(cs + lc), l1 = (int)__ldg(cs + lc + 1);
+    for (int s = l0; s < l1; ++s) {
+      const float fr = __ldg(wgt + s) * third;
+      acc[f].add(fr);
+      if (MOM) { mm[f][0].add(fr * __ldg(b.uf + s)); mm[f][1].add(fr * __ldg(b.vf + s)); mm[f][2].add(fr * __ldg(b.wf + s)); }
+    }
+  };
+  if (face_i && i > 0) lower(0, b.a1f, c - 1);
+  if (face_j && j > 0) lower(1, b.a2f, ((long long)k * JM + (j - 1)) * IM + i);
+  if (face_k && k > 0) lower(2, b.a3f, ((long long)(k - 1) * JM + j) * IM + i);
+  KSum sum;
+  for (int s = s0; s < s1; ++s) {
+    sum.add(__ldg(b.Pf + s));
+    const float w[3] = {__ldg(b.a1f + s), __ldg(b.a2f + s), __ldg(b.a3f + s)};
+    float u = 0.f, v = 0.f, ww = 0.f;
+    if (MOM) { u = __ldg(b.uf + s); v = __ldg(b.vf + s); ww = __ldg(b.wf + s); }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const float fr = (1.f - w[f]) * third;
+      acc[f].add(fr);
+      if (MOM) { mm[f][0].add(fr * u); mm[f][1].add(fr * v); mm[f][2].add(fr * ww); }
+    }
+  }
   {
-    KSum sum;
-    for (int s = s0; s < s1; ++s) sum.add(__ldg(b.Pf + s));
     const int nc = s1 - s0;
     count[q] = (float)nc;
     avg[q] = nc > 0 ? sum.value() / (float)nc : 0.f;
   }
-  auto face = [&](const float *__restrict__ wgt, long long lower, bool has_lower, bool has_upper, float *vol,
-                  float *mom, long long nf, long long fidx) {
-    KSum acc, m0, m1, m2;
-    if (has_lower) {
-      const int l0 = (int)__ldg(cs + lower), l1 = (int)__ldg(cs + lower + 1);
-      for (int s = l0; s < l1; ++s) {
-        const float f = __ldg(wgt + s) * third;
-        acc.add(f);
-        if (MOM) { m0.add(f * __ldg(b.uf + s)); m1.add(f * __ldg(b.vf + s)); m2.add(f * __ldg(b.wf + s)); }
-      }
-    }
-    if (has_upper)
-      for (int s = s0; s < s1; ++s) {
-        const float f = (1.f - __ldg(wgt + s)) * third;
-        acc.add(f);
-        if (MOM) { m0.add(f * __ldg(b.uf + s)); m1.add(f * __ldg(b.vf + s)); m2.add(f * __ldg(b.wf + s)); }
-      }
-    vol[fidx] = acc.value();
-    if (MOM) { mom[fidx] = m0.value(); mom[nf + fidx] = m1.value(); mom[2 * nf + fidx] = m2.value(); }
+  auto store = [&](int f, float *vol, float *mom, long long nf, long long fidx) {
+    vol[fidx] = acc[f].value();
+    if (MOM) { mom[fidx] = mm[f][0].value(); mom[nf + fidx] = mm[f][1].value(); mom[2 * nf + fidx] = mm[f][2].value(); }
   };
-  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
-  if (j < JM && k < KM)
-    face(b.a1f, c - 1, i > 0, i < IM, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);
-  if (i < IM && k < KM)
-    face(b.a2f, ((long long)k * JM + (j - 1)) * IM + i, j > 0, j < JM, fj, mj, nfj,
-         ((long long)k * (JM + 1) + j) * IM + i);
-  if (i < IM && j < JM)
-    face(b.a3f, ((long long)(k - 1) * JM + j) * IM + i, k > 0, k < KM, fk, mk, nfk, c);
+  if (face_i) store(0, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);
+  if (face_j) store(1, fj, mj, nfj, ((long long)k * (JM + 1) + j) * IM + i);
+  if (face_k) store(2, fk, mk, nfk, c);
 }
 
 __global__ void k_from_aos32(const double *__restrict__ pos, const double *__restrict__ vel,

@@ -104,56 +104,62 @@ __global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const u
   const long long c = ((long long)k * JM + j) * IM + i;
   int s0 = 0, s1 = 0;
   if (is_cell) { s0 = (int)__ldg(cs + c); s1 = (int)__ldg(cs + c + 1); }
-  // AccumulateParticleField + CalculateParticleCountPerCell + NormalizeGridVectorByCount
-  {
-    double sum = 0.0;
-    if (s1 > s0) {
-      sum = fdfx::add0(__ldg(b.P + s0));
-      for (int s = s0 + 1; s < s1; ++s) sum = add(sum, __ldg(b.P + s));
+  // Face accumulators: per face the lower cell's segment (weight a) first, then this cell's
+  // (weight 1 - a).  The three lower segments run first; this cell's segment then feeds the P
+  // sum and the three faces' upper parts in one pass, so every accumulator still receives its
+  // values in the order above.
+  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
+  const bool face_i = j < JM && k < KM, face_j = i < IM && k < KM, face_k = i < IM && j < JM;
+  double acc[3] = {0.0, 0.0, 0.0}, mm[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+  auto lower = [&](int f, const double *__restrict__ wgt, long long lc) {
+    const int l0 = (int)__ldg(cs + lc), l1 = (int)__ldg(cs + lc + 1);
+    for (int s = l0; s < l1; ++s) {
+      const double fr = mul(__ldg(wgt + s), third);
+      acc[f] = add(acc[f], fr);
+      if (MOM) {
+        mm[f][0] = add(mm[f][0], mul(fr, __ldg(b.u + s)));
+        mm[f][1] = add(mm[f][1], mul(fr, __ldg(b.v + s)));
+        mm[f][2] = add(mm[f][2], mul(fr, __ldg(b.w + s)));
+      }
     }
+  };
+  if (face_i && i > 0) lower(0, b.a1, c - 1);
+  if (face_j && j > 0) lower(1, b.a2, ((long long)k * JM + (j - 1)) * IM + i);
+  if (face_k && k > 0) lower(2, b.a3, ((long long)(k - 1) * JM + j) * IM + i);
+  // AccumulateParticleField + CalculateParticleCountPerCell + NormalizeGridVectorByCount, and
+  // the upper parts of the three faces (a cell node owns all three)
+  double sum = 0.0;
+  for (int s = s0; s < s1; ++s) {
+    const double P = __ldg(b.P + s);
+    sum = (s == s0) ? fdfx::add0(P) : add(sum, P);
+    const double w[3] = {__ldg(b.a1 + s), __ldg(b.a2 + s), __ldg(b.a3 + s)};
+    double u = 0.0, v = 0.0, ww = 0.0;
+    if (MOM) { u = __ldg(b.u + s); v = __ldg(b.v + s); ww = __ldg(b.w + s); }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const double fr = mul(sub(1.0, w[f]), third);
+      acc[f] = add(acc[f], fr);
+      if (MOM) {
+        mm[f][0] = add(mm[f][0], mul(fr, u));
+        mm[f][1] = add(mm[f][1], mul(fr, v));
+        mm[f][2] = add(mm[f][2], mul(fr, ww));
+      }
+    }
+  }
+  {
     const unsigned int ncell = (unsigned int)(s1 - s0);   // count += 1.0 per particle is exact in FP64
     count[q] = fdfx::u32_to_double(ncell);
     double a = 0.0;
     if (ncell > 0) a = fdfx::div_count(sum, ncell);
     avg[q] = a;
   }
-  // one face: the lower cell's segment with weight a, then the upper cell's with 1 - a
-  auto face = [&](const double *__restrict__ wgt, long long lower, bool has_lower, bool has_upper, double *vol,
-                  double *mom, long long nf, long long fidx) {
-    double acc = 0.0, m0 = 0.0, m1 = 0.0, m2 = 0.0;
-    if (has_lower) {
-      const int l0 = (int)__ldg(cs + lower), l1 = (int)__ldg(cs + lower + 1);
-      for (int s = l0; s < l1; ++s) {
-        const double f = mul(__ldg(wgt + s), third);
-        acc = add(acc, f);
-        if (MOM) {
-          m0 = add(m0, mul(f, __ldg(b.u + s)));
-          m1 = add(m1, mul(f, __ldg(b.v + s)));
-          m2 = add(m2, mul(f, __ldg(b.w + s)));
-        }
-      }
-    }
-    if (has_upper)
-      for (int s = s0; s < s1; ++s) {
-        const double f = mul(sub(1.0, __ldg(wgt + s)), third);
-        acc = add(acc, f);
-        if (MOM) {
-          m0 = add(m0, mul(f, __ldg(b.u + s)));
-          m1 = add(m1, mul(f, __ldg(b.v + s)));
-          m2 = add(m2, mul(f, __ldg(b.w + s)));
-        }
-      }
-    vol[fidx] = acc;
-    if (MOM) { mom[fidx] = m0; mom[nf + fidx] = m1; mom[2 * nf + fidx] = m2; }
+  auto store = [&](int f, double *vol, double *mom, long long nf, long long fidx) {
+    vol[fidx] = acc[f];
+    if (MOM) { mom[fidx] = mm[f][0]; mom[nf + fidx] = mm[f][1]; mom[2 * nf + fidx] = mm[f][2]; }
   };
-  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
-  if (j < JM && k < KM)   // i-face (i,j,k), i in [0, IM]
-    face(b.a1, c - 1, i > 0, i < IM, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);
-  if (i < IM && k < KM)   // j-face (i,j,k), j in [0, JM]
-    face(b.a2, ((long long)k * JM + (j - 1)) * IM + i, j > 0, j < JM, fj, mj, nfj,
-         ((long long)k * (JM + 1) + j) * IM + i);
-  if (i < IM && j < JM)   // k-face (i,j,k), k in [0, KM]
-    face(b.a3, ((long long)(k - 1) * JM + j) * IM + i, k > 0, k < KM, fk, mk, nfk, c);
+  if (face_i) store(0, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);   // i-face (i,j,k), i in [0, IM]
+  if (face_j) store(1, fj, mj, nfj, ((long long)k * (JM + 1) + j) * IM + i);   // j-face (i,j,k), j in [0, JM]
+  if (face_k) store(2, fk, mk, nfk, c);                                        // k-face (i,j,k), k in [0, KM]
 }
 
 __global__ void k_from_aos(const double *__restrict__ pos, const double *__restrict__ vel,
