@@ -412,7 +412,7 @@ namespace {
 // deposit; the learned form adds the flag scan (3), the compaction, the network, the walk
 // from the guess and the fallback walk.
 long long launches_per_step(const FdfContext *ctx) {
-  return 9 + (ctx->swarm_form == FDF_FORM_LEARNED_FP32 ? 7 : 0);
+  return 10 + (ctx->swarm_form == FDF_FORM_LEARNED_FP32 ? 7 : 0);
 }
 
 // The shared pipeline of the initial setup (advect=0, drop=0) and a step (1, 1).
@@ -497,6 +497,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     launch_deposit(dst, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, m,
                    m ? m + 3 * nfi : nullptr, m ? m + 3 * (nfi + nfj) : nullptr, s);
   }
+  launch_fold_counts(ctx->cnt, s);
   ctx->out_momentum = ctx->momentum;
   ctx->out_form = ctx->swarm_form;
   size_t e5 = prof ? record_event(ctx, s) : 0;
@@ -519,7 +520,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   ctx->launches += launches_per_step(ctx);
   if (info) {
     DevCounters c{};
-    CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(&c, ctx->cnt, DEVCOUNTERS_HEAD, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     info->n_start = n_start;
     info->n_end = c.n_sorted;
@@ -611,7 +612,7 @@ int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_eval
   if (!ctx || !particle_steps || !walk_evals || !corner_nodes) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));
   DevCounters c{};
-  CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(&c, ctx->cnt, DEVCOUNTERS_HEAD, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   *particle_steps = (int64_t)c.psteps_total;
   *walk_evals = (int64_t)c.evals_total;

@@ -46,16 +46,8 @@ __device__ __forceinline__ void block_flush_counts(const LocCounts &m, DevCounte
     if (q < 6) {
       unsigned long long t = 0;
       for (int k = 0; k < nw; ++k) t += red[k][q];
-      if (t) {
-        switch (q) {
-          case 0: atomicAdd(&cnt->removed_lost, t); break;
-          case 1: atomicAdd(&cnt->removed_oob, t); break;
-          case 2: atomicAdd(&cnt->evals, t); break;
-          case 3: atomicAdd(&cnt->evals_total, t); break;
-          case 4: atomicAdd(&cnt->lost_total, t); break;
-          default: atomicAdd(&cnt->fallbacks, t); atomicAdd(&cnt->fallbacks_total, t); break;
-        }
-      }
+      // slot q of this block's flush row (CNT_LOST .. CNT_FB are 0 .. 5, the order of v[])
+      if (t) atomicAdd(&cnt->stripes[blockIdx.x & (FDF_CNT_STRIPES - 1)][q], t);
     } else {
       unsigned int t = 0;
       for (int k = 0; k < nw; ++k) t |= rerr[k];

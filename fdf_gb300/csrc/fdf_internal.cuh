@@ -36,6 +36,13 @@ enum { ST_NEEDS_LOCATION = 0, ST_ACTIVE_AND_LOCATED = 1, ST_MIGRATING_OUT = 2, S
 // Device error word bits.
 enum { ERRBIT_DEGENERATE = 1u, ERRBIT_TC_TIMEOUT = 4u };
 
+// The walk kernels' block flushes go to one of FDF_CNT_STRIPES rows (by block index), so that
+// they spread over the L2 slices instead of queueing on one line; k_fold_counts adds the rows
+// to the counters at the end of every pipeline run and zeroes them.
+#define FDF_CNT_STRIPES 512
+enum { CNT_LOST = 0, CNT_OOB = 1, CNT_EVALS = 2, CNT_EVALS_TOTAL = 3, CNT_LOST_TOTAL = 4, CNT_FB = 5,
+       CNT_SLOTS = 8 };
+
 // Counters kept on the device so that a step needs no host round trip.
 struct DevCounters {
   // reset at the start of every pipeline run
@@ -58,7 +65,10 @@ struct DevCounters {
   unsigned long long guess_taken_total;   // ... whose walk from the guess was accepted
   unsigned long long guess_evals_total;   // ... evaluations made by the walks from the guess
   unsigned long long fallback_evals_total;   // ... by the reference walks of the guesses not taken
+  unsigned long long stripes[FDF_CNT_STRIPES][CNT_SLOTS];   // pending block flushes (k_fold_counts)
 };
+// The counters without the flush rows (what the host reads back).
+#define DEVCOUNTERS_HEAD offsetof(DevCounters, stripes)
 
 struct SwarmBuf {
   double *x, *y, *z;                         // positions (both forms)
@@ -139,6 +149,8 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #endif
 
 // ---------------------------------------------------------------- kernels (launchers)
+// Adds the pending block flushes to the counters and clears them (end of a pipeline run).
+void launch_fold_counts(DevCounters *cnt, cudaStream_t s);
 void launch_build_planes(const double *coor_aos, GridDims g, double *planes, unsigned int *err, cudaStream_t s);
 // cell_start == nullptr: every node; else only nodes adjacent to an occupied cell.
 void launch_center_to_corner(const double *ucat, GridDims g, double *corner, const unsigned int *cell_start,

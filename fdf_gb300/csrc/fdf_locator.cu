@@ -429,7 +429,7 @@ int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t
   if (!ctx || !asked || !taken || !guess_evals || !fallback_evals) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));
   DevCounters c{};
-  CU(cudaMemcpyAsync(&c, ctx->cnt, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaMemcpyAsync(&c, ctx->cnt, DEVCOUNTERS_HEAD, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   *asked = (int64_t)c.guess_asked_total;
   *taken = (int64_t)c.guess_taken_total;

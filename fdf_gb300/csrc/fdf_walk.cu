@@ -140,7 +140,32 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locat
   block_flush_counts(m, cnt);
 }
 
+// One warp per flush slot: sums the slot over the rows, clears them, and adds the sum to its
+// counter(s).  Integer sums, so the totals do not depend on the flush order.
+__global__ void k_fold_counts(DevCounters *cnt) {
+  const int lane = threadIdx.x & 31, q = threadIdx.x >> 5;
+  if (q > CNT_FB) return;
+  unsigned long long t = 0;
+  for (int r = lane; r < FDF_CNT_STRIPES; r += 32) {
+    t += cnt->stripes[r][q];
+    cnt->stripes[r][q] = 0ull;
+  }
+  t = warp_sum_u64(t);
+  if (lane == 0 && t) {
+    switch (q) {
+      case CNT_LOST: cnt->removed_lost += t; break;
+      case CNT_OOB: cnt->removed_oob += t; break;
+      case CNT_EVALS: cnt->evals += t; break;
+      case CNT_EVALS_TOTAL: cnt->evals_total += t; break;
+      case CNT_LOST_TOTAL: cnt->lost_total += t; break;
+      default: cnt->fallbacks += t; cnt->fallbacks_total += t; break;
+    }
+  }
+}
+
 }  // namespace
+
+void launch_fold_counts(DevCounters *cnt, cudaStream_t s) { k_fold_counts<<<1, 32 * (CNT_FB + 1), 0, s>>>(cnt); }
 
 void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
                    const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *count,
