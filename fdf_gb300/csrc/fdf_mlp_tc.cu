@@ -93,6 +93,27 @@ __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
 
+// Issues the load of 16 consecutive FP32 accumulator columns of this thread's TMEM lane; r is
+// undefined until tmem_wait_ld(r).
+__device__ __forceinline__ void tmem_ld16_issue(unsigned taddr, unsigned (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+// Waits for this thread's outstanding tcgen05.ld; r passes through the wait so that the compiler
+// schedules no use of it before.
+__device__ __forceinline__ void tmem_wait_ld(unsigned (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15])
+               :
+               : "memory");
+}
+
 // 16 consecutive FP32 accumulator columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
   unsigned r[16];
@@ -223,17 +244,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     return !bad;
   };
   // bias + SiLU of the 128 accumulator columns (b: half-biases), stored as the next layer's A operand
-  auto epilogue = [&](const float *b) {
-#pragma unroll 1
-    for (int c = 0; c < 8; ++c) {
-      float v[16];
-      tmem_ld16(tmem + lane_base + (unsigned)(16 * c), v);
-      unsigned w[8];
+  // (the next chunk's TMEM load is in flight while a chunk is converted)
+  auto chunk = [&](const unsigned (&r)[16], const float *b, int c) {
+    unsigned w[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-        w[q] = pack2(silu_half(v[2 * q], b[16 * c + 2 * q]), silu_half(v[2 * q + 1], b[16 * c + 2 * q + 1]));
-      *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
-      *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
+    for (int q = 0; q < 8; ++q)
+      w[q] = pack2(silu_half(__uint_as_float(r[2 * q]), b[16 * c + 2 * q]),
+                   silu_half(__uint_as_float(r[2 * q + 1]), b[16 * c + 2 * q + 1]));
+    *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
+  };
+  auto epilogue = [&](const float *b) {
+    unsigned ra[16], rb[16];
+    tmem_ld16_issue(tmem + lane_base, ra);
+    tmem_wait_ld(ra);
+#pragma unroll 1
+    for (int c = 0; c < 8; c += 2) {
+      tmem_ld16_issue(tmem + lane_base + (unsigned)(16 * (c + 1)), rb);
+      chunk(ra, b, c);
+      tmem_wait_ld(rb);
+      if (c + 2 < 8) tmem_ld16_issue(tmem + lane_base + (unsigned)(16 * (c + 2)), ra);
+      chunk(rb, b, c + 1);
+      if (c + 2 < 8) tmem_wait_ld(ra);
     }
   };
   auto load_inputs = [&](long long tile, float &x, float &y, float &z) {
