@@ -19,7 +19,7 @@ struct LocatorState {
   float *bias = nullptr;
   MlpNorm norm{};
   long long adam_t = 0;
-  float far_cells = 1.0f;             // particles at least this far past their cell get a guess
+  float far_cells = 2.0f;             // particles at least this far past their cell get a guess
   // per-particle buffers of the learned form's locate
   unsigned int *pending = nullptr;    // [cap]: slots that left their previous cell, in slot order
   unsigned int *pflag = nullptr;      // [cap+1]: their flags, then the flags' exclusive scan

@@ -76,7 +76,7 @@ typedef struct {
  * threshold plus the cell's overlap margin (the largest gap between the cell's face planes
  * and the planes of the same grid surfaces on the neighbouring patches), within
  * FDF_GUESS_REACH = 16 cells of the previous cell in each index; otherwise the reference
- * walk from the previous cell decides.  Particles that stay within about a cell of their
+ * walk from the previous cell decides.  Particles that stay within about two cells of their
  * previous cell skip the network (fdf_LocatorSetMinDistance).  Cells, weights and statuses are
  * then those of the FP32 form except where the reference's own result depends on where its
  * walk starts. */
@@ -224,7 +224,8 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
 /* Which particles the learned form asks the network: after the reference's first evaluation
  * (in the previous cell), a particle estimated at least `cells` cells past that cell (from the
  * evaluation's face distances) gets a guess; a nearer one continues the reference walk at once.
- * Default 1.0; 0 asks for every particle that left its cell.  Results do not depend on it. */
+ * Default 2.0 (nearer particles cost more walk evaluations from a guess than from their previous
+ * cell); 0 asks for every particle that left its cell.  Results do not depend on it. */
 int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells);
 /* Running totals of the learned form: particles given a guess, guesses whose walk was
  * kept, evaluations made by the walks from the guesses, and by the reference walks that

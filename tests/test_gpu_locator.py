@@ -179,7 +179,7 @@ def test_learned_form_identical_to_fp32_form(pipe_runs):
 def test_trained_locator_shortens_walk(pipe_runs):
     """Asking the network for every particle that left its cell: the trained network needs far
     fewer walk evaluations than the untrained one; the default policy asks only for particles
-    a cell or more away."""
+    two cells or more away and makes fewer walk evaluations than the FP32 form's walk."""
     _, r = pipe_runs
     ps = r["fp32"][3]
     e = {k: r[k][4] / ps for k in ("fp32", "learned", "learned_all", "untrained")}
@@ -192,3 +192,4 @@ def test_trained_locator_shortens_walk(pipe_runs):
     assert taken > 0.5 * asked
     assert e["learned_all"] < e["untrained"]
     assert st["learned"][0] < st["learned_all"][0]
+    assert e["learned"] < e["fp32"]
