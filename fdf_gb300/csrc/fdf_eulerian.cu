@@ -393,7 +393,9 @@ void eulerian_free(FdfContext *ctx) {
   cfree(ctx->c2c_table);
   cfree(ctx->ucont);
   ctx->c2c_rc = FDF_SUCCESS;
+  ctx->c2c_msg.clear();
   ctx->c2c_flipped = 0;
+  ctx->c2c_half = false;
 }
 
 extern "C" {
