@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from fdf_gb300 import workloads as W
-from fdf_gb300.context import FORM_FP32, PetscError, PicContext
+from fdf_gb300.context import FORM_FP32, FORM_PLAIN_FP64, PetscError, PicContext
 from oracle import oracle as O
 from tests import pyref_metrics as R
 from tests.parity_util import assert_swarm_bitwise, from_oracle_swarm, to_oracle_swarm
@@ -165,7 +165,7 @@ def _converted_workload(wl):
 def test_particle_path_on_converted_field_matches_oracle(ctx):
     wl = W.config_sinusoidal(IM=12, JM=10, KM=24, n=3000, cfl=1.0, steps=3)
     ucont, wl2 = _converted_workload(wl)
-    ctx.load_workload(wl)
+    ctx.load_workload(wl, form=FORM_PLAIN_FP64)
     ctx.set_ucont(ucont)
     ctx.contra2cart()
     s0 = ctx.get_swarm()
@@ -217,3 +217,36 @@ def test_full_size_grid_bitwise_and_uniform_flow(ctx):
     assert_bitwise(got, want[:KM, :JM, :IM], "full-size ucat")
     err = np.abs(got[1:, 1:, 1:] - u).max()
     assert err < 1e-12 * np.abs(u).max(), err
+
+
+def test_contra2cart_before_every_step(ctx):
+    """The coupled pattern: new face velocities converted before every step.  Steps replayed
+    from the captured step graph (fdf_AdvanceSteps) and eager steps (fdf_AdvanceStep) both read
+    that step's converted ucat, bit for bit like the oracle fed the oracle's Contra2Cart."""
+    wl = W.config_sinusoidal(IM=12, JM=10, KM=24, n=3000, cfl=1.0, steps=4)
+    base, _ = _node_field_fluxes(wl.coor, W.field_taylor_green)
+    fluxes = [base * (1.0 + 0.25 * t) for t in range(wl.steps)]
+    g = O.Grid(wl.coor)
+    csi, eta, zet, _, _ = O.grid_metrics(g)
+    IM, JM, KM = wl.dims
+    outs = []
+    for replay in (True, False):
+        ctx.load_workload(wl, form=FORM_PLAIN_FP64)
+        s0 = ctx.get_swarm()
+        ctx.initial_setup()
+        os_ = to_oracle_swarm(s0)
+        sim = O.Simulation(g, wl.ucat_node_sized(), os_, wl.dt)
+        sim.initial_setup()
+        for t in range(wl.steps):
+            ctx.set_ucont(fluxes[t])
+            ctx.contra2cart()
+            if replay:
+                ctx.steps(1)
+            else:
+                ctx.step()
+            sim.ucat = np.ascontiguousarray(O.contra2cart(g, fluxes[t], csi, eta, zet, sim.ucat))
+            sim.step()
+        got = ctx.get_swarm()
+        assert_swarm_bitwise(got, from_oracle_swarm(os_), f"coupled steps (replay={replay})")
+        outs.append(got)
+    assert_swarm_bitwise(outs[0], outs[1], "graph replay against eager steps")
