@@ -165,6 +165,17 @@ class PicContext:
         """ucat of the interior cells from the face velocity, on the device (stream-ordered)."""
         self._check(self.lib.fdf_Contra2Cart(self.h))
 
+    def contra2cart_device(self, ucont):
+        """Contra2Cart reading a CUDA float64 tensor [KM+1][JM+1][IM+1][3] in place (no copy).
+        The tensor's pending writes on PyTorch's current stream are waited for first."""
+        import torch
+        IM, JM, KM = self.dims
+        if not (isinstance(ucont, torch.Tensor) and ucont.is_cuda and ucont.dtype == torch.float64
+                and ucont.is_contiguous() and tuple(ucont.shape) == (KM + 1, JM + 1, IM + 1, 3)):
+            raise ValueError("ucont must be a contiguous CUDA float64 tensor [KM+1][JM+1][IM+1][3]")
+        torch.cuda.current_stream(ucont.device).synchronize()
+        self._check(self.lib.fdf_Contra2CartDevice(self.h, ctypes.c_void_p(ucont.data_ptr())))
+
     def set_form(self, form: int):
         """FORM_PLAIN_FP64 (bit-exact), FORM_FP32 (precision form) or FORM_LEARNED_FP32 (precision
         form with the learned start cell); applies at the next set_swarm / seed_particles."""

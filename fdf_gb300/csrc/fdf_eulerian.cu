@@ -431,20 +431,22 @@ int fdf_SetUcont(FdfContext *ctx, const double *ucont) {
   return FDF_SUCCESS;
 }
 
-int fdf_Contra2Cart(FdfContext *ctx) {
-  if (!ctx) return FDF_ERR_ARG_NULL;
-  if (!ctx->has_grid || !ctx->ucont)   // setup.c:1311-1313
-    return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_Contra2Cart: requires the grid and the face velocity (fdf_SetUcont)");
+}  // extern "C"
+
+namespace {
+
+// The conversion of a face-velocity array in device memory (the context's copy or the caller's).
+int contra2cart_from(FdfContext *ctx, const double *ucont) {
   CU(cudaSetDevice(ctx->device));
   int r = ensure_c2c_table(ctx);
   if (r) return r;
   const bool prof = ctx->profiling;
   const size_t e0 = prof ? record_event(ctx, ctx->stream) : 0;
   if (ctx->c2c_half)
-    k_contra2cart<true><<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ctx->ucont, ctx->c2c_table, ctx->g,
-                                                                          ctx->ucat, ctx->ucat32);
+    k_contra2cart<true><<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ucont, ctx->c2c_table, ctx->g, ctx->ucat,
+                                                                          ctx->ucat32);
   else
-    k_contra2cart<false><<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ctx->ucont, ctx->c2c_table, ctx->g,
+    k_contra2cart<false><<<blocks_of(ctx->g.Nc, 256), 256, 0, ctx->stream>>>(ucont, ctx->c2c_table, ctx->g,
                                                                            ctx->ucat, ctx->ucat32);
   CHECK_LAUNCH();
   ctx->launches += 1;
@@ -454,6 +456,27 @@ int fdf_Contra2Cart(FdfContext *ctx) {
   }
   ctx->has_ucat = true;
   return FDF_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdf_Contra2Cart(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->has_grid || !ctx->ucont)   // setup.c:1311-1313
+    return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_Contra2Cart: requires the grid and the face velocity (fdf_SetUcont)");
+  return contra2cart_from(ctx, ctx->ucont);
+}
+
+int fdf_Contra2CartDevice(FdfContext *ctx, const double *ucont_device) {
+  if (!ctx || !ucont_device) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_Contra2CartDevice: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_Contra2CartDevice: call fdf_SetGrid first");
+  cudaPointerAttributes at{};
+  CU(cudaPointerGetAttributes(&at, ucont_device));
+  if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != ctx->device)
+    return fail(ctx, FDF_ERR_ARG_WRONG, "fdf_Contra2CartDevice: the face velocity is not in this context's device memory");
+  return contra2cart_from(ctx, ucont_device);
 }
 
 int fdf_GetUcat(FdfContext *ctx, double *ucat, int node_sized) {

@@ -115,6 +115,11 @@ int fdf_SetUcont(FdfContext *ctx, const double *ucont);
  * without fdf_SetUcont, the errors of fdf_GetGridMetrics, FDF_ERR_FLOP_COUNT (a cell's
  * |det| < 1e-18; ucat is then left unchanged). */
 int fdf_Contra2Cart(FdfContext *ctx);
+/* Contra2Cart from a face velocity already in device memory (a solver that keeps lUcont on the
+ * GPU): ucont_device, node-sized [KM+1][JM+1][IM+1][3] on the context's device, is read in place,
+ * without a copy, on the context stream (fdf_GetStream): the caller orders its writes of the
+ * array before the call.  FDF_ERR_ARG_WRONG when the pointer is not memory of that device. */
+int fdf_Contra2CartDevice(FdfContext *ctx, const double *ucont_device);
 
 /* Selects the form used by the next fdf_SetSwarm (default PLAIN_FP64). */
 int fdf_SetForm(FdfContext *ctx, int form);

@@ -250,3 +250,22 @@ def test_contra2cart_before_every_step(ctx):
         assert_swarm_bitwise(got, from_oracle_swarm(os_), f"coupled steps (replay={replay})")
         outs.append(got)
     assert_swarm_bitwise(outs[0], outs[1], "graph replay against eager steps")
+
+
+def test_contra2cart_from_device_memory(ctx):
+    """fdf_Contra2CartDevice reads a face velocity that is already on the GPU (a CUDA tensor)
+    in place: the same bits as the host upload; host memory is refused (62)."""
+    import torch
+    coor = GRIDS["bent_pipe"]()
+    KM, JM, IM = (s - 1 for s in coor.shape[:3])
+    ucont = np.random.default_rng(31).uniform(-1.0, 1.0, size=coor.shape)
+    ctx.set_grid(coor)
+    ctx.contra2cart_device(torch.from_numpy(ucont).cuda())
+    got = _ucat_cells(ctx)
+    g = O.Grid(coor)
+    csi, eta, zet, _, _ = O.grid_metrics(g)
+    want = O.contra2cart(g, ucont, csi, eta, zet)
+    assert_bitwise(got[1:, 1:, 1:], want[1:KM, 1:JM, 1:IM], "device-resident face velocity")
+    with pytest.raises(PetscError) as e:
+        ctx._check(ctx.lib.fdf_Contra2CartDevice(ctx.h, ucont.ctypes.data))
+    assert e.value.code == 62
