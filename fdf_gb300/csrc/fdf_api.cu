@@ -63,8 +63,8 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox); cfree(ctx->mom); cfree(ctx->mom32);
   eulerian_free(ctx);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
-  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm);
-  cfree(ctx->cell_start); cfree(ctx->cursor); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank);
+  cfree(ctx->cell_start); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
   locator_free(ctx);
   for (auto &gx : ctx->step_graph)
     if (gx) cudaGraphExecDestroy(gx);
@@ -89,7 +89,7 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   CU(cudaStreamSynchronize(ctx->stream));
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk); cfree(ctx->cell_start);
-  cfree(ctx->cursor); cfree(ctx->scan_sums);
+  cfree(ctx->scan_sums);
   cfree(ctx->table32); cfree(ctx->ucat32); cfree(ctx->corner32); cfree(ctx->count32); cfree(ctx->avg32);
   cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->mom); cfree(ctx->mom32);
   eulerian_free(ctx);
@@ -118,7 +118,6 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   CU(cudaMalloc((void **)&ctx->fk32, 4ull * nfk));
   CU(cudaMemsetAsync(ctx->ucat32, 0, 12ull * Nc, ctx->stream));
   CU(cudaMalloc((void **)&ctx->cell_start, 4ull * (Nc + 2)));
-  CU(cudaMalloc((void **)&ctx->cursor, 4ull * (Nc + 1)));
   CU(cudaMalloc((void **)&ctx->scan_sums, 4ull * scan_scratch_words(Nc + 2)));
   CU(cudaMemsetAsync(ctx->cell_start, 0, 4ull * (Nc + 2), ctx->stream));
   CU(cudaMemsetAsync(ctx->ucat, 0, 24ull * Nc, ctx->stream));
@@ -223,7 +222,7 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   if (capacity <= ctx->cap && ctx->swarm_mem) return FDF_SUCCESS;
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
-  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->staging);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->staging);
   int cap = (int)(capacity < 256 ? 256 : capacity);   // never zero: the sort always has scratch
   size_t per = swarm_bytes_per_buf(cap);
   CU(cudaMalloc(&ctx->swarm_mem, 2 * per));
@@ -231,6 +230,7 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   carve_swarm((char *)ctx->swarm_mem + per, cap, ctx->buf[1]);
   CU(cudaMalloc((void **)&ctx->keys, 4ull * cap));
   CU(cudaMalloc((void **)&ctx->perm, 4ull * cap));
+  CU(cudaMalloc((void **)&ctx->rank, 4ull * cap));
   ctx->staging_bytes = (size_t)cap * 120 + 1024;
   CU(cudaMalloc(&ctx->staging, ctx->staging_bytes));
   ctx->cap = cap;
@@ -436,7 +436,6 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   // zero the per-step counters; the error word stays set until the swarm is replaced
   CU(cudaMemsetAsync(ctx->cnt, 0, offsetof(DevCounters, err), s));
   CU(cudaMemsetAsync(ctx->cell_start, 0, 4ull * (g.Nc + 2), s));
-  CU(cudaMemsetAsync(ctx->cursor, 0, 4ull * (g.Nc + 1), s));
   const bool prof = ctx->profiling;
   SwarmBuf &src = ctx->buf[ctx->cur];
   SwarmBuf &dst = ctx->buf[1 - ctx->cur];
@@ -448,7 +447,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     // start cell and walk from there (k_locate32_guess)
     LocatorState &L = ctx->loc;
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
-                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, L.pflag, L.far_cells, s);
+                    ctx->cnt, ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, L.pflag, L.far_cells, s);
     exclusive_scan_u32(L.pflag, (long long)ctx->cap + 1, L.scan_sums, s);
     launch_compact_pending(L.pflag, ctx->cap, L.pending, ctx->cnt, s);
     eg0 = prof ? record_event(ctx, s) : 0;
@@ -456,12 +455,12 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
                  L.guess, ctx->num_sms, &ctx->cnt->err, s);
     eg1 = prof ? record_event(ctx, s) : 0;
     launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
-                          ctx->keys, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
+                          ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
   } else if (f32) {
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
-                    ctx->cnt, ctx->keys, ctx->cell_start, ctx->sentinel, nullptr, 0.f, s);
+                    ctx->cnt, ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, nullptr, 0.f, s);
   } else {
-    launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys,
+    launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys, ctx->rank,
                   ctx->cell_start, ctx->sentinel, s);
   }
   size_t e1 = prof ? record_event(ctx, s) : 0;
@@ -476,7 +475,7 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
     launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->side);
   size_t c1 = prof ? record_event(ctx, ctx->side) : 0;
   CU(cudaEventRecord(ctx->ev_corner, ctx->side));
-  launch_scatter_slots(ctx->keys, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start, ctx->cursor,
+  launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start,
                        ctx->perm, s);
   launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
   size_t e2 = prof ? record_event(ctx, s) : 0;

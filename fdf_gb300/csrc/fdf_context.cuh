@@ -54,8 +54,8 @@ struct FdfContext {
   int cur = 0;
   void *swarm_mem = nullptr;
   unsigned int *keys = nullptr, *perm = nullptr;   // [cap]: cell key per slot, sorted slot -> previous slot
+  unsigned int *rank = nullptr;                    // [cap]: rank of the slot's particle within its new cell
   unsigned int *cell_start = nullptr;              // [Nc+2]: histogram, then its exclusive scan
-  unsigned int *cursor = nullptr;                  // [Nc+1]: per-cell slot cursors of the counting sort
   unsigned int *scan_sums = nullptr;
   DevCounters *cnt = nullptr;
   void *staging = nullptr;

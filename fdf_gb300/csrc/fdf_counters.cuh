@@ -24,6 +24,18 @@ __device__ __forceinline__ void warp_histogram(unsigned int hkey, unsigned int *
   if (hkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(count + hkey, (unsigned int)__popc(peers));
 }
 
+// The same histogram, returning each particle's rank among the particles of its key: a warp's
+// particles of one key take consecutive ranks after the count the key had (the atomic's old
+// value).  The rank is undefined for hkey = all ones.
+__device__ __forceinline__ unsigned int warp_histogram_rank(unsigned int hkey, unsigned int *__restrict__ count) {
+  const unsigned int peers = __match_any_sync(0xffffffffu, hkey);
+  const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+  unsigned int base = 0u;
+  if (hkey != 0xffffffffu && lane == leader) base = atomicAdd(count + hkey, (unsigned int)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + (unsigned int)__popc(peers & ((1u << lane) - 1u));
+}
+
 // Adds the block's counters to cnt.  Every thread of the block calls it (blockDim.x a
 // multiple of 32, at most 1024).
 __device__ __forceinline__ void block_flush_counts(const LocCounts &m, DevCounters *cnt) {

@@ -337,6 +337,7 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_LOC_MIN_BLOCKS) k_locate3
                                                   int reset_first, const double *__restrict__ bbox,
                                                   const float *__restrict__ fbox, int drop_removed,
                                                   DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                  unsigned int *__restrict__ rank,
                                                   unsigned int *__restrict__ count, unsigned int sentinel,
                                                   unsigned int *__restrict__ pending, int n_cap, float far_cells) {
   const int n = cnt->n_sorted;
@@ -403,7 +404,8 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_LOC_MIN_BLOCKS) k_locate3
     pending[s] = wait ? 1u : 0u;
     if (s == n_cap - 1) pending[n_cap] = 0u;
   }
-  warp_histogram(hkey, count);
+  const unsigned int r = warp_histogram_rank(hkey, count);
+  if (hkey != 0xffffffffu) rank[s] = r;
   block_flush_counts(m, cnt);
 }
 
@@ -432,6 +434,7 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(Sw
                                                         const double *__restrict__ bbox,
                                                         const float *__restrict__ fbox, int drop_removed,
                                                         DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                        unsigned int *__restrict__ rank,
                                                         unsigned int *__restrict__ count, unsigned int sentinel,
                                                         const unsigned int *__restrict__ pending,
                                                         int *__restrict__ guess) {
@@ -443,8 +446,9 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(Sw
   for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < npend; base += stride) {
     const long long t = base + lane;
     unsigned int hkey = 0xffffffffu;
+    int s = 0;
     if (t < npend) {
-      const int s = (int)pending[t];
+      s = (int)pending[t];
       const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
       int pi, pj, pk;
       cell_ijk(g, (unsigned int)b.cell[s], pi, pj, pk);
@@ -483,7 +487,8 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(Sw
         guess[t] = -1;   // the reference walk from P1 decides (k_locate32_fallback)
       }
     }
-    warp_histogram(hkey, count);
+    const unsigned int r = warp_histogram_rank(hkey, count);
+    if (hkey != 0xffffffffu) rank[s] = r;
   }
   block_flush_counts(m, cnt);
   block_add_u64(acc, &cnt->guess_taken_total);
@@ -501,6 +506,7 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_fallback
                                                            const double *__restrict__ bbox,
                                                            const float *__restrict__ fbox, int drop_removed,
                                                            DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                           unsigned int *__restrict__ rank,
                                                            unsigned int *__restrict__ count, unsigned int sentinel,
                                                            const unsigned int *__restrict__ pending,
                                                            const int *__restrict__ guess) {
@@ -524,8 +530,9 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_fallback
     __syncwarp();
     for (int base = 0; base < nq; base += 32) {
       unsigned int hkey = 0xffffffffu;
+      int s = 0;
       if (base + lane < nq) {
-        const int s = (int)pending[q[base + lane]];
+        s = (int)pending[q[base + lane]];
         const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
         Walk32 w;
         w.err = 0u;
@@ -544,7 +551,8 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_fallback
         if (key < sentinel) hkey = key;
         else if (!drop_removed) hkey = sentinel;
       }
-      warp_histogram(hkey, count);
+      const unsigned int r = warp_histogram_rank(hkey, count);
+      if (hkey != 0xffffffffu) rank[s] = r;
     }
     __syncwarp();
   }
@@ -780,16 +788,16 @@ void launch_build_table32(const double *planes, const double *coor, GridDims g, 
 
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                     unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
-                     float far_cells, cudaStream_t s) {
+                     unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
+                     unsigned int *pending, float far_cells, cudaStream_t s) {
   constexpr int th = FDF_LOC_THREADS;
   if (pending)
     k_locate32<true><<<blocks_for(n_cap, th), th, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed, bbox,
-                                                          fbox, drop_removed, cnt, keys, count, sentinel, pending,
-                                                          n_cap, far_cells);
+                                                          fbox, drop_removed, cnt, keys, rank, count, sentinel,
+                                                          pending, n_cap, far_cells);
   else
     k_locate32<false><<<blocks_for(n_cap, th), th, 0, s>>>(b, g, table, planes, (float)dt, advect, drop_removed,
-                                                           bbox, fbox, drop_removed, cnt, keys, count, sentinel,
+                                                           bbox, fbox, drop_removed, cnt, keys, rank, count, sentinel,
                                                            nullptr, n_cap, 0.f);
 }
 
@@ -800,7 +808,7 @@ void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *l
 
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
                            const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                           unsigned int *keys, unsigned int *count, unsigned int sentinel,
+                           unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
                            const unsigned int *pending, int *guess, int num_sms, cudaStream_t s) {
   // grid-stride kernels: one wave of resident blocks, so that no SM runs a partial last wave
   static int resident[2] = {0, 0}, res_device = -1;
@@ -817,10 +825,10 @@ void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float
     if (blocks > need) blocks = need;
     return (unsigned)(blocks < 1 ? 1 : blocks);
   };
-  k_locate32_guess<<<wave(resident[0]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, count,
-                                                     sentinel, pending, guess);
+  k_locate32_guess<<<wave(resident[0]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, rank,
+                                                     count, sentinel, pending, guess);
   k_locate32_fallback<<<wave(resident[1]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys,
-                                                        count, sentinel, pending, guess);
+                                                        rank, count, sentinel, pending, guess);
 }
 
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,

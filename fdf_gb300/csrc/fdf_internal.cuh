@@ -157,9 +157,10 @@ void launch_center_to_corner(const double *ucat, GridDims g, double *corner, con
                              unsigned long long *nodes_done, cudaStream_t s);
 // Advect + walk.  Writes the new cell (or -1) and status in place, keys[s] = cell
 // or sentinel (LOST / removed), and histograms the kept keys into count[] (bucket
-// Nc = LOST particles, counted only when keep_lost).
+// Nc = LOST particles, counted only when keep_lost), with rank[s] = the particle's rank
+// among its key's particles (rank may be null).
 void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
-                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys,
+                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *rank,
                    unsigned int *count, unsigned int sentinel, cudaStream_t s);
 // sorted slot s takes the particle perm[s]; n = cell_start[Nc+1] (read on the device)
 void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g,
@@ -174,8 +175,10 @@ void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_star
 size_t scan_scratch_words(long long count);
 long long scan_max_count();
 void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums, cudaStream_t s);
-void launch_scatter_slots(const unsigned int *keys, int n_cap, const DevCounters *cnt, unsigned int sentinel,
-                          int keep_lost, const unsigned int *cell_start, unsigned int *cursor, unsigned int *perm,
+// perm[cell_start[key] + rank[s]] = s for every kept particle (keys and ranks from the locate
+// kernels' histogram).
+void launch_scatter_slots(const unsigned int *keys, const unsigned int *rank, int n_cap, const DevCounters *cnt,
+                          unsigned int sentinel, int keep_lost, const unsigned int *cell_start, unsigned int *perm,
                           cudaStream_t s);
 void launch_order_segments(const unsigned int *cell_start, int nseg, const long long *pid, unsigned int *perm,
                            cudaStream_t s);
@@ -198,8 +201,8 @@ void launch_build_table32(const double *planes, const double *coor, GridDims g, 
 // for s <= n_cap; the others are located here).
 void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                     unsigned int *keys, unsigned int *count, unsigned int sentinel, unsigned int *pending,
-                     float far_cells, cudaStream_t s);
+                     unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
+                     unsigned int *pending, float far_cells, cudaStream_t s);
 // The learned form's pending list from the scanned flags (sets cnt->pending).
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
                             cudaStream_t s);
@@ -208,7 +211,7 @@ void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *l
 // to -1 in between).
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
                            const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                           unsigned int *keys, unsigned int *count, unsigned int sentinel,
+                           unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
                            const unsigned int *pending, int *guess, int num_sms, cudaStream_t s);
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
                                unsigned long long *nodes_done, cudaStream_t s);

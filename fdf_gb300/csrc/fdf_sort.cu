@@ -5,7 +5,8 @@
 //   2. an exclusive scan turns count[0..Nc+1) into cell_start[0..Nc+1]: cell c
 //      owns sorted slots [cell_start[c], cell_start[c+1]); bucket Nc holds the LOST
 //      particles the initial setup keeps, and removed particles get no slot;
-//   3. each particle takes slot cell_start[key] + (atomic cursor of its cell);
+//   3. each particle takes slot cell_start[key] + its rank within its cell, which the
+//      histogram atomic of step 1 returned;
 //   4. each cell's slots are then ordered by (PID, previous slot), so the final
 //      order -- and every later sum -- is the same on every run, whatever order
 //      the atomics took, and does not depend on the history of the swarm.
@@ -108,29 +109,22 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(unsigned int *__res
   }
 }
 
-// Slot of every kept particle: cell_start[key] + its rank among the particles of the
-// same cell that reached the cursor before it (warp-aggregated atomics).
-__global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__restrict__ keys, const DevCounters *cnt,
+// Slot of every kept particle: cell_start[key] + its rank among the particles of the same
+// key, which the locate kernels took from their histogram atomics.
+__global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__restrict__ keys,
+                                                      const unsigned int *__restrict__ rank, const DevCounters *cnt,
                                                       unsigned int sentinel, int keep_lost,
                                                       const unsigned int *__restrict__ cell_start,
-                                                      unsigned int *__restrict__ cursor,
                                                       unsigned int *__restrict__ perm) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned int key = 0xffffffffu;
-  if (s < n) {
-    key = keys[s];
-    if (key >= sentinel) key = keep_lost ? sentinel : 0xffffffffu;
+  if (s >= n) return;
+  unsigned int key = keys[s];
+  if (key >= sentinel) {
+    if (!keep_lost) return;
+    key = sentinel;
   }
-  const unsigned int peers = __match_any_sync(0xffffffffu, key);
-  if (key == 0xffffffffu) return;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  const unsigned int rank = __popc(peers & ((1u << lane) - 1u));
-  unsigned int base = 0;
-  if (lane == leader) base = atomicAdd(cursor + key, (unsigned int)__popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  perm[cell_start[key] + base + rank] = (unsigned int)s;
+  perm[cell_start[key] + rank[s]] = (unsigned int)s;
 }
 
 // Orders every cell's slots by (PID, previous slot) -- or by previous slot alone when
@@ -248,13 +242,13 @@ void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums,
   k_scan_apply<<<(unsigned)blocks, SCAN_THREADS, 0, s>>>(data, count, sums);
 }
 
-void launch_scatter_slots(const unsigned int *keys, int n_cap, const DevCounters *cnt, unsigned int sentinel,
-                          int keep_lost, const unsigned int *cell_start, unsigned int *cursor, unsigned int *perm,
+void launch_scatter_slots(const unsigned int *keys, const unsigned int *rank, int n_cap, const DevCounters *cnt,
+                          unsigned int sentinel, int keep_lost, const unsigned int *cell_start, unsigned int *perm,
                           cudaStream_t s) {
   int th = 256;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
-  k_scatter_slots<<<blocks, th, 0, s>>>(keys, cnt, sentinel, keep_lost, cell_start, cursor, perm);
+  k_scatter_slots<<<blocks, th, 0, s>>>(keys, rank, cnt, sentinel, keep_lost, cell_start, perm);
 }
 
 void launch_order_segments(const unsigned int *cell_start, int nseg, const long long *pid, unsigned int *perm,

@@ -37,7 +37,8 @@ using fdfx::mul;
 __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
                                                 double dt, int advect, int reset_first, const double *__restrict__ bbox,
                                                 int drop_removed, DevCounters *cnt, unsigned int *__restrict__ keys,
-                                                unsigned int *__restrict__ count, unsigned int sentinel) {
+                                                unsigned int *__restrict__ rank, unsigned int *__restrict__ count,
+                                                unsigned int sentinel) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
@@ -133,7 +134,8 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locat
     if (key < sentinel) hkey = key;
     else if (!drop_removed) hkey = sentinel;   // the initial setup keeps LOST particles, at the end
   }
-  warp_histogram(hkey, count);
+  const unsigned int r = warp_histogram_rank(hkey, count);
+  if (rank && hkey != 0xffffffffu) rank[s] = r;
   LocCounts m;
   m.lost = my_lost; m.oob = my_oob; m.evals = my_evals; m.done = my_done; m.lost_total = my_lost_total;
   m.err = my_err;
@@ -168,13 +170,13 @@ __global__ void k_fold_counts(DevCounters *cnt) {
 void launch_fold_counts(DevCounters *cnt, cudaStream_t s) { k_fold_counts<<<1, 32 * (CNT_FB + 1), 0, s>>>(cnt); }
 
 void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
-                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *count,
-                   unsigned int sentinel, cudaStream_t s) {
+                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *rank,
+                   unsigned int *count, unsigned int sentinel, cudaStream_t s) {
   // advect and drop_removed are both set by the fused step, which also resets statuses first.
   int reset_first = drop_removed;
   constexpr int th = FDF_LOC_THREADS;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
-  k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, count,
+  k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, rank, count,
                                  sentinel);
 }
