@@ -429,7 +429,7 @@ __global__ void k_compact_pending(const unsigned int *__restrict__ scan, int n_c
 // margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise guess[t] becomes
 // -1 and k_locate32_fallback continues the reference walk from P1.  Grid-stride over the
 // list, warp-uniform trip count.
-__global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(FDF_GUESS_THREADS, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                         const double *__restrict__ planes,
                                                         const double *__restrict__ bbox,
                                                         const float *__restrict__ fbox, int drop_removed,
@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(Sw
 // scans a chunk of 32 x 32 list entries, queues the failed ones in shared memory and walks
 // them 32 at a time, so every lane has a particle.
 constexpr int FB_CHUNK = 1024;
-__global__ void __launch_bounds__(256, FDF_GUESS_MIN_BLOCKS) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
+__global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                            const double *__restrict__ planes,
                                                            const double *__restrict__ bbox,
                                                            const float *__restrict__ fbox, int drop_removed,
@@ -815,19 +815,19 @@ void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float
   int dev = 0;
   cudaGetDevice(&dev);
   if (res_device != dev) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_locate32_guess, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_locate32_guess, FDF_GUESS_THREADS, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_locate32_fallback, 256, 0);
     res_device = dev;
   }
-  const long long need = ((long long)n_cap + 255) / 256;
-  auto wave = [&](int r) {
+  auto wave = [&](int r, int th) {
+    const long long need = ((long long)n_cap + th - 1) / th;
     long long blocks = (long long)num_sms * (r > 0 ? r : 1);
     if (blocks > need) blocks = need;
     return (unsigned)(blocks < 1 ? 1 : blocks);
   };
-  k_locate32_guess<<<wave(resident[0]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, rank,
-                                                     count, sentinel, pending, guess);
-  k_locate32_fallback<<<wave(resident[1]), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys,
+  k_locate32_guess<<<wave(resident[0], FDF_GUESS_THREADS), FDF_GUESS_THREADS, 0, s>>>(
+      b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, rank, count, sentinel, pending, guess);
+  k_locate32_fallback<<<wave(resident[1], 256), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys,
                                                         rank, count, sentinel, pending, guess);
 }
 

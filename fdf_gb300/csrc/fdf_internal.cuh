@@ -147,6 +147,11 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_GUESS_MIN_BLOCKS
 #define FDF_GUESS_MIN_BLOCKS 3
 #endif
+// Threads per block of the walk from the guess (the fallback walk keeps 256: its queues are per
+// block of 8 warps).
+#ifndef FDF_GUESS_THREADS
+#define FDF_GUESS_THREADS 256
+#endif
 
 // ---------------------------------------------------------------- kernels (launchers)
 // Adds the pending block flushes to the counters and clears them (end of a pipeline run).
