@@ -31,6 +31,13 @@ _SIGS = {
     "fdf_GetGridMetrics": (ctypes.c_int, [ctypes.c_void_p] * 6),
     "fdf_SetUcont": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_Contra2Cart": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdf_ResetAllParticleStatuses": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdf_UpdateAllParticlePositions": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdf_LocateAllParticlesInGrid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_CheckAndRemoveLostParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_CheckAndRemoveOutOfBoundsParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fdf_InterpolateAllFieldsToSwarm": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdf_ScatterAllParticleFieldsToEulerFields": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_Contra2CartDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTimeStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),

@@ -268,6 +268,34 @@ class PicContext:
         self._check(self.lib.fdf_GetFaceMomentum(self.h, _ptr(mi), _ptr(mj), _ptr(mk)))
         return mi, mj, mk
 
+    # -- the reference's stages one call at a time (ParticleMotion.c, interpolation.c)
+    def reset_statuses(self):
+        self._check(self.lib.fdf_ResetAllParticleStatuses(self.h))
+
+    def update_positions(self):
+        self._check(self.lib.fdf_UpdateAllParticlePositions(self.h))
+
+    def locate(self) -> FdfStepInfo:
+        info = FdfStepInfo()
+        self._check(self.lib.fdf_LocateAllParticlesInGrid(self.h, ctypes.byref(info)))
+        return info
+
+    def remove_lost(self) -> int:
+        n = ctypes.c_int64()
+        self._check(self.lib.fdf_CheckAndRemoveLostParticles(self.h, ctypes.byref(n)))
+        return n.value
+
+    def remove_out_of_bounds(self) -> int:
+        n = ctypes.c_int64()
+        self._check(self.lib.fdf_CheckAndRemoveOutOfBoundsParticles(self.h, ctypes.byref(n)))
+        return n.value
+
+    def interpolate(self):
+        self._check(self.lib.fdf_InterpolateAllFieldsToSwarm(self.h))
+
+    def scatter(self):
+        self._check(self.lib.fdf_ScatterAllParticleFieldsToEulerFields(self.h))
+
     # -- the hot path
     def initial_setup(self) -> FdfStepInfo:
         info = FdfStepInfo()

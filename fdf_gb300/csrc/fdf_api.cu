@@ -277,6 +277,7 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->cur = 0;
   ctx->swarm_set = true;
+  ctx->layout_ok = false;
   ctx->gen++;
   ctx->swarm_form = ctx->form;
   return FDF_SUCCESS;
@@ -303,6 +304,7 @@ int fdf_SeedParticles(FdfContext *ctx, int64_t n, uint64_t seed, int start_in_ge
   CU(cudaMemcpyAsync(ctx->cnt, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->swarm_set = true;
+  ctx->layout_ok = false;
   ctx->gen++;
   ctx->swarm_form = ctx->form;
   return FDF_SUCCESS;
@@ -415,8 +417,9 @@ long long launches_per_step(const FdfContext *ctx) {
   return 10 + (ctx->swarm_form == FDF_FORM_LEARNED_FP32 ? 7 : 0);
 }
 
-// The shared pipeline of the initial setup (advect=0, drop=0) and a step (1, 1).
-int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
+// The shared pipeline of the initial setup (advect=0, drop=0) and a step (1, 1); locate_only:
+// the walk and the re-sort alone (fdf_LocateAllParticlesInGrid), no interpolation or deposit.
+int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool locate_only = false) {
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no grid: call fdf_SetGrid first");
   if (!ctx->has_ucat) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no ucat: call fdf_SetUcat first");
   if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
@@ -466,28 +469,34 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   size_t e1 = prof ? record_event(ctx, s) : 0;
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
   // the corner field needs only cell_start: compute it beside the slot assignment
-  CU(cudaEventRecord(ctx->ev_scan, s));
-  CU(cudaStreamWaitEvent(ctx->side, ctx->ev_scan, 0));
-  size_t c0 = prof ? record_event(ctx, ctx->side) : 0;
-  if (f32)   // FP32 arithmetic is cheap: every node, no occupancy test
-    launch_center_to_corner32(ctx->ucat32, g, ctx->corner32, nullptr, nullptr, ctx->side);
-  else
-    launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->side);
-  size_t c1 = prof ? record_event(ctx, ctx->side) : 0;
-  CU(cudaEventRecord(ctx->ev_corner, ctx->side));
+  size_t c0 = 0, c1 = 0;
+  if (!locate_only) {
+    CU(cudaEventRecord(ctx->ev_scan, s));
+    CU(cudaStreamWaitEvent(ctx->side, ctx->ev_scan, 0));
+    c0 = prof ? record_event(ctx, ctx->side) : 0;
+    if (f32)   // FP32 arithmetic is cheap: every node, no occupancy test
+      launch_center_to_corner32(ctx->ucat32, g, ctx->corner32, nullptr, nullptr, ctx->side);
+    else
+      launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->side);
+    c1 = prof ? record_event(ctx, ctx->side) : 0;
+    CU(cudaEventRecord(ctx->ev_corner, ctx->side));
+  }
   launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start,
                        ctx->perm, s);
   launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
   size_t e2 = prof ? record_event(ctx, s) : 0;
-  CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
+  if (!locate_only) CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
   size_t e3 = prof ? record_event(ctx, s) : 0;
+  const int gmode = locate_only ? GATHER_COPY : GATHER_INTERP;
   if (f32)
-    launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s);
+    launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s, gmode);
   else
-    launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s);
+    launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s, gmode);
   size_t e4 = prof ? record_event(ctx, s) : 0;
   const long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM;
-  if (f32) {
+  if (locate_only) {
+    // no deposit
+  } else if (f32) {
     float *m = ctx->momentum ? ctx->mom32 : nullptr;
     launch_deposit32(dst, g, ctx->cell_start, ctx->volume, ctx->count32, ctx->avg32, ctx->fi32, ctx->fj32, ctx->fk32,
                      m, m ? m + 3 * nfi : nullptr, m ? m + 3 * (nfi + nfj) : nullptr, s);
@@ -509,14 +518,17 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   }
   if (prof) {
     ctx->ev_spans.push_back({FDF_STAGE_SORT, {e1, e2}});
-    ctx->ev_spans.push_back({FDF_STAGE_CORNER, {c0, c1}});
-    ctx->ev_spans.push_back({FDF_STAGE_WAIT, {e2, e3}});
+    if (!locate_only) {
+      ctx->ev_spans.push_back({FDF_STAGE_CORNER, {c0, c1}});
+      ctx->ev_spans.push_back({FDF_STAGE_WAIT, {e2, e3}});
+    }
     ctx->ev_spans.push_back({FDF_STAGE_GATHER_INTERP, {e3, e4}});
-    ctx->ev_spans.push_back({FDF_STAGE_DEPOSIT, {e4, e5}});
+    if (!locate_only) ctx->ev_spans.push_back({FDF_STAGE_DEPOSIT, {e4, e5}});
   }
   CHECK_LAUNCH();
   ctx->cur = 1 - ctx->cur;
-  ctx->launches += launches_per_step(ctx);
+  ctx->layout_ok = true;
+  ctx->launches += launches_per_step(ctx) - (locate_only ? 2 : 0);
   if (info) {
     DevCounters c{};
     CU(cudaMemcpyAsync(&c, ctx->cnt, DEVCOUNTERS_HEAD, cudaMemcpyDeviceToHost, s));
@@ -534,9 +546,131 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info) {
   return FDF_SUCCESS;
 }
 
+// Re-sorts the held particles by (cell, PID) into the other buffer, dropping the LOST and/or
+// the out-of-bounds ones; cell_start then matches the held particles.
+int resort(FdfContext *ctx, int remove_lost, int remove_oob, int64_t *removed_lost, int64_t *removed_oob) {
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no grid: call fdf_SetGrid first");
+  if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
+  CU(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const GridDims &g = ctx->g;
+  const bool f32 = form_is32(ctx->swarm_form);
+  SwarmBuf &src = ctx->buf[ctx->cur];
+  SwarmBuf &dst = ctx->buf[1 - ctx->cur];
+  CU(cudaMemsetAsync(ctx->cnt, 0, offsetof(DevCounters, err), s));
+  CU(cudaMemsetAsync(ctx->cell_start, 0, 4ull * (g.Nc + 2), s));
+  launch_resort_keys(src, ctx->cap, g, f32 ? 1 : 0, remove_lost, remove_oob, ctx->bbox, ctx->fbox, ctx->cnt,
+                     ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, s);
+  exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
+  launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, 1, ctx->cell_start, ctx->perm, s);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
+  if (f32)
+    launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s, GATHER_COPY);
+  else
+    launch_gather_interp(src, dst, ctx->cap, g, ctx->corner, ctx->perm, ctx->cell_start, ctx->cnt, s, GATHER_COPY);
+  launch_fold_counts(ctx->cnt, s);
+  CHECK_LAUNCH();
+  ctx->launches += 8;
+  ctx->cur = 1 - ctx->cur;
+  ctx->layout_ok = true;
+  DevCounters c{};
+  CU(cudaMemcpyAsync(&c, ctx->cnt, DEVCOUNTERS_HEAD, cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if (removed_lost) *removed_lost = (int64_t)c.removed_lost;
+  if (removed_oob) *removed_oob = (int64_t)c.removed_oob;
+  return FDF_SUCCESS;
+}
+
+int ensure_layout(FdfContext *ctx) { return ctx->layout_ok ? FDF_SUCCESS : resort(ctx, 0, 0, nullptr, nullptr); }
+
 }  // namespace
 
 extern "C" {
+
+int fdf_ResetAllParticleStatuses(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
+  CU(cudaSetDevice(ctx->device));
+  launch_reset_status(ctx->buf[ctx->cur], ctx->cap, ctx->cnt, ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  return FDF_SUCCESS;
+}
+
+int fdf_UpdateAllParticlePositions(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
+  CU(cudaSetDevice(ctx->device));
+  if (form_is32(ctx->swarm_form))
+    launch_advect32(ctx->buf[ctx->cur], ctx->cap, ctx->dt, ctx->cnt, ctx->stream);
+  else
+    launch_advect(ctx->buf[ctx->cur], ctx->cap, ctx->dt, ctx->cnt, ctx->stream);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  return FDF_SUCCESS;
+}
+
+int fdf_LocateAllParticlesInGrid(FdfContext *ctx, FdfStepInfo *info) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  FdfStepInfo local{};
+  return run_pipeline(ctx, 0, 0, info ? info : &local, true);
+}
+
+int fdf_CheckAndRemoveLostParticles(FdfContext *ctx, int64_t *removed) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  return resort(ctx, 1, 0, removed, nullptr);
+}
+
+int fdf_CheckAndRemoveOutOfBoundsParticles(FdfContext *ctx, int64_t *removed) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  return resort(ctx, 0, 1, nullptr, removed);
+}
+
+int fdf_InterpolateAllFieldsToSwarm(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (!ctx->has_ucat) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no ucat: call fdf_SetUcat first");
+  int r = ensure_layout(ctx);
+  if (r) return r;
+  const GridDims &g = ctx->g;
+  SwarmBuf &b = ctx->buf[ctx->cur];
+  if (form_is32(ctx->swarm_form)) {
+    launch_center_to_corner32(ctx->ucat32, g, ctx->corner32, nullptr, nullptr, ctx->stream);
+    launch_gather_interp32(b, b, ctx->cap, g, ctx->corner32, nullptr, ctx->cell_start, ctx->cnt, ctx->stream,
+                           INTERP_KEEP);
+  } else {
+    launch_center_to_corner(ctx->ucat, g, ctx->corner, ctx->cell_start, &ctx->cnt->nodes_total, ctx->stream);
+    launch_gather_interp(b, b, ctx->cap, g, ctx->corner, nullptr, ctx->cell_start, ctx->cnt, ctx->stream,
+                         INTERP_KEEP);
+  }
+  CHECK_LAUNCH();
+  ctx->launches += 2;
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FDF_SUCCESS;
+}
+
+int fdf_ScatterAllParticleFieldsToEulerFields(FdfContext *ctx) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  int r = ensure_layout(ctx);
+  if (r) return r;
+  const GridDims &g = ctx->g;
+  SwarmBuf &b = ctx->buf[ctx->cur];
+  const long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM;
+  if (form_is32(ctx->swarm_form)) {
+    float *m = ctx->momentum ? ctx->mom32 : nullptr;
+    launch_deposit32(b, g, ctx->cell_start, ctx->volume, ctx->count32, ctx->avg32, ctx->fi32, ctx->fj32, ctx->fk32,
+                     m, m ? m + 3 * nfi : nullptr, m ? m + 3 * (nfi + nfj) : nullptr, ctx->stream);
+  } else {
+    double *m = ctx->momentum ? ctx->mom : nullptr;
+    launch_deposit(b, g, ctx->cell_start, ctx->volume, ctx->count, ctx->avg, ctx->fi, ctx->fj, ctx->fk, m,
+                   m ? m + 3 * nfi : nullptr, m ? m + 3 * (nfi + nfj) : nullptr, ctx->stream);
+  }
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  ctx->out_momentum = ctx->momentum;
+  ctx->out_form = ctx->swarm_form;
+  CU(cudaStreamSynchronize(ctx->stream));
+  return FDF_SUCCESS;
+}
 
 int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info) {
   if (!ctx) return FDF_ERR_ARG_NULL;

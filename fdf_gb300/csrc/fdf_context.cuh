@@ -62,6 +62,7 @@ struct FdfContext {
   size_t staging_bytes = 0;
   unsigned int sentinel = 0;
   bool swarm_set = false;
+  bool layout_ok = false;   // the held particles are sorted by (cell, PID) and cell_start matches them
   int swarm_form = FDF_FORM_PLAIN_FP64;   // form the swarm's device arrays are held in
   int out_form = FDF_FORM_PLAIN_FP64;     // form of the last deposits
   bool out_momentum = false;              // the last deposits include the momentum

@@ -560,6 +560,61 @@ __global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDi
   block_add_u64(fev, &cnt->fallback_evals_total);
 }
 
+// UpdateAllParticlePositions in the precision form: fl32(v dt) added to the (hi, lo) position,
+// as the fused step does it.
+__global__ void k_advect32(SwarmBuf b, float dt32, DevCounters *cnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) atomicAdd(&cnt->psteps_total, (unsigned long long)cnt->n_sorted);   // particles advanced
+  if (s >= cnt->n_sorted) return;
+  st_pair(b.x, s, pair_add(ld_pair(b.x, s), __fmul_rn(b.uf[s], dt32)));
+  st_pair(b.y, s, pair_add(ld_pair(b.y, s), __fmul_rn(b.vf[s], dt32)));
+  st_pair(b.z, s, pair_add(ld_pair(b.z, s), __fmul_rn(b.wf[s], dt32)));
+}
+
+// Sort keys of the particles held (a re-sort by (cell, PID)), dropping the LOST ones
+// (CheckAndRemoveLostParticles, ParticleMotion.c:532-625) and/or the ones outside the
+// bounding box (CheckAndRemoveOutOfBoundsParticles, :283-383; the FP32 form decides as the
+// step does).  Kept particles without a cell go to the LOST bucket at the end; the removed
+// ones get key all ones and no slot.
+template <bool F32>
+__global__ void __launch_bounds__(256) k_resort_keys(SwarmBuf b, GridDims g, int remove_lost, int remove_oob,
+                                                    const double *__restrict__ bbox, const float *__restrict__ fbox,
+                                                    DevCounters *cnt, unsigned int *__restrict__ keys,
+                                                    unsigned int *__restrict__ rank, unsigned int *__restrict__ count,
+                                                    unsigned int sentinel) {
+  const int n = cnt->n_sorted;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  LocCounts m;
+  unsigned int hkey = 0xffffffffu;
+  if (s < n) {
+    const int cell = b.cell[s];
+    unsigned int key = (cell >= 0 && (long long)cell < g.Nc) ? (unsigned int)cell : sentinel;
+    if (remove_lost && b.status[s] == ST_LOST) {
+      m.lost += 1;
+      key = 0xffffffffu;
+    } else if (remove_oob) {
+      bool inside;
+      if (F32) {
+        const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
+        unsigned int l0 = 0, o1 = 0, l2 = 0;
+        inside = settle_key32(false, 0, px, py, pz, 1, bbox, fbox, sentinel, l0, o1, l2) != sentinel;
+      } else {
+        const double x = b.x[s], y = b.y[s], z = b.z[s];
+        inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
+      }
+      if (!inside) {
+        m.oob += 1;
+        key = 0xffffffffu;
+      }
+    }
+    keys[s] = key;
+    hkey = key;
+  }
+  const unsigned int r = warp_histogram_rank(hkey, count);
+  if (hkey != 0xffffffffu) rank[s] = r;
+  block_flush_counts(m, cnt);
+}
+
 // Corner field in FP32: mean of the valid adjacent cells (nodes next to occupied cells).
 __global__ void k_center_to_corner32(const float *__restrict__ ucat, GridDims g, float *__restrict__ corner,
                                      const unsigned int *__restrict__ cell_start, unsigned long long *nodes_done) {
@@ -604,7 +659,7 @@ __global__ void __launch_bounds__(256) k_gather_interp32(SwarmBuf src, SwarmBuf 
                                                          const float *__restrict__ corner,
                                                          const unsigned int *__restrict__ perm,
                                                          const unsigned int *__restrict__ cell_start,
-                                                         DevCounters *cnt) {
+                                                         DevCounters *cnt, int mode) {
   const int n = (int)cell_start[g.Nc + 1];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {
@@ -612,20 +667,27 @@ __global__ void __launch_bounds__(256) k_gather_interp32(SwarmBuf src, SwarmBuf 
     cnt->n_sorted = n;
   }
   if (s >= n) return;
-  const unsigned int p = perm[s];
+  const unsigned int p = perm ? perm[s] : (unsigned int)s;
   const int cell = src.cell[p];
   float a1 = src.a1f[p], a2 = src.a2f[p], a3 = src.a3f[p];
+  const unsigned char st = src.status[p];
   dst.x[s] = src.x[p]; dst.y[s] = src.y[p]; dst.z[s] = src.z[p];
   dst.a1f[s] = a1; dst.a2f[s] = a2; dst.a3f[s] = a3;
   dst.Pf[s] = src.Pf[p];
   dst.pid[s] = src.pid[p];
+  if (mode == GATHER_COPY) {
+    dst.uf[s] = src.uf[p]; dst.vf[s] = src.vf[p]; dst.wf[s] = src.wf[p];
+    dst.cell[s] = cell;
+    dst.status[s] = st;
+    return;
+  }
   float ux = 0.f, uy = 0.f, uz = 0.f;
   if (cell < 0) {
     dst.cell[s] = -1;
-    dst.status[s] = ST_LOST;
+    dst.status[s] = mode == GATHER_INTERP ? (unsigned char)ST_LOST : st;
   } else {
     dst.cell[s] = cell;
-    dst.status[s] = ST_ACTIVE_AND_LOCATED;
+    dst.status[s] = mode == GATHER_INTERP ? (unsigned char)ST_ACTIVE_AND_LOCATED : st;
     int i, j, k;
     cell_ijk(g, (unsigned int)cell, i, j, k);
     a1 = fminf(fmaxf(a1, 0.f), 1.f);   // NaN -> 0 as PetscMax(0, PetscMin(1, NaN))
@@ -836,10 +898,25 @@ void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, con
   k_center_to_corner32<<<blocks_for(g.Nn, 256), 256, 0, s>>>(ucat, g, corner, cell_start, nodes_done);
 }
 
+void launch_advect32(const SwarmBuf &b, int n_cap, double dt, DevCounters *cnt, cudaStream_t s) {
+  k_advect32<<<blocks_for(n_cap, 256), 256, 0, s>>>(b, (float)dt, cnt);
+}
+
+void launch_resort_keys(const SwarmBuf &b, int n_cap, GridDims g, int f32, int remove_lost, int remove_oob,
+                        const double *bbox, const float *fbox, DevCounters *cnt, unsigned int *keys,
+                        unsigned int *rank, unsigned int *count, unsigned int sentinel, cudaStream_t s) {
+  if (f32)
+    k_resort_keys<true><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, remove_lost, remove_oob, bbox, fbox, cnt, keys,
+                                                               rank, count, sentinel);
+  else
+    k_resort_keys<false><<<blocks_for(n_cap, 256), 256, 0, s>>>(b, g, remove_lost, remove_oob, bbox, fbox, cnt, keys,
+                                                                rank, count, sentinel);
+}
+
 void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,
                             const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
-                            cudaStream_t s) {
-  k_gather_interp32<<<blocks_for(n_cap, 256), 256, 0, s>>>(src, dst, g, corner, perm, cell_start, cnt);
+                            cudaStream_t s, int mode) {
+  k_gather_interp32<<<blocks_for(n_cap, 256), 256, 0, s>>>(src, dst, g, corner, perm, cell_start, cnt, mode);
 }
 
 void launch_deposit32(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, float *count,

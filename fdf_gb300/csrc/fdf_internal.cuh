@@ -167,10 +167,15 @@ void launch_center_to_corner(const double *ucat, GridDims g, double *corner, con
 void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
                    const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *rank,
                    unsigned int *count, unsigned int sentinel, cudaStream_t s);
-// sorted slot s takes the particle perm[s]; n = cell_start[Nc+1] (read on the device)
+// Modes of the gather kernels: sorted slot s takes the particle perm[s] (perm == nullptr: s
+// itself, src == dst allowed) for s < n = cell_start[Nc+1] (read on the device), and
+//   GATHER_INTERP  interpolates its velocity and sets its status from its cell (the step),
+//   GATHER_COPY    copies velocity and status (a re-sort or a removal),
+//   INTERP_KEEP    interpolates its velocity and keeps its status (InterpolateAllFieldsToSwarm).
+enum { GATHER_COPY = 0, GATHER_INTERP = 1, INTERP_KEEP = 2 };
 void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g,
                           const double *corner, const unsigned int *perm, const unsigned int *cell_start,
-                          DevCounters *cnt, cudaStream_t s);
+                          DevCounters *cnt, cudaStream_t s, int mode = GATHER_INTERP);
 // mi, mj, mk (SoA [3][faces], or nullptr): the momentum deposit, V * velocity split like the volume.
 void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,
                     double *avg, double *fi, double *fj, double *fk, double *mi, double *mj, double *mk,
@@ -197,6 +202,16 @@ void launch_swarm_from_aos(const double *pos, const double *vel, const double *w
 void launch_swarm_to_aos(const SwarmBuf &b, int n, GridDims g, double *pos, double *vel, double *wgt,
                          double *P, long long *cell3, long long *pid, long long *status, cudaStream_t s);
 
+// The reference's stages one at a time (ParticleMotion.c): status reset, position update
+// (plain and precision forms), and the sort keys of a re-sort that may drop the LOST and/or the
+// out-of-bounds particles (either form; ranks and histogram as the locate kernels make them).
+void launch_reset_status(const SwarmBuf &b, int n_cap, const DevCounters *cnt, cudaStream_t s);
+void launch_advect(const SwarmBuf &b, int n_cap, double dt, DevCounters *cnt, cudaStream_t s);
+void launch_advect32(const SwarmBuf &b, int n_cap, double dt, DevCounters *cnt, cudaStream_t s);
+void launch_resort_keys(const SwarmBuf &b, int n_cap, GridDims g, int f32, int remove_lost, int remove_oob,
+                        const double *bbox, const float *fbox, DevCounters *cnt, unsigned int *keys,
+                        unsigned int *rank, unsigned int *count, unsigned int sentinel, cudaStream_t s);
+
 // Precision form (fdf_fp32.cu).
 void launch_build_table32(const double *planes, const double *coor, GridDims g, float *table, cudaStream_t s);
 // fbox: 12 floats, (x, y, z, -) lower and (x, y, z, -) upper bounds strictly inside the
@@ -222,7 +237,7 @@ void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, con
                                unsigned long long *nodes_done, cudaStream_t s);
 void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,
                             const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
-                            cudaStream_t s);
+                            cudaStream_t s, int mode = GATHER_INTERP);
 void launch_deposit32(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, float *count,
                       float *avg, float *fi, float *fj, float *fk, float *mi, float *mj, float *mk, cudaStream_t s);
 void launch_swarm_from_aos32(const double *pos, const double *vel, const double *wgt, const double *P,

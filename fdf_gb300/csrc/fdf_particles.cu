@@ -18,7 +18,7 @@ __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf ds
                                                        const double *__restrict__ corner,
                                                        const unsigned int *__restrict__ perm,
                                                        const unsigned int *__restrict__ cell_start,
-                                                       DevCounters *cnt) {
+                                                       DevCounters *cnt, int mode) {
   const int n = (int)cell_start[g.Nc + 1];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {   // the new sizes, read by the next step
@@ -26,20 +26,27 @@ __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf ds
     cnt->n_sorted = n;
   }
   if (s >= n) return;
-  const unsigned int p = perm[s];
+  const unsigned int p = perm ? perm[s] : (unsigned int)s;
   const int cell = src.cell[p];
   double a1 = src.a1[p], a2 = src.a2[p], a3 = src.a3[p];
+  const unsigned char st = src.status[p];
   dst.x[s] = src.x[p]; dst.y[s] = src.y[p]; dst.z[s] = src.z[p];
   dst.a1[s] = a1; dst.a2[s] = a2; dst.a3[s] = a3;
   dst.P[s] = src.P[p];
   dst.pid[s] = src.pid[p];
+  if (mode == GATHER_COPY) {
+    dst.u[s] = src.u[p]; dst.v[s] = src.v[p]; dst.w[s] = src.w[p];
+    dst.cell[s] = cell;
+    dst.status[s] = st;
+    return;
+  }
   double ux = 0.0, uy = 0.0, uz = 0.0;
   if (cell < 0) {
     dst.cell[s] = -1;
-    dst.status[s] = ST_LOST;
+    dst.status[s] = mode == GATHER_INTERP ? (unsigned char)ST_LOST : st;
   } else {
     dst.cell[s] = cell;
-    dst.status[s] = ST_ACTIVE_AND_LOCATED;
+    dst.status[s] = mode == GATHER_INTERP ? (unsigned char)ST_ACTIVE_AND_LOCATED : st;
     int i, j, k;
     cell_ijk(g, (unsigned int)cell, i, j, k);
     a1 = fdfx::clamp01(a1);
@@ -202,15 +209,40 @@ __global__ void k_to_aos(SwarmBuf b, int n, GridDims g, double *__restrict__ pos
   status[p] = b.status[p];
 }
 
+// ResetAllParticleStatuses (ParticleMotion.c:2149-2176): ACTIVE_AND_LOCATED -> NEEDS_LOCATION.
+__global__ void k_reset_status(unsigned char *__restrict__ status, const DevCounters *cnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < cnt->n_sorted && status[s] == ST_ACTIVE_AND_LOCATED) status[s] = ST_NEEDS_LOCATION;
+}
+
+// UpdateAllParticlePositions (ParticleMotion.c:38-95): x += v dt per component, as the fused
+// step does it.
+__global__ void k_advect(SwarmBuf b, double dt, DevCounters *cnt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) atomicAdd(&cnt->psteps_total, (unsigned long long)cnt->n_sorted);   // particles advanced
+  if (s >= cnt->n_sorted) return;
+  b.x[s] = add(b.x[s], mul(b.u[s], dt));
+  b.y[s] = add(b.y[s], mul(b.v[s], dt));
+  b.z[s] = add(b.z[s], mul(b.w[s], dt));
+}
+
 }  // namespace
+
+void launch_reset_status(const SwarmBuf &b, int n_cap, const DevCounters *cnt, cudaStream_t s) {
+  k_reset_status<<<(n_cap + 255) / 256 > 0 ? (n_cap + 255) / 256 : 1, 256, 0, s>>>(b.status, cnt);
+}
+
+void launch_advect(const SwarmBuf &b, int n_cap, double dt, DevCounters *cnt, cudaStream_t s) {
+  k_advect<<<(n_cap + 255) / 256 > 0 ? (n_cap + 255) / 256 : 1, 256, 0, s>>>(b, dt, cnt);
+}
 
 void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const double *corner,
                           const unsigned int *perm, const unsigned int *cell_start, DevCounters *cnt,
-                          cudaStream_t s) {
+                          cudaStream_t s, int mode) {
   int th = 256;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
-  k_gather_interp<<<blocks, th, 0, s>>>(src, dst, g, corner, perm, cell_start, cnt);
+  k_gather_interp<<<blocks, th, 0, s>>>(src, dst, g, corner, perm, cell_start, cnt, mode);
 }
 
 void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,

@@ -119,11 +119,8 @@ __global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__res
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  unsigned int key = keys[s];
-  if (key >= sentinel) {
-    if (!keep_lost) return;
-    key = sentinel;
-  }
+  const unsigned int key = keys[s];   // sentinel: a LOST particle kept at the end; above: removed
+  if (key > sentinel || (key == sentinel && !keep_lost)) return;
   perm[cell_start[key] + rank[s]] = (unsigned int)s;
 }
 

@@ -174,6 +174,29 @@ int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info);
 int fdf_AdvanceStep(FdfContext *ctx, FdfStepInfo *info);
 int fdf_AdvanceSteps(FdfContext *ctx, int nsteps);
 
+/* ---- the same stages one call at a time, for callers that keep the reference's loop ----
+ * Called in the reference's order (reset, update, locate, remove LOST, remove out of bounds,
+ * interpolate, scatter) they give bit for bit what fdf_AdvanceStep gives. */
+/* ResetAllParticleStatuses (ParticleMotion.c:2149-2176): ACTIVE_AND_LOCATED -> NEEDS_LOCATION. */
+int fdf_ResetAllParticleStatuses(FdfContext *ctx);
+/* UpdateAllParticlePositions (ParticleMotion.c:38-95): position += velocity * dt. */
+int fdf_UpdateAllParticlePositions(FdfContext *ctx);
+/* LocateAllParticlesInGrid_TEST (ParticleMotion.c:1931-2135): the walk for every particle not
+ * ACTIVE_AND_LOCATED, from its previous cell; LOST particles are kept (at the end of the
+ * cell-sorted order).  Velocities are not touched. */
+int fdf_LocateAllParticlesInGrid(FdfContext *ctx, FdfStepInfo *info);
+/* CheckAndRemoveLostParticles (ParticleMotion.c:532-625); *removed (optional) = count. */
+int fdf_CheckAndRemoveLostParticles(FdfContext *ctx, int64_t *removed);
+/* CheckAndRemoveOutOfBoundsParticles (ParticleMotion.c:283-383): positions outside the
+ * grid's bounding box widened by 1e-6 (grid.c:816-858); *removed (optional) = count. */
+int fdf_CheckAndRemoveOutOfBoundsParticles(FdfContext *ctx, int64_t *removed);
+/* InterpolateAllFieldsToSwarm (interpolation.c:1660-1711): center->corner and the trilinear
+ * velocity of every particle from its cell and weights; statuses are kept. */
+int fdf_InterpolateAllFieldsToSwarm(FdfContext *ctx);
+/* ScatterAllParticleFieldsToEulerFields (interpolation.c:2223-2313): ParticleCount and the P
+ * average, plus the face deposit (read them with fdf_GetScatteredFields, fdf_GetFaceDeposits). */
+int fdf_ScatterAllParticleFieldsToEulerFields(FdfContext *ctx);
+
 /* ---- sort by cell (the per-step re-sort of the hot path, as a standalone call) ---- */
 /* Stable counting sort of n particle slots by cell id, all pointers on the device.
  * Slots whose id is negative or >= ncells get no place.  On return cell_start[c] is the
