@@ -38,6 +38,7 @@ _SIGS = {
     "fdf_CheckAndRemoveOutOfBoundsParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_InterpolateAllFieldsToSwarm": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_ScatterAllParticleFieldsToEulerFields": (ctypes.c_int, [ctypes.c_void_p]),
+    "fdf_LocatePoints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 5),
     "fdf_Contra2CartDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTimeStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),

@@ -296,6 +296,17 @@ class PicContext:
     def scatter(self):
         self._check(self.lib.fdf_ScatterAllParticleFieldsToEulerFields(self.h))
 
+    def locate_points(self, position: np.ndarray, cell: np.ndarray | None = None):
+        """The reference walk for points outside the swarm: (cell [n][3], weight [n][3], status [n])."""
+        position = np.ascontiguousarray(position, dtype=np.float64).reshape(-1, 3)
+        n = len(position)
+        cin = None if cell is None else np.ascontiguousarray(cell, dtype=np.int64).reshape(n, 3)
+        cout = np.empty((n, 3), dtype=np.int64)
+        w = np.empty((n, 3))
+        st = np.empty(n, dtype=np.int64)
+        self._check(self.lib.fdf_LocatePoints(self.h, n, _ptr(position), _ptr(cin), _ptr(cout), _ptr(w), _ptr(st)))
+        return cout, w, st
+
     # -- the hot path
     def initial_setup(self) -> FdfStepInfo:
         info = FdfStepInfo()

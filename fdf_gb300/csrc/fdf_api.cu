@@ -672,6 +672,67 @@ int fdf_ScatterAllParticleFieldsToEulerFields(FdfContext *ctx) {
   return FDF_SUCCESS;
 }
 
+int fdf_LocatePoints(FdfContext *ctx, int64_t n, const double *position, const int64_t *cell_in, int64_t *cell_out,
+                     double *weight, int64_t *status) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (n > 0 && (!position || !cell_out || !weight || !status))
+    return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatePoints: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatePoints: call fdf_SetGrid first");
+  if (n < 0 || n > FDF_MAX_PARTICLES) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatePoints: n out of range");
+  if (n == 0) return FDF_SUCCESS;
+  CU(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const GridDims &g = ctx->g;
+  const int m = (int)n;
+  // the points as a temporary plain-form swarm: NEEDS_LOCATION, walk start = the given cell
+  void *mem = nullptr;
+  const size_t sw = swarm_bytes_per_buf(m), aos = 24ull * m, one = 8ull * m;
+  const size_t bytes = sw + 4 * aos + 3 * one + 4ull * m + 4ull * (g.Nc + 2) + sizeof(DevCounters) + 256 * 12;
+  CU(cudaMalloc(&mem, bytes));
+  char *p = (char *)mem;
+  SwarmBuf tb;
+  carve_swarm(p, m, tb);
+  auto take = [&](size_t nb) { char *q = p; p += (nb + 255) / 256 * 256; return q; };
+  take(sw);
+  double *d_pos = (double *)take(aos);
+  long long *d_cell = (long long *)take(aos);
+  double *d_zero = (double *)take(aos);   // velocity, weight, P, pid, status (0 = NEEDS_LOCATION)
+  double *d_w = (double *)take(aos);
+  double *d_P = (double *)take(one);
+  long long *d_pid = (long long *)take(one);
+  long long *d_st = (long long *)take(one);
+  unsigned int *keys = (unsigned int *)take(4ull * m);
+  unsigned int *hist = (unsigned int *)take(4ull * (g.Nc + 2));
+  DevCounters *tc = (DevCounters *)take(sizeof(DevCounters));
+  DevCounters c0{};
+  c0.n = m;
+  c0.n_sorted = m;
+  cudaError_t e = cudaMemcpyAsync(d_pos, position, aos, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cell_in ? cudaMemcpyAsync(d_cell, cell_in, aos, cudaMemcpyHostToDevice, s) : cudaMemsetAsync(d_cell, 0xff, aos, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_zero, 0, aos, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, 4ull * (g.Nc + 2), s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tc, &c0, sizeof(c0), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    launch_swarm_from_aos(d_pos, d_zero, d_zero, d_zero, d_cell, (const long long *)d_zero, (const long long *)d_zero,
+                          m, g, tb, s);
+    launch_locate(tb, m, g, ctx->planes, 0.0, 0, ctx->bbox, 0, tc, keys, nullptr, hist, ctx->sentinel, s);
+    launch_swarm_to_aos(tb, m, g, d_pos, d_zero, d_w, d_P, d_cell, d_pid, d_st, s);
+    ctx->launches += 3;
+    e = cudaGetLastError();
+  }
+  unsigned int err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cell_out, d_cell, aos, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(weight, d_w, aos, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status, d_st, one, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, &tc->err, sizeof(err), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(mem);
+  if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_LocatePoints: ") + cudaGetErrorString(e));
+  if (err & ERRBIT_DEGENERATE) return fail(ctx, FDF_ERR_USER, "Degenerate plane detected (normal vector is near zero).");
+  return FDF_SUCCESS;
+}
+
 int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   FdfStepInfo local{};

@@ -197,6 +197,14 @@ int fdf_InterpolateAllFieldsToSwarm(FdfContext *ctx);
  * average, plus the face deposit (read them with fdf_GetScatteredFields, fdf_GetFaceDeposits). */
 int fdf_ScatterAllParticleFieldsToEulerFields(FdfContext *ctx);
 
+/* LocateParticleOrFindMigrationTarget_TEST (walkingsearch.c:1094-1242) for a batch of points
+ * that are not the swarm (probes, post-processing): the plain FP64 walk, bit-identical to the
+ * reference, from cell_in[p] (or cell (0,0,0), a new particle's start, where it is -1 or
+ * cell_in is NULL).  Outputs: cell_out [n][3] (-1 when LOST), weight [n][3] (zero when LOST),
+ * status [n] (ACTIVE_AND_LOCATED or LOST).  Host arrays; the swarm is not touched. */
+int fdf_LocatePoints(FdfContext *ctx, int64_t n, const double *position, const int64_t *cell_in, int64_t *cell_out,
+                     double *weight, int64_t *status);
+
 /* ---- sort by cell (the per-step re-sort of the hot path, as a standalone call) ---- */
 /* Stable counting sort of n particle slots by cell id, all pointers on the device.
  * Slots whose id is negative or >= ncells get no place.  On return cell_start[c] is the

@@ -111,3 +111,29 @@ def test_stage_calls_sort_an_unsorted_swarm(require_gpu):
             assert np.array_equal(getattr(got, f), getattr(ref, f)), f
         for x, y in zip(ctx.get_faces() + ctx.get_scattered(), ref_faces + ref_sc):
             assert np.array_equal(x, y)
+
+
+def test_locate_points_matches_the_reference_walk(require_gpu):
+    """fdf_LocatePoints: the reference walk for arbitrary points (inside, outside, on the grid's
+    boundary), from given cells or from cell (0,0,0), bit for bit against the oracle's
+    LocateParticleOrFindMigrationTarget."""
+    wl = W.config_sinusoidal(IM=10, JM=8, KM=20, n=10, cfl=1.0, steps=1)
+    g = O.Grid(wl.coor)
+    rng = np.random.default_rng(9)
+    pts = rng.uniform(-0.1, 1.1, size=(3000, 3))
+    pts[:200] = wl.coor.reshape(-1, 3)[rng.integers(0, wl.coor.reshape(-1, 3).shape[0], 200)]   # grid nodes
+    cells = np.full((3000, 3), -1, dtype=np.int64)
+    cells[1000:] = np.stack([rng.integers(0, 10, 2000), rng.integers(0, 8, 2000), rng.integers(0, 20, 2000)], 1)
+    with PicContext(0) as ctx:
+        ctx.set_grid(wl.coor)
+        cout, w, st = ctx.locate_points(pts, cells)
+        cout0, w0, st0 = ctx.locate_points(pts[:500])          # no start cells: (0,0,0)
+    for p in range(len(pts)):
+        r = O.locate_particle(g, pts[p], cells[p])
+        assert r["err"] == 0
+        assert np.array_equal(cout[p], r["cell"]) and st[p] == r["status"], p
+        assert np.array_equal(w[p].view(np.int64), r["weights"].view(np.int64)), p
+    for p in range(500):
+        r = O.locate_particle(g, pts[p])
+        assert np.array_equal(cout0[p], r["cell"]) and st0[p] == r["status"]
+    assert (st == 3).any() and (st == 1).any()   # both LOST and located points
