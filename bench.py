@@ -32,9 +32,10 @@ METRIC = "particle-steps/s on 1 GB300: learned+FP32 vs plain FP64 walk, exact ce
 UNIT = "particle-steps/s"
 
 # Algorithmic bytes: particle state per particle, plus
-# one plane-table row per walk evaluation beyond the first (the first evaluation's row is the
-# particle's own cell, shared by the cell's particles in the cell-sorted order).
-ROW_BYTES = 296          # 36 plane doubles + threshold read per walk evaluation
+# one FP32 plane-table row per walk evaluation beyond the first (the first evaluation's row is
+# the particle's own cell, shared by the cell's particles in the cell-sorted order; so is the
+# FP64 row of the cell the plain walk concludes in, whose six distances give the weights).
+ROW_BYTES = 176          # 11 x 16 B FP32 row read per walk evaluation
 LOCATE_PER_PARTICLE = 53 + 61
 GATHER_PER_PARTICLE = 8 + 64 + 93
 

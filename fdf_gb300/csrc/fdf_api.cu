@@ -463,8 +463,8 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
                     ctx->cnt, ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, nullptr, 0.f, s);
   } else {
-    launch_locate(src, ctx->cap, g, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt, ctx->keys, ctx->rank,
-                  ctx->cell_start, ctx->sentinel, s);
+    launch_locate(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, drop, ctx->cnt,
+                    ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, s);
   }
   size_t e1 = prof ? record_event(ctx, s) : 0;
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
@@ -716,7 +716,8 @@ int fdf_LocatePoints(FdfContext *ctx, int64_t n, const double *position, const i
   if (e == cudaSuccess) {
     launch_swarm_from_aos(d_pos, d_zero, d_zero, d_zero, d_cell, (const long long *)d_zero, (const long long *)d_zero,
                           m, g, tb, s);
-    launch_locate(tb, m, g, ctx->planes, 0.0, 0, ctx->bbox, 0, tc, keys, nullptr, hist, ctx->sentinel, s);
+    launch_locate(tb, m, g, ctx->table32, ctx->planes, 0.0, 0, ctx->bbox, 0, tc, keys, nullptr, hist, ctx->sentinel,
+                    s);
     launch_swarm_to_aos(tb, m, g, d_pos, d_zero, d_w, d_P, d_cell, d_pid, d_st, s);
     ctx->launches += 3;
     e = cudaGetLastError();

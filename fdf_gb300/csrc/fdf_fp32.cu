@@ -7,30 +7,14 @@
 // Uploads split the caller's FP64 position (an error of at most 2^-48 |p|); downloads
 // return hi + lo exactly.
 //
-// Walk.  Each face class the walk needs -- d < 0, d == 0 (|d| < thr), d > 0 -- is
-// decided from an FP32 signed distance when that is provably the FP64 class for the
-// form's position, and from the exact FP64 distance (the plain path's plane table)
-// otherwise.  With c0 = c0h + c0l the cell's first vertex as a float pair (exact),
-// fcr = fl32(fc - c0), pr = fl32(fl32(ph - c0h) + fl32(pl - c0l)), n32 = fl32(n) and
-// d32 = (fcr - pr) . n32 (FP32, fused), every rounding is bounded by u32 = 2^-24 times
-// the magnitudes involved:
-//     |pr_i - (p_i - c0_i)| <= u32 (2 B_i + 2 u32 (|ph_i| + |c0h_i|)),  B_i = |p_i - c0_i|
-//     |d32 - d64| <= 7.001 u32 S,   S = sum_i (A_i + B_i + u32 (|ph_i| + |c0h_i|)) |n_i|
-// with A_i = |fc_i - c0_i| (d64 is the reference's FP64 value; its own error is
-// ~1e-16 S).  The kernel uses E = 12 u32 S32 (S32, the FP32 estimate of S, is within
-// 8 u32 of S) and M = fl32(E + thr32) with thr32 >= thr (1 + 2^-22) rounded up, and
-// classifies
-//     d32 > M -> d64 >= thr (positive);  d32 < -M -> d64 <= -thr (negative);
-// anything else (including NaN) falls back to the exact FP64 distance of that face.
-// The cells, statuses and walk paths are therefore the reference's for the form's own
-// positions.  Fallbacks are counted.  The hot loop issues no FP64 instruction.
-//
-// Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32, negative for a degenerate
-// cell), c0l (3 x f32), overlap margin (f32, see cell_margin), then per face LEFT..BACK:
-// fcr (3 x f32), n32 (3 x f32).
+// Walk.  Every face class the walk needs is decided exactly as the FP64 reference decides it
+// (fdf_walk.cuh: the FP32 plane table with a rigorous error bound, FP64 where it cannot
+// decide), so the cells, statuses and walk paths are the reference's for the form's own
+// positions.
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
 #include "fdf_counters.cuh"
+#include "fdf_walk.cuh"
 
 namespace {
 
@@ -146,119 +130,6 @@ __device__ __forceinline__ float2 pair_add(float2 p, float v) {
   return make_float2(h, __fsub_rn(t, __fsub_rn(h, sh)));
 }
 
-__device__ __forceinline__ double pair_value(float2 p) { return __dadd_rn((double)p.x, (double)p.y); }
-
-// Exact FP64 signed distance of face f (the plain path's arithmetic), thresholded.
-__device__ __forceinline__ double exact_face(const double *__restrict__ row64, int f, double x, double y, double z) {
-  const double2 *r = reinterpret_cast<const double2 *>(row64);
-  double2 p0 = __ldg(r + 3 * f), p1 = __ldg(r + 3 * f + 1), p2 = __ldg(r + 3 * f + 2);
-  double2 tf = __ldg(r + 18);
-  double dd = add(add(mul(sub(p0.x, x), p1.y), mul(sub(p0.y, y), p2.x)), mul(sub(p1.x, z), p2.y));
-  if (fdfx::abs_lt_bits(dd, fdfx::ubits(tf.x), fdfx::is_nan(tf.x))) dd = 0.0;
-  return dd;
-}
-
-// One cell evaluated for the form's position: the face classes the walk needs, the
-// distances the weights use, and (CERT) whether every face is positive by more than
-// thr + the cell's overlap margin, which the FP32 bound certifies without FP64.
-struct Eval32 {
-  unsigned int neg;   // bit f: face f negative
-  bool zero;          // some face within its threshold
-  bool degenerate;
-  bool clear;
-  float dv[6];
-};
-
-template <bool CERT>
-__device__ __forceinline__ void eval_cell32(const float *__restrict__ table, const double *__restrict__ planes,
-                                            long long cur, float2 px, float2 py, float2 pz, float sx, float sy,
-                                            float sz, Eval32 &e, unsigned int &fb) {
-  const float4 *row = reinterpret_cast<const float4 *>(table + cur * FDF_ROW32);
-  const float4 h0 = __ldg(row), h1 = __ldg(row + 1);
-  e.neg = 0u;
-  e.zero = false;
-  e.clear = CERT;
-  e.degenerate = (__float_as_uint(h0.w) >> 31) != 0u;
-  if (e.degenerate) return;
-  const float thr32 = h0.w;
-  const float prx = __fadd_rn(__fsub_rn(px.x, h0.x), __fsub_rn(px.y, h1.x));
-  const float pry = __fadd_rn(__fsub_rn(py.x, h0.y), __fsub_rn(py.y, h1.y));
-  const float prz = __fadd_rn(__fsub_rn(pz.x, h0.z), __fsub_rn(pz.y, h1.z));
-  // the split term u32 (|ph| + |c0h|) of the bound, per component
-  const float ex = __fmul_rn(__fadd_rn(sx, fabsf(h0.x)), 5.9604644775390625e-8f);
-  const float ey = __fmul_rn(__fadd_rn(sy, fabsf(h0.y)), 5.9604644775390625e-8f);
-  const float ez = __fmul_rn(__fadd_rn(sz, fabsf(h0.z)), 5.9604644775390625e-8f);
-  float fr[36];   // per face: fcr (3), n32 (3); nine 16-B loads
-#pragma unroll
-  for (int q = 0; q < 9; ++q) {
-    const float4 v = __ldg(row + 2 + q);
-    fr[4 * q] = v.x; fr[4 * q + 1] = v.y; fr[4 * q + 2] = v.z; fr[4 * q + 3] = v.w;
-  }
-#pragma unroll
-  for (int f = 0; f < 6; ++f) {
-    const float fx = fr[6 * f], fy = fr[6 * f + 1], fz = fr[6 * f + 2];
-    const float nx = fr[6 * f + 3], ny = fr[6 * f + 4], nz = fr[6 * f + 5];
-    const float tx = __fsub_rn(fx, prx), ty = __fsub_rn(fy, pry), tz = __fsub_rn(fz, prz);
-    const float d32 = __fmaf_rn(tz, nz, __fmaf_rn(ty, ny, __fmul_rn(tx, nx)));
-    const float S = __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fz), fabsf(prz)), ez), fabsf(nz),
-                              __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fy), fabsf(pry)), ey), fabsf(ny),
-                                        __fmul_rn(__fadd_rn(__fadd_rn(fabsf(fx), fabsf(prx)), ex), fabsf(nx))));
-    const float M = __fadd_rn(__fmul_rn(S, 12.0f * 5.9604644775390625e-8f), thr32);
-    if (d32 > M) {
-      e.dv[f] = d32;
-      if (CERT) e.clear = e.clear && d32 > __fadd_ru(M, h1.w);
-    } else if (d32 < -M) {
-      e.neg |= 1u << f;
-      e.dv[f] = d32;
-      if (CERT) e.clear = false;
-    } else {
-      const double d64 = exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py), pair_value(pz));
-      if (fdfx::lt0(d64)) e.neg |= 1u << f;
-      e.zero = e.zero || fdfx::eq0(d64);
-      e.dv[f] = __double2float_rn(d64);
-      if (CERT) e.clear = false;
-      ++fb;
-    }
-  }
-}
-
-// The reference walk from (i, j, k) for at most `limit` evaluations, with Brent cycle
-// detection (a revisited cell repeats forever, which the reference ends as LOST after
-// MAX_TRAVERSAL evaluations).
-struct Walk32 {
-  int i, j, k, steps, evaluated;
-  bool concluded, lost, cycle;
-  unsigned int err;
-  Eval32 e;
-};
-
-__device__ __forceinline__ void walk_ref32(const float *__restrict__ table, const double *__restrict__ planes,
-                                           const GridDims &g, float2 px, float2 py, float2 pz, int limit, Walk32 &w,
-                                           unsigned int &fb) {
-  const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
-  long long saved = -1;
-  int power = 1, lam = 0;
-  w.steps = 0; w.evaluated = 0;
-  w.concluded = false; w.lost = false; w.cycle = false;
-  while (!w.concluded && w.steps < limit) {
-    ++w.steps;
-    if (w.i < 0 || w.i >= g.IM || w.j < 0 || w.j >= g.JM || w.k < 0 || w.k >= g.KM) { w.lost = true; break; }
-    const long long cur = ((long long)w.k * g.JM + w.j) * g.IM + w.i;
-    if (cur == saved) { w.cycle = true; w.lost = true; break; }
-    if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
-    eval_cell32<false>(table, planes, cur, px, py, pz, sx, sy, sz, w.e, fb);
-    if (w.e.degenerate) { w.err |= ERRBIT_DEGENERATE; w.lost = true; break; }
-    ++w.evaluated;
-    if (!w.e.neg || w.e.zero) {
-      w.concluded = true;
-    } else {
-      const unsigned int ng = w.e.neg;
-      if (ng & (1u << F_FRONT)) w.k += 1; else if (ng & (1u << F_BACK)) w.k -= 1;
-      if (ng & (1u << F_LEFT)) w.i -= 1; else if (ng & (1u << F_RIGHT)) w.i += 1;
-      if (ng & (1u << F_BOTTOM)) w.j -= 1; else if (ng & (1u << F_TOP)) w.j += 1;
-    }
-  }
-}
 
 // Writes the located (or LOST) particle: weights (UpdateParticleWeights in FP32: clamp
 // d <= 1e-14, then the three ratios), cell and status.

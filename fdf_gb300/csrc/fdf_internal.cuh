@@ -134,11 +134,12 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_LOC_MIN_BLOCKS
 #define FDF_LOC_MIN_BLOCKS (1024 / FDF_LOC_THREADS)
 #endif
-// Resident blocks per SM of the plain FP64 walk (FP64-bound: occupancy barely matters) and of
-// the per-cell PID ordering (latency-bound: 2048 resident threads at 32 registers, 1.59 -> 1.24 ms
-// for the 64M-particle sort stage).
+// Resident blocks per SM of the plain walk (its steps decided from the FP32 table: latency-bound
+// like the FP32 walk; 768 and 1024 resident threads time the same, 13.3 ms per 64M-particle
+// step) and of the per-cell PID ordering (latency-bound: 2048 resident threads at 32 registers,
+// 1.59 -> 1.24 ms for the 64M-particle sort stage).
 #ifndef FDF_PLAIN_MIN_BLOCKS
-#define FDF_PLAIN_MIN_BLOCKS 12
+#define FDF_PLAIN_MIN_BLOCKS 8
 #endif
 #ifndef FDF_ORDER_MIN_BLOCKS
 #define FDF_ORDER_MIN_BLOCKS 8
@@ -164,9 +165,10 @@ void launch_center_to_corner(const double *ucat, GridDims g, double *corner, con
 // or sentinel (LOST / removed), and histograms the kept keys into count[] (bucket
 // Nc = LOST particles, counted only when keep_lost), with rank[s] = the particle's rank
 // among its key's particles (rank may be null).
-void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
-                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *rank,
-                   unsigned int *count, unsigned int sentinel, cudaStream_t s);
+// table: the FP32 plane table, which decides the walk's steps exactly.
+void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
+                   int advect, const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys,
+                   unsigned int *rank, unsigned int *count, unsigned int sentinel, cudaStream_t s);
 // Modes of the gather kernels: sorted slot s takes the particle perm[s] (perm == nullptr: s
 // itself, src == dst allowed) for s < n = cell_start[Nc+1] (read on the device), and
 //   GATHER_INTERP  interpolates its velocity and sets its status from its cell (the step),

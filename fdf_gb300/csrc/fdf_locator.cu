@@ -319,7 +319,8 @@ int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t 
   CUT(cudaMemcpyAsync(tc, &c0, sizeof(c0), cudaMemcpyHostToDevice, s));
   CUT(cudaMemsetAsync(hist, 0, 4ull * (g.Nc + 2), s));
   launch_seed(ctx->coor, g, n, seed, 0, 1, 0, 0.0, tb, s);
-  launch_locate(tb, (int)n, g, ctx->planes, 0.0, 0, ctx->bbox, 0, tc, keys, nullptr, hist, ctx->sentinel, s);
+  launch_locate(tb, (int)n, g, ctx->table32, ctx->planes, 0.0, 0, ctx->bbox, 0, tc, keys, nullptr, hist,
+                  ctx->sentinel, s);
   mlp_flag_located(tb.cell, tb.status, n, flag, s);
   CUT(cudaMemcpyAsync(slot, flag, 4ull * n, cudaMemcpyDeviceToDevice, s));
   exclusive_scan_u32(slot, n, sums, s);

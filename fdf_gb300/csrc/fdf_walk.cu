@@ -6,8 +6,15 @@
 // UpdateCellIndicesBasedOnDistancesTEST (:882-959) and UpdateParticleWeights
 // (ParticleSwarm.c:1010-1047).  The per-cell plane table holds every
 // particle-independent value of ComputeSignedDistanceToPlane, computed with the
-// reference's own operation order, so each signed distance here is the
+// reference's own operation order, so each FP64 signed distance here is the
 // reference's bit for bit: d = (fc - p) . n, then |d| < thr -> 0.
+//
+// The walk's steps take their face classes from the FP32 plane table with a rigorous
+// error bound and fall back to the FP64 distance of a face only where the bound cannot
+// decide (fdf_walk.cuh), so the path of cells is the FP64 walk's; the concluding cell's
+// six distances are computed in FP64 as the reference computes them, for the weights.
+// Positions, velocities and weights are the reference's bit for bit; what goes is the
+// FP64 work of every evaluation before the last.
 //
 // The stuck-cell tie-breaker (walkingsearch.c:1149-1185) cannot fire on one
 // rank: an evaluation either concludes (position >= 0) or reports some d < 0,
@@ -27,6 +34,7 @@
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
 #include "fdf_counters.cuh"
+#include "fdf_walk.cuh"
 
 namespace {
 
@@ -34,17 +42,16 @@ using fdfx::add;
 using fdfx::sub;
 using fdfx::mul;
 
-__global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locate(SwarmBuf b, GridDims g, const double *__restrict__ planes,
-                                                double dt, int advect, int reset_first, const double *__restrict__ bbox,
-                                                int drop_removed, DevCounters *cnt, unsigned int *__restrict__ keys,
-                                                unsigned int *__restrict__ rank, unsigned int *__restrict__ count,
-                                                unsigned int sentinel) {
+__global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS)
+    k_locate(SwarmBuf b, GridDims g, const float *__restrict__ table, const double *__restrict__ planes, double dt,
+               int advect, int reset_first, const double *__restrict__ bbox, int drop_removed, DevCounters *cnt,
+               unsigned int *__restrict__ keys, unsigned int *__restrict__ rank, unsigned int *__restrict__ count,
+               unsigned int sentinel) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && advect) atomicAdd(&cnt->psteps_total, (unsigned long long)n);
-  unsigned int my_lost = 0, my_oob = 0, my_evals = 0, my_done = 0, my_lost_total = 0;
-  unsigned int my_err = 0;
-  unsigned int hkey = 0xffffffffu;   // histogram bucket of this particle (none = all ones)
+  LocCounts m;
+  unsigned int hkey = 0xffffffffu;
   if (s < n) {
     double x = b.x[s], y = b.y[s], z = b.z[s];
     if (advect) {
@@ -58,52 +65,31 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locat
     int cell = b.cell[s];
     bool lost = false;
     if (st != ST_ACTIVE_AND_LOCATED) {
-      // InitializeTraversalParameters: previous cell if it is inside the grid, else (0,0,0)
-      int i = 0, j = 0, k = 0;
-      if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, i, j, k);
-      int steps = 0, evaluated = 0;
-      bool concluded = false, cycle = false;
-      long long saved = -1;
-      int power = 1, lam = 0;
-      double d[6];
-      while (!concluded && steps < FDF_MAX_TRAVERSAL) {
-        ++steps;
-        if (i < 0 || i >= g.IM || j < 0 || j >= g.JM || k < 0 || k >= g.KM) { lost = true; break; }
-        const long long cur = ((long long)k * g.JM + j) * g.IM + i;
-        if (cur == saved) { cycle = true; lost = true; break; }
-        if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
-        const double2 *row = reinterpret_cast<const double2 *>(planes + cur * FDF_ROW);
-        double2 tf = __ldg(row + 18);   // thr, degenerate flag
-        if (fdfx::ubits(tf.y) != 0ULL) { my_err |= ERRBIT_DEGENERATE; lost = true; break; }
-        const unsigned long long thr_bits = fdfx::ubits(tf.x);
-        const bool thr_nan = fdfx::is_nan(tf.x);
-        ++evaluated;
-        bool neg = false, zero = false;
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
-          double2 p0 = __ldg(row + 3 * f), p1 = __ldg(row + 3 * f + 1), p2 = __ldg(row + 3 * f + 2);
-          // p0 = (fc.x, fc.y), p1 = (fc.z, n.x), p2 = (n.y, n.z); d = (fc - p) . n
-          double dd = add(add(mul(sub(p0.x, x), p1.y), mul(sub(p0.y, y), p2.x)), mul(sub(p1.x, z), p2.y));
-          if (fdfx::abs_lt_bits(dd, thr_bits, thr_nan)) dd = 0.0;
-          d[f] = dd;
-          neg |= fdfx::lt0(dd);
-          zero |= fdfx::eq0(dd);
-        }
-        if (!neg || zero) {
-          concluded = true;   // position >= 0: inside, or on a face (accepted even if outside another)
-        } else {
-          if (fdfx::lt0(d[F_FRONT])) k += 1; else if (fdfx::lt0(d[F_BACK])) k -= 1;
-          if (fdfx::lt0(d[F_LEFT])) i -= 1; else if (fdfx::lt0(d[F_RIGHT])) i += 1;
-          if (fdfx::lt0(d[F_BOTTOM])) j -= 1; else if (fdfx::lt0(d[F_TOP])) j += 1;
-        }
-      }
-      my_evals = (unsigned long long)(cycle ? FDF_MAX_TRAVERSAL : steps);
-      my_done = (unsigned long long)evaluated;
-      if (lost || !concluded) {
+      // (hi, lo) within 2^-48 |v| of v; a nonzero |v| below 2^-120 (where the split's error is
+      // absolute) gives a NaN pair, whose faces all take the FP64 route
+      auto split = [](double v) {
+        const float h = __double2float_rn(v);
+        const unsigned int hw = (unsigned int)__double2hiint(v) & 0x7fffffffu;
+        if (hw < (903u << 20) && (hw | (unsigned int)__double2loint(v)) != 0u) return make_float2(__int_as_float(0x7fc00000), 0.f);
+        return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+      };
+      Walk32 w;
+      w.i = 0; w.j = 0; w.k = 0; w.err = 0u;   // InitializeTraversalParameters: previous cell, else (0,0,0)
+      if (cell >= 0 && (long long)cell < g.Nc) cell_ijk(g, (unsigned int)cell, w.i, w.j, w.k);
+      walk_ref32<true>(table, planes, g, split(x), split(y), split(z), FDF_MAX_TRAVERSAL, w, m.fb, x, y, z);
+      m.err |= w.err;
+      m.evals += (unsigned int)(w.cycle ? FDF_MAX_TRAVERSAL : w.steps);
+      m.done += (unsigned int)w.evaluated;
+      if (w.lost || !w.concluded) {
         lost = true;
         cell = -1;
         st = ST_LOST;
       } else {
+        cell = (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
+        const double *row = planes + (long long)cell * FDF_ROW;
+        double d[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) d[f] = exact_face(row, f, x, y, z);
         const unsigned long long tol_bits = fdfx::ubits(FDF_INTERP_DIST_TOL);
 #pragma unroll
         for (int f = 0; f < 6; ++f)
@@ -111,7 +97,6 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locat
         b.a1[s] = __ddiv_rn(d[F_LEFT], add(d[F_LEFT], d[F_RIGHT]));
         b.a2[s] = __ddiv_rn(d[F_BOTTOM], add(d[F_BOTTOM], d[F_TOP]));
         b.a3[s] = __ddiv_rn(d[F_BACK], add(d[F_FRONT], d[F_BACK]));
-        cell = (int)(((long long)k * g.JM + j) * g.IM + i);
         st = ST_ACTIVE_AND_LOCATED;
       }
       b.cell[s] = cell;
@@ -120,14 +105,13 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locat
       lost = (cell < 0);
     }
     unsigned int key = lost ? sentinel : (unsigned int)cell;
-    if (lost) my_lost_total = 1;
-    if (drop_removed) {
-      // CheckAndRemoveLostParticles, then CheckAndRemoveOutOfBoundsParticles on the rest.
+    if (lost) m.lost_total += 1;
+    if (drop_removed) {   // CheckAndRemoveLostParticles, then CheckAndRemoveOutOfBoundsParticles
       if (lost) {
-        my_lost = 1;
+        m.lost += 1;
       } else {
-        bool inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
-        if (!inside) { my_oob = 1; key = sentinel; }
+        const bool inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
+        if (!inside) { m.oob += 1; key = sentinel; }
       }
     }
     keys[s] = key;
@@ -136,9 +120,6 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS) k_locat
   }
   const unsigned int r = warp_histogram_rank(hkey, count);
   if (rank && hkey != 0xffffffffu) rank[s] = r;
-  LocCounts m;
-  m.lost = my_lost; m.oob = my_oob; m.evals = my_evals; m.done = my_done; m.lost_total = my_lost_total;
-  m.err = my_err;
   block_flush_counts(m, cnt);
 }
 
@@ -169,14 +150,12 @@ __global__ void k_fold_counts(DevCounters *cnt) {
 
 void launch_fold_counts(DevCounters *cnt, cudaStream_t s) { k_fold_counts<<<1, 32 * (CNT_FB + 1), 0, s>>>(cnt); }
 
-void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const double *planes, double dt, int advect,
-                   const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys, unsigned int *rank,
-                   unsigned int *count, unsigned int sentinel, cudaStream_t s) {
-  // advect and drop_removed are both set by the fused step, which also resets statuses first.
-  int reset_first = drop_removed;
+void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes, double dt,
+                   int advect, const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys,
+                   unsigned int *rank, unsigned int *count, unsigned int sentinel, cudaStream_t s) {
+  // advect and drop_removed are both set by the fused step, which also resets statuses first
   constexpr int th = FDF_LOC_THREADS;
-  int blocks = (n_cap + th - 1) / th;
-  if (blocks == 0) blocks = 1;
-  k_locate<<<blocks, th, 0, s>>>(b, g, planes, dt, advect, reset_first, bbox, drop_removed, cnt, keys, rank, count,
-                                 sentinel);
+  const unsigned int blocks = n_cap > 0 ? (unsigned int)((n_cap + th - 1) / th) : 1u;
+  k_locate<<<blocks, th, 0, s>>>(b, g, table, planes, dt, advect, drop_removed, bbox, drop_removed, cnt,
+                                                keys, rank, count, sentinel);
 }

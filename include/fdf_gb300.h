@@ -60,7 +60,7 @@ typedef struct {
   int64_t removed_oob;     /* CheckAndRemoveOutOfBoundsParticles count      */
   int64_t walk_evals;      /* cell evaluations the reference's walk makes (a walk that cycles
                               until MAX_TRAVERSAL counts 1000; the GPU walk stops at the cycle) */
-  int64_t fp64_fallbacks;  /* precision form: faces whose class needed the exact FP64 distance */
+  int64_t fp64_fallbacks;  /* walk faces whose class needed the exact FP64 distance (every form) */
 } FdfStepInfo;
 
 /* Forms of the path.  PLAIN_FP64: every value as the reference computes it, bit for bit.

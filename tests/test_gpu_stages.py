@@ -118,14 +118,22 @@ def test_locate_points_matches_the_reference_walk(require_gpu):
     boundary), from given cells or from cell (0,0,0), bit for bit against the oracle's
     LocateParticleOrFindMigrationTarget."""
     wl = W.config_sinusoidal(IM=10, JM=8, KM=20, n=10, cfl=1.0, steps=1)
-    g = O.Grid(wl.coor)
+    coor = wl.coor - 0.5   # the origin inside the grid
+    g = O.Grid(coor)
     rng = np.random.default_rng(9)
-    pts = rng.uniform(-0.1, 1.1, size=(3000, 3))
-    pts[:200] = wl.coor.reshape(-1, 3)[rng.integers(0, wl.coor.reshape(-1, 3).shape[0], 200)]   # grid nodes
+    pts = rng.uniform(-0.6, 0.6, size=(3000, 3))
+    pts[:200] = coor.reshape(-1, 3)[rng.integers(0, coor.reshape(-1, 3).shape[0], 200)]   # grid nodes
+    # one coordinate at a value the FP32 split cannot carry (tiny, subnormal, signed zero, beyond
+    # FP32's range, non-finite), the others inside the grid: the walk's faces then take the FP64
+    # route
+    special = [0.0, -0.0, 1e-200, -3e-310, 5e-324, 2.0 ** -121, 1e30, -1e39, 1e300, np.inf, -np.inf, np.nan]
+    for q, v in enumerate(special * 5):
+        pts[200 + q] = (0.01 * (q % 7), -0.02, 0.03)
+        pts[200 + q, q % 3] = v
     cells = np.full((3000, 3), -1, dtype=np.int64)
     cells[1000:] = np.stack([rng.integers(0, 10, 2000), rng.integers(0, 8, 2000), rng.integers(0, 20, 2000)], 1)
     with PicContext(0) as ctx:
-        ctx.set_grid(wl.coor)
+        ctx.set_grid(coor)
         cout, w, st = ctx.locate_points(pts, cells)
         cout0, w0, st0 = ctx.locate_points(pts[:500])          # no start cells: (0,0,0)
     for p in range(len(pts)):
