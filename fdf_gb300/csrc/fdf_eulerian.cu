@@ -19,6 +19,7 @@
 // values exactly, and the halved form is exact in the range it is used, so every bit of ucat is
 // the reference's.  The kernel is bound by GB300's FP64 pipe, not HBM.
 #include "fdf_context.cuh"
+#include "fdf_exact.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -40,23 +41,7 @@ __device__ __forceinline__ bool mid_range(double x) {
   return b == 0ull || (e - (1023u - 400u)) <= 800u;
 }
 
-// The hardware conversion, out of line so that it is not if-converted into every lane.
-__device__ __noinline__ float d2f_hw(double x) { return __double2float_rn(x); }
-
-// double -> float, round to nearest even, on the integer pipe for results in the normal
-// float range (the FP64 pipe is this path's bound); the rest takes the hardware conversion.
-// The low 29 mantissa bits round into bit 29 (ties to even), a carry moves into the exponent,
-// and the exponent is rebased from 1023 to 127.
-__device__ __forceinline__ float d2f_rn(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned long long mag = b & 0x7fffffffffffffffull;
-  if (mag >= 0x3810000000000000ull && mag < 0x47efffffe0000000ull) {   // [2^-126, FLT_MAX)
-    const unsigned long long r = mag + 0x0fffffffull + ((mag >> 29) & 1ull);
-    const unsigned int f = (unsigned int)(r >> 29) - ((1023u - 127u) << 23);
-    return __uint_as_float(f | ((unsigned int)(b >> 32) & 0x80000000u));
-  }
-  return d2f_hw(x);
-}
+using fdfx::d2f_rn;   // double -> float on the integer pipe
 
 __device__ __forceinline__ long long nid(const GridDims &g, int i, int j, int k) {
   return ((long long)k * (g.JM + 1) + j) * (g.IM + 1) + i;

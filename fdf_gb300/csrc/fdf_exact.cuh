@@ -19,7 +19,6 @@ namespace fdfx {
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
 
 constexpr unsigned long long ABS_MASK = 0x7fffffffffffffffULL;
 constexpr unsigned long long INF_BITS = 0x7ff0000000000000ULL;
@@ -60,6 +59,129 @@ __device__ __forceinline__ double u32_to_double(unsigned int n) {
   return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | mant));
 }
 
+// ---------------------------------------------------------------------------------------
+// Division and conversions off the FP64 pipe.  On GB300 one warp-wide FP64 instruction holds
+// an SM sub-partition's FP64 unit for 64 cycles, while FP32 and integer instructions issue
+// every cycle or two; a correctly rounded double division (about ten FP64 instructions) or a
+// double <-> float conversion therefore costs far more than the same result built from
+// integer and FP32 operations.  Each routine below returns the IEEE result bit for bit; inputs
+// outside its fast range go to the hardware instruction, kept out of line so that the
+// compiler does not if-convert it into every lane.
+
+static __device__ __noinline__ double div_hw(double a, double b) { return __ddiv_rn(a, b); }
+static __device__ __noinline__ float d2f_hw(double x) { return __double2float_rn(x); }
+
+// double -> float, round to nearest even, on the integer pipe for results in the normal
+// float range; the rest takes the hardware conversion.  The low 29 mantissa bits round into
+// bit 29 (ties to even), a carry moves into the exponent, and the exponent is rebased from
+// 1023 to 127.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned long long b = ubits(x);
+  const unsigned long long mag = b & ABS_MASK;
+  if (mag >= 0x3810000000000000ull && mag < 0x47efffffe0000000ull) {   // [2^-126, FLT_MAX)
+    const unsigned long long r = mag + 0x0fffffffull + ((mag >> 29) & 1ull);
+    const unsigned int f = (unsigned int)(r >> 29) - ((1023u - 127u) << 23);
+    return __uint_as_float(f | ((unsigned int)(b >> 32) & 0x80000000u));
+  }
+  return d2f_hw(x);
+}
+
+// (hi, lo) = (fl32(x), fl32(x - fl32(x))): |x - (hi + lo)| <= 2^-48 |x|.  For 2^-74 <= |x| <
+// 2^127 it is built on the integer and FP32 pipes: hi as in d2f_rn; x - hi is an integer
+// number of x's ulps (|.| <= 2^28, the difference of the two bit patterns, which stays exact
+// across a binade carry), converted to float (one rounding: fl32(x - hi)) and scaled by
+// ulp(x) = 2^(E - 1075), a normal float there.  Zero gives (x, 0); the rest goes through FP64.
+__device__ __forceinline__ float2 split_rn(double x) {
+  const unsigned long long b = ubits(x);
+  const unsigned long long mag = b & ABS_MASK;
+  const unsigned int sgn = (unsigned int)(b >> 32) & 0x80000000u;
+  if (mag >= 0x3b50000000000000ull && mag < 0x47e0000000000000ull) {
+    const unsigned long long r = mag + 0x0fffffffull + ((mag >> 29) & 1ull);
+    const unsigned long long hmag = r & ~0x1fffffffull;
+    const float hi = __uint_as_float(((unsigned int)(r >> 29) - ((1023u - 127u) << 23)) | sgn);
+    const int units = (int)((long long)mag - (long long)hmag);
+    const float ulp = __uint_as_float((unsigned int)((mag >> 52) - 948ull) << 23);
+    const float lo = __fmul_rn(__int2float_rn(units), ulp);                 // x - hi == 0 gives +0
+    return make_float2(hi, __uint_as_float(__float_as_uint(lo) ^ (units != 0 ? sgn : 0u)));
+  }
+  if (mag == 0ull) return make_float2(__uint_as_float(sgn), 0.0f);
+  const float h = d2f_hw(x);
+  return make_float2(h, d2f_hw(__dsub_rn(x, (double)h)));
+}
+
+// Correctly rounded a / b (round to nearest even) from integer and FP32 operations, for
+// normal a (or zero) and b with a normal quotient; other operands take the hardware divide.
+// With ma, mb the 53-bit significands and s = 53 (ma >= mb) or 54, the quotient's 54-bit
+// truncation is Q = floor(ma 2^s / mb) and the result's significand is (Q + 1) >> 1: an exact
+// tie would need ma 2^s = mb Q with Q odd, impossible since mb < 2^53 cannot hold the factor
+// 2^s, so the rounding bit alone decides.  Q is found in three steps:
+//   1. a double-float quotient from 24 + 23-bit parts of ma and mb and a Newton-refined FP32
+//      reciprocal, |Q1 - Q| < 2^11;
+//   2. the exact remainder R1 = ma 2^s - Q1 mb (128-bit; |R1| < 2^65), its top bits times the
+//      reciprocal give the integer correction dl with |R1 / mb - dl| < 0.51;
+//   3. R2 = R1 - dl mb (exact in 64 bits), and Q = Q1 + dl - (R2 < 0).
+// A divisor used several times is prepared once (Divisor).
+struct Divisor {
+  double b;
+  unsigned long long ub, mb;
+  float fbh, fbl, r;
+  int eb;
+  bool normal;
+};
+
+__device__ __forceinline__ Divisor make_divisor(double b) {
+  Divisor d;
+  d.b = b;
+  d.ub = ubits(b);
+  d.eb = (int)((d.ub >> 52) & 0x7ff);
+  d.normal = d.eb != 0 && d.eb != 0x7ff;
+  d.mb = (d.ub & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  d.fbh = __uint_as_float(0x3f800000u | ((unsigned int)(d.mb >> 29) & 0x7fffffu));   // bits 52..29, in [1, 2)
+  d.fbl = __fmul_rn(__fsub_rn(__uint_as_float(0x4b000000u | ((unsigned int)(d.mb >> 6) & 0x7fffffu)), 8388608.0f),
+                    0x1p-46f);                                                       // bits 28..6
+  const float r0 = __fdividef(1.0f, d.fbh);                 // within 2 ulps
+  d.r = __fmaf_rn(r0, __fmaf_rn(-d.fbh, r0, 1.0f), r0);     // one Newton step
+  return d;
+}
+
+__device__ __forceinline__ double div_by(double a, const Divisor &d) {
+  const unsigned long long ua = ubits(a);
+  const unsigned long long sign = (ua ^ d.ub) & NEG_ZERO;
+  const int ea = (int)((ua >> 52) & 0x7ff), de = ea - d.eb;
+  if ((ua & ABS_MASK) == 0ull && d.normal) return __longlong_as_double((long long)sign);
+  if (!d.normal || ea == 0 || ea == 0x7ff || de < -1021 || de > 1021) return div_hw(a, d.b);
+  const unsigned long long ma = (ua & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  const float fah = __uint_as_float(0x3f800000u | ((unsigned int)(ma >> 29) & 0x7fffffu));
+  const float fal = __fmul_rn(__fsub_rn(__uint_as_float(0x4b000000u | ((unsigned int)(ma >> 6) & 0x7fffffu)), 8388608.0f),
+                              0x1p-46f);
+  const float qh = __fmul_rn(fah, d.r);
+  const float p = __fmul_rn(qh, d.fbh);
+  const float pe = __fmaf_rn(qh, d.fbh, -p);                              // exact error of p
+  const float rem = __fadd_rn(__fsub_rn(__fsub_rn(fah, p), pe), __fmaf_rn(-qh, d.fbl, fal));
+  const float ql = __fmul_rn(rem, d.r);
+  const int ge = ma >= d.mb;
+  const int s = 54 - ge;
+  const unsigned int qb = __float_as_uint(qh);
+  const int sh = s - 23 + (int)((qb >> 23) & 0xffu) - 127;              // qh in (0.5, 2): 29..32
+  unsigned long long Q = ((unsigned long long)((qb & 0x7fffffu) | 0x800000u) << sh) +
+                         (unsigned long long)((long long)__float2int_rn(__fmul_rn(ql, ge ? 0x1p42f : 0x1p43f)) << 11);
+  // R1 = ma 2^s - Q mb as (R_hi, R_lo), two's complement
+  const unsigned long long n_lo = ma << s, n_hi = ma >> (64 - s);
+  const unsigned long long p_lo = Q * d.mb, p_hi = __umul64hi(Q, d.mb);
+  const unsigned long long r_lo = n_lo - p_lo;
+  const unsigned long long r_hi = n_hi - p_hi - (n_lo < p_lo ? 1ull : 0ull);
+  const int t = (int)(unsigned int)((r_hi << 29) | (r_lo >> 35));          // R1 >> 35
+  const int dl = __float2int_rn(__fmul_rn(__fmul_rn(__int2float_rn(t), d.r), 0x1p-17f));
+  Q += (unsigned long long)(long long)dl;
+  const long long r2 = (long long)(r_lo - (unsigned long long)((long long)dl * (long long)d.mb));
+  Q -= (r2 < 0) ? 1ull : 0ull;
+  const unsigned long long qr = (Q + 1ull) >> 1;                           // [2^52, 2^53]
+  const unsigned long long e1 = (unsigned long long)(de + 1021 + ge);      // biased exponent - 1
+  return __longlong_as_double((long long)(sign | ((e1 << 52) + qr)));
+}
+
+__device__ __forceinline__ double div_rn(double a, double b) { return div_by(a, make_divisor(b)); }
+
 // x / n for an integer count n >= 1: x for n = 1, x * 2^-k (exact) for n = 2^k,
 // else the correctly rounded division -- all three equal the IEEE quotient.
 __device__ __forceinline__ double div_count(double x, unsigned int n) {
@@ -68,7 +190,7 @@ __device__ __forceinline__ double div_count(double x, unsigned int n) {
     const int e = 31 - __clz((int)n);
     return __dmul_rn(x, __longlong_as_double((long long)((unsigned long long)(1023 - e) << 52)));
   }
-  return __ddiv_rn(x, u32_to_double(n));
+  return div_rn(x, u32_to_double(n));
 }
 
 // PETSc's PetscMin / PetscMax macros: a<b ? a : b and a<b ? b : a.

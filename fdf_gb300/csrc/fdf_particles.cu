@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf ds
       if (fdfx::ubits(sw) == 0x3ff0000000000000ULL) {
         ux = ax; uy = ay; uz = az;
       } else {
-        ux = fdfx::div(ax, sw); uy = fdfx::div(ay, sw); uz = fdfx::div(az, sw);
+        const fdfx::Divisor dsw = fdfx::make_divisor(sw);
+        ux = fdfx::div_by(ax, dsw); uy = fdfx::div_by(ay, dsw); uz = fdfx::div_by(az, dsw);
       }
     }
   }

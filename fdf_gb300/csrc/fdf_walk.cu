@@ -68,10 +68,9 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS)
       // (hi, lo) within 2^-48 |v| of v; a nonzero |v| below 2^-120 (where the split's error is
       // absolute) gives a NaN pair, whose faces all take the FP64 route
       auto split = [](double v) {
-        const float h = __double2float_rn(v);
         const unsigned int hw = (unsigned int)__double2hiint(v) & 0x7fffffffu;
         if (hw < (903u << 20) && (hw | (unsigned int)__double2loint(v)) != 0u) return make_float2(__int_as_float(0x7fc00000), 0.f);
-        return make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+        return fdfx::split_rn(v);
       };
       Walk32 w;
       w.i = 0; w.j = 0; w.k = 0; w.err = 0u;   // InitializeTraversalParameters: previous cell, else (0,0,0)
@@ -94,9 +93,9 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS)
 #pragma unroll
         for (int f = 0; f < 6; ++f)
           if (fdfx::le_pos(d[f], tol_bits)) d[f] = FDF_INTERP_DIST_TOL;
-        b.a1[s] = __ddiv_rn(d[F_LEFT], add(d[F_LEFT], d[F_RIGHT]));
-        b.a2[s] = __ddiv_rn(d[F_BOTTOM], add(d[F_BOTTOM], d[F_TOP]));
-        b.a3[s] = __ddiv_rn(d[F_BACK], add(d[F_FRONT], d[F_BACK]));
+        b.a1[s] = fdfx::div_rn(d[F_LEFT], add(d[F_LEFT], d[F_RIGHT]));
+        b.a2[s] = fdfx::div_rn(d[F_BOTTOM], add(d[F_BOTTOM], d[F_TOP]));
+        b.a3[s] = fdfx::div_rn(d[F_BACK], add(d[F_FRONT], d[F_BACK]));
         st = ST_ACTIVE_AND_LOCATED;
       }
       b.cell[s] = cell;

@@ -1,0 +1,91 @@
+// Self-test of the off-FP64-pipe helpers in fdf_exact.cuh against the hardware instructions
+// they replace: div_rn / div_by against __ddiv_rn, d2f_rn against __double2float_rn, split_rn
+// against (fl32(x), fl32(x - fl32(x))), bit for bit, over seeded operands from several
+// distributions (random bit patterns with every exponent, the fast range, divisors near 1,
+// extreme significands, zeros, subnormals, infinities and NaNs).  Test infrastructure: built
+// by the GPU tests, not part of the library.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fdf_exact.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// An operand from distribution k of 8, from the random word r.
+__device__ double operand(uint64_t r, int k) {
+  const uint64_t frac = r & 0x000fffffffffffffull, sgn = (r >> 63) << 63;
+  const uint64_t e = (r >> 52) & 0x7ffull;
+  switch (k) {
+    case 0: return __longlong_as_double((long long)r);                                   // any bit pattern
+    case 1: return __longlong_as_double((long long)(sgn | ((960ull + (e % 128)) << 52) | frac));   // moderate range
+    case 2: return __longlong_as_double((long long)(((1023ull + (e % 3) - 1) << 52) | frac));   // near 1
+    case 3: {                                                                            // 1 +- a few ulps
+      const long long k2 = (long long)(e % 17) - 8;
+      return 1.0 + (double)k2 * 0x1p-52;
+    }
+    case 4: {                                                                            // extreme significands
+      const uint64_t f[4] = {0ull, 1ull, 0x000fffffffffffffull, 0x000ffffffffffffeull};
+      return __longlong_as_double((long long)(sgn | ((1000ull + (e % 48)) << 52) | f[(r >> 8) & 3]));
+    }
+    case 5: return __longlong_as_double((long long)(sgn | ((e % 64) << 52) | frac));   // subnormal / tiny
+    case 6: return __longlong_as_double((long long)(sgn | ((1985ull + (e % 63)) << 52) | frac));   // huge, inf, NaN
+    default: {                                                                           // a small integer count
+      return (double)(1 + (r % 1000));
+    }
+  }
+}
+
+__device__ __forceinline__ bool same(double a, double b) {
+  const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
+  const bool na = (ua & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+  const bool nb = (ub & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+  return (na && nb) || ua == ub;
+}
+__device__ __forceinline__ bool samef(float a, float b) {
+  return (a != a && b != b) || __float_as_uint(a) == __float_as_uint(b);
+}
+
+// out[0..2]: division, d2f, split mismatches; out[4..5]: the first bad division's operands.
+__global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const uint64_t r1 = mix(seed ^ (2 * (uint64_t)t)), r2 = mix(seed ^ (2 * (uint64_t)t + 1)), r3 = mix(r1 ^ r2);
+    const double a = operand(r1, (int)(r3 & 7)), b = operand(r2, (int)((r3 >> 3) & 7));
+    const double q = fdfx::div_rn(a, b), qh = __ddiv_rn(a, b);
+    if (!same(q, qh)) {
+      if (atomicAdd(&out[0], 1ull) == 0ull) {
+        out[4] = (unsigned long long)__double_as_longlong(a);
+        out[5] = (unsigned long long)__double_as_longlong(b);
+      }
+    }
+    if (!samef(fdfx::d2f_rn(a), __double2float_rn(a))) atomicAdd(&out[1], 1ull);
+    const float2 p = fdfx::split_rn(a);
+    const float h = __double2float_rn(a);
+    const float l = __double2float_rn(__dsub_rn(a, (double)h));
+    if (!samef(p.x, h) || !samef(p.y, l)) atomicAdd(&out[2], 1ull);
+  }
+}
+
+}  // namespace
+
+// Runs n cases from the seed; writes the six counters to host memory.  Returns a CUDA error code.
+extern "C" int fdf_test_exact(unsigned long long seed, long long n, unsigned long long *host_out) {
+  unsigned long long *d = nullptr;
+  cudaError_t e = cudaMalloc((void **)&d, 6 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return (int)e;
+  e = cudaMemset(d, 0, 6 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    k_check<<<152 * 8, 256>>>(seed, n, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  host_out[3] = (unsigned long long)n;
+  return (int)e;
+}

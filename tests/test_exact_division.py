@@ -1,0 +1,122 @@
+"""The division of fdf_exact.cuh (div_by) restated step by step in Python: FP32 steps in numpy
+float32 (round to nearest), integer steps in Python integers with the kernel's 64-bit wrap,
+the reciprocal perturbed by up to 2^-22 (the approximate reciprocal's 2 ulps) before its Newton
+step.  Checks the bounds the kernel relies on (|Q1 - Q| < 2^11, |R1| < 2^65, R2 in (-mb, mb),
+the 32-bit top word of R1) and that the result is Python's correctly rounded quotient."""
+import random
+import struct
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+M64 = (1 << 64) - 1
+F = np.float32
+
+
+def _ub(x):
+    return struct.unpack("<Q", struct.pack("<d", x))[0]
+
+
+def _fb(u):
+    return struct.unpack("<d", struct.pack("<Q", u & M64))[0]
+
+
+def _u2f(u):
+    return np.frombuffer(struct.pack("<I", u & 0xFFFFFFFF), dtype=np.float32)[0]
+
+
+def _f2u(f):
+    return struct.unpack("<I", np.float32(f).tobytes())[0]
+
+
+def _fma(a, b, c):
+    """fl32(a * b + c) with a single rounding."""
+    v = Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c))
+    r = np.float32(float(v))
+    cands = [r, np.nextafter(r, F(np.inf)), np.nextafter(r, F(-np.inf))]
+    return min(cands, key=lambda c: (abs(Fraction(float(c)) - v), _f2u(c) & 1))
+
+
+def _parts(m):
+    hi = _u2f(0x3F800000 | ((m >> 29) & 0x7FFFFF))
+    lo = F(F(_u2f(0x4B000000 | ((m >> 6) & 0x7FFFFF)) - F(8388608.0)) * F(2.0 ** -46))
+    return hi, lo
+
+
+def div_by(a, b, rcp_err):
+    ua, ub = _ub(a), _ub(b)
+    ea, eb = (ua >> 52) & 0x7FF, (ub >> 52) & 0x7FF
+    de = ea - eb
+    assert 0 < ea < 0x7FF and 0 < eb < 0x7FF and -1021 <= de <= 1021
+    ma = (ua & ((1 << 52) - 1)) | (1 << 52)
+    mb = (ub & ((1 << 52) - 1)) | (1 << 52)
+    fbh, fbl = _parts(mb)
+    r0 = F(float(F(1.0) / fbh) * (1.0 + rcp_err))
+    r = _fma(r0, _fma(-fbh, r0, F(1.0)), r0)
+    fah, fal = _parts(ma)
+    qh = F(fah * r)
+    p = F(qh * fbh)
+    pe = _fma(qh, fbh, -p)
+    rem = F(F(F(fah - p) - pe) + _fma(-qh, fbl, fal))
+    ql = F(rem * r)
+    ge = 1 if ma >= mb else 0
+    s = 54 - ge
+    qb = _f2u(qh)
+    sh = s - 23 + ((qb >> 23) & 0xFF) - 127
+    assert 29 <= sh <= 32
+    x = F(ql * F(2.0 ** (42 + 1 - ge)))
+    assert abs(float(x)) < 2 ** 31
+    Q1 = (((qb & 0x7FFFFF) | 0x800000) << sh) + (int(np.rint(x)) << 11)
+    Q = (ma << s) // mb
+    assert abs(Q1 - Q) < 2 ** 11, (a, b, Q1 - Q)
+    n_lo, n_hi = (ma << s) & M64, ma >> (64 - s)
+    prod = Q1 * mb
+    p_lo, p_hi = prod & M64, (prod >> 64) & M64
+    r_lo = (n_lo - p_lo) & M64
+    r_hi = (n_hi - p_hi - (1 if n_lo < p_lo else 0)) & M64
+    R1 = (ma << s) - Q1 * mb
+    assert abs(R1) < 2 ** 65
+    t = ((r_hi << 29) | (r_lo >> 35)) & 0xFFFFFFFF
+    t = t - (1 << 32) if t >= 1 << 31 else t
+    assert t == R1 >> 35
+    dl = int(np.rint(F(F(F(t) * r) * F(2.0 ** -17))))
+    Qc = Q1 + dl
+    r2 = (r_lo - ((dl * mb) & M64)) & M64
+    r2 = r2 - (1 << 64) if r2 >= 1 << 63 else r2
+    assert r2 == R1 - dl * mb and -mb < r2 < mb
+    Qc -= 1 if r2 < 0 else 0
+    assert Qc == Q
+    qr = (Qc + 1) >> 1
+    return _fb(((ua ^ ub) & (1 << 63)) | (((de + 1021 + ge) << 52) + qr))
+
+
+def _cases(n, seed):
+    rng = random.Random(seed)
+    ext = [(1 << 53) - 1, 1 << 52, (1 << 52) + 1, (1 << 53) - 2]
+    for i in range(n):
+        a = rng.uniform(1, 2) * 2.0 ** rng.randint(-80, 80) * rng.choice([1, -1])
+        b = rng.uniform(1, 2) * 2.0 ** rng.randint(-80, 80) * rng.choice([1, -1])
+        if i % 3 == 0:
+            b = 1.0 + rng.randint(-8, 8) * 2.0 ** -52          # a trilinear weight sum
+        if i % 4 == 0:
+            a = rng.choice(ext) * 2.0 ** rng.randint(-60, -40)
+        if i % 5 == 0:
+            b = rng.choice(ext) * 2.0 ** rng.randint(-60, -40)
+        if i % 7 == 0:
+            b = float(rng.randint(3, 1000))                  # a particle count
+        yield a, b, rng.uniform(-2.0 ** -22, 2.0 ** -22)
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_division_restatement_is_correctly_rounded(seed):
+    for a, b, e in _cases(4000, seed):
+        q = div_by(a, b, e)
+        assert _ub(q) == _ub(a / b), (a, b)
+
+
+def test_division_extreme_reciprocal_errors():
+    for a in (1.0, 2.0 - 2.0 ** -52, 1.0 + 2.0 ** -52, 1.5, 0.1, 1e-14, 1 / 3):
+        for b in (1.0, 2.0 - 2.0 ** -52, 1.0 + 2.0 ** -52, 3.0, 0.1, 2e-14, 7.0):
+            for e in (2.0 ** -22, -(2.0 ** -22), 0.0):
+                assert _ub(div_by(a, b, e)) == _ub(a / b)
