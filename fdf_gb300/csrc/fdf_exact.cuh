@@ -182,14 +182,23 @@ __device__ __forceinline__ double div_by(double a, const Divisor &d) {
 
 __device__ __forceinline__ double div_rn(double a, double b) { return div_by(a, make_divisor(b)); }
 
+// x * 2^-k for 0 <= k <= 52: an exponent decrement on the integer pipe while the product stays
+// normal (then exact, as the FP64 multiply is); zeros, infinities and NaNs are their own
+// products; a subnormal product takes the FP64 multiply, which rounds it.
+static __device__ __noinline__ double mul_hw(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double scale_down(double x, int k) {
+  const unsigned long long b = ubits(x);
+  const unsigned long long e = (b >> 52) & 0x7ffull;
+  if (e > (unsigned long long)k && e != 0x7ffull) return __longlong_as_double((long long)(b - ((unsigned long long)k << 52)));
+  if ((b & ABS_MASK) == 0ull || e == 0x7ffull) return x;
+  return mul_hw(x, __longlong_as_double((long long)((unsigned long long)(1023 - k) << 52)));
+}
+
 // x / n for an integer count n >= 1: x for n = 1, x * 2^-k (exact) for n = 2^k,
 // else the correctly rounded division -- all three equal the IEEE quotient.
 __device__ __forceinline__ double div_count(double x, unsigned int n) {
   if (n == 1) return x;
-  if ((n & (n - 1)) == 0) {
-    const int e = 31 - __clz((int)n);
-    return __dmul_rn(x, __longlong_as_double((long long)((unsigned long long)(1023 - e) << 52)));
-  }
+  if ((n & (n - 1)) == 0) return scale_down(x, 31 - __clz((int)n));
   return div_rn(x, u32_to_double(n));
 }
 

@@ -148,8 +148,8 @@ __global__ void k_center_to_corner(const double *__restrict__ ucat, GridDims g, 
   }
   double ox = 0.0, oy = 0.0, oz = 0.0;
   if (count > 0) {
-    const double r = count == 1 ? 1.0 : count == 2 ? 0.5 : count == 4 ? 0.25 : 0.125;
-    ox = mul(sx, r); oy = mul(sy, r); oz = mul(sz, r);
+    const int sh = count == 1 ? 0 : count == 2 ? 1 : count == 4 ? 2 : 3;   // sum * 0.5^sh, exact
+    ox = fdfx::scale_down(sx, sh); oy = fdfx::scale_down(sy, sh); oz = fdfx::scale_down(sz, sh);
   }
   corner[q] = ox; corner[g.Nn + q] = oy; corner[2 * g.Nn + q] = oz;
 }

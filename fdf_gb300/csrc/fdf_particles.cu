@@ -94,80 +94,229 @@ __global__ void __launch_bounds__(256) k_gather_interp(SwarmBuf src, SwarmBuf ds
 // corner is this node: i-face (i,j,k) between cells i-1 and i, and likewise j, k.
 // A face sums its lower cell's particles (weight a) and then its upper cell's
 // (weight 1-a), each in sorted order: a fixed order, so the sum is deterministic.
-// Face deposits of the sorted segments; MOM adds the same split of V * velocity
-// (SoA [3][faces]), each component summed in the same order.
-template <bool MOM>
-__global__ void __launch_bounds__(256) k_deposit(SwarmBuf b, GridDims g, const unsigned int *__restrict__ cs,
-                                                 double third, double *__restrict__ count,
-                                                 double *__restrict__ avg, double *__restrict__ fi,
-                                                 double *__restrict__ fj, double *__restrict__ fk,
-                                                 double *__restrict__ mi, double *__restrict__ mj,
-                                                 double *__restrict__ mk) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= g.Nn) return;
+// The momentum variant adds the same split of V * velocity (SoA [3][faces]), each component
+// summed in the same order.
+//
+// The products are moved out of the per-node loops.  A node's four segment loops have
+// different lengths across a warp, and a warp-wide FP64 instruction costs the same with one
+// active lane as with 32; so the warp's 32 consecutive nodes first compute, lanes striding over
+// whole particle ranges, every product their loops will add -- a * V/3 for the three lower
+// faces, (1 - a) * V/3 for the upper ones -- into shared memory, and the divergent loops then
+// only add.  The lower-cell (and own-cell)
+// cells of consecutive nodes are consecutive cells, so each of the four roles is one
+// contiguous particle range per warp.  A warp whose range exceeds DEP_CAP particles computes
+// the products in its loops.  Every sum takes the same values in the same order either way.
+constexpr int DEP_WARPS = 8;
+constexpr int DEP_CAP = 256;
+
+__global__ void __launch_bounds__(DEP_WARPS * 32) k_deposit_staged(SwarmBuf b, GridDims g,
+                                                                    const unsigned int *__restrict__ cs, double third,
+                                                                    double *__restrict__ count,
+                                                                    double *__restrict__ avg, double *__restrict__ fi,
+                                                                    double *__restrict__ fj, double *__restrict__ fk) {
+  __shared__ double stage[DEP_WARPS][3][DEP_CAP];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long long q = (blockIdx.x * (long long)DEP_WARPS + wid) * 32 + lane;
+  if (q - lane >= g.Nn) return;   // the whole warp is past the last node
+  const bool node = q < g.Nn;
   const int IM = g.IM, JM = g.JM, KM = g.KM;
-  int i, j, k;
-  node_ijk(g, (unsigned int)q, i, j, k);
-  const bool is_cell = i < IM && j < JM && k < KM;
+  int i = 0, j = 0, k = 0;
+  if (node) node_ijk(g, (unsigned int)q, i, j, k);
   const long long c = ((long long)k * JM + j) * IM + i;
-  int s0 = 0, s1 = 0;
-  if (is_cell) { s0 = (int)__ldg(cs + c); s1 = (int)__ldg(cs + c + 1); }
-  // Face accumulators: per face the lower cell's segment (weight a) first, then this cell's
-  // (weight 1 - a).  The three lower segments run first; this cell's segment then feeds the P
-  // sum and the three faces' upper parts in one pass, so every accumulator still receives its
-  // values in the order above.
-  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
-  const bool face_i = j < JM && k < KM, face_j = i < IM && k < KM, face_k = i < IM && j < JM;
-  double acc[3] = {0.0, 0.0, 0.0}, mm[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
-  auto lower = [&](int f, const double *__restrict__ wgt, long long lc) {
-    const int l0 = (int)__ldg(cs + lc), l1 = (int)__ldg(cs + lc + 1);
-    for (int s = l0; s < l1; ++s) {
-      const double fr = mul(__ldg(wgt + s), third);
-      acc[f] = add(acc[f], fr);
-      if (MOM) {
-        mm[f][0] = add(mm[f][0], mul(fr, __ldg(b.u + s)));
-        mm[f][1] = add(mm[f][1], mul(fr, __ldg(b.v + s)));
-        mm[f][2] = add(mm[f][2], mul(fr, __ldg(b.w + s)));
-      }
+  const bool face_i = node && j < JM && k < KM, face_j = node && i < IM && k < KM, face_k = node && i < IM && j < JM;
+  const bool is_cell = node && i < IM && j < JM && k < KM;
+  // the cell of each role: lower i, lower j, lower k, own (0xffffffff: none)
+  const unsigned int NONE = 0xffffffffu;
+  unsigned int rc[4];
+  rc[0] = (face_i && i > 0) ? (unsigned int)(c - 1) : NONE;
+  rc[1] = (face_j && j > 0) ? (unsigned int)(c - IM) : NONE;
+  rc[2] = (face_k && k > 0) ? (unsigned int)(c - (long long)IM * JM) : NONE;
+  rc[3] = is_cell ? (unsigned int)c : NONE;
+  // each role's particle range for the warp: [p0, p1)
+  unsigned int p0[4], p1[4];
+  bool staged = true;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const unsigned int lo = __reduce_min_sync(0xffffffffu, rc[r]);
+    const unsigned int hi = __reduce_max_sync(0xffffffffu, rc[r] == NONE ? 0u : rc[r]);
+    p0[r] = 0u;
+    p1[r] = 0u;
+    if (lo != NONE) {
+      p0[r] = __ldg(cs + lo);
+      p1[r] = __ldg(cs + hi + 1);
+      staged = staged && p1[r] - p0[r] <= (unsigned int)DEP_CAP;
     }
-  };
-  if (face_i && i > 0) lower(0, b.a1, c - 1);
-  if (face_j && j > 0) lower(1, b.a2, ((long long)k * JM + (j - 1)) * IM + i);
-  if (face_k && k > 0) lower(2, b.a3, ((long long)(k - 1) * JM + j) * IM + i);
-  // AccumulateParticleField + CalculateParticleCountPerCell + NormalizeGridVectorByCount, and
-  // the upper parts of the three faces (a cell node owns all three)
-  double sum = 0.0;
-  for (int s = s0; s < s1; ++s) {
-    const double P = __ldg(b.P + s);
-    sum = (s == s0) ? fdfx::add0(P) : add(sum, P);
-    const double w[3] = {__ldg(b.a1 + s), __ldg(b.a2 + s), __ldg(b.a3 + s)};
-    double u = 0.0, v = 0.0, ww = 0.0;
-    if (MOM) { u = __ldg(b.u + s); v = __ldg(b.v + s); ww = __ldg(b.w + s); }
+  }
+  double acc[3] = {0.0, 0.0, 0.0};
+  const double *wgt[3] = {b.a1, b.a2, b.a3};
+  if (staged) {
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+      for (unsigned int s = p0[f] + lane; s < p1[f]; s += 32) stage[wid][f][s - p0[f]] = mul(__ldg(wgt[f] + s), third);
+    __syncwarp();
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
-      const double fr = mul(sub(1.0, w[f]), third);
-      acc[f] = add(acc[f], fr);
-      if (MOM) {
-        mm[f][0] = add(mm[f][0], mul(fr, u));
-        mm[f][1] = add(mm[f][1], mul(fr, v));
-        mm[f][2] = add(mm[f][2], mul(fr, ww));
-      }
+      if (rc[f] == NONE) continue;
+      const unsigned int l0 = __ldg(cs + rc[f]), l1 = __ldg(cs + rc[f] + 1);
+      for (unsigned int s = l0; s < l1; ++s) acc[f] = add(acc[f], stage[wid][f][s - p0[f]]);
+    }
+    __syncwarp();
+  } else {
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      if (rc[f] == NONE) continue;
+      const unsigned int l0 = __ldg(cs + rc[f]), l1 = __ldg(cs + rc[f] + 1);
+      for (unsigned int s = l0; s < l1; ++s) acc[f] = add(acc[f], mul(__ldg(wgt[f] + s), third));
     }
   }
-  {
-    const unsigned int ncell = (unsigned int)(s1 - s0);   // count += 1.0 per particle is exact in FP64
-    count[q] = fdfx::u32_to_double(ncell);
-    double a = 0.0;
-    if (ncell > 0) a = fdfx::div_count(sum, ncell);
-    avg[q] = a;
+  // AccumulateParticleField + CalculateParticleCountPerCell + NormalizeGridVectorByCount, and
+  // the upper parts of the three faces
+  unsigned int s0 = 0u, s1 = 0u;
+  if (is_cell) { s0 = __ldg(cs + c); s1 = __ldg(cs + c + 1); }
+  double sum = 0.0;
+  for (unsigned int s = s0; s < s1; ++s) {
+    const double P = __ldg(b.P + s);
+    sum = (s == s0) ? fdfx::add0(P) : add(sum, P);
   }
+  if (staged) {
+    for (unsigned int s = p0[3] + lane; s < p1[3]; s += 32) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f) stage[wid][f][s - p0[3]] = mul(sub(1.0, __ldg(wgt[f] + s)), third);
+    }
+    __syncwarp();
+    for (unsigned int s = s0; s < s1; ++s) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f) acc[f] = add(acc[f], stage[wid][f][s - p0[3]]);
+    }
+  } else {
+    for (unsigned int s = s0; s < s1; ++s) {
+#pragma unroll
+      for (int f = 0; f < 3; ++f) acc[f] = add(acc[f], mul(sub(1.0, __ldg(wgt[f] + s)), third));
+    }
+  }
+  if (!node) return;
+  {
+    const unsigned int ncell = s1 - s0;   // count += 1.0 per particle is exact in FP64
+    count[q] = fdfx::u32_to_double(ncell);
+    avg[q] = ncell > 0 ? fdfx::div_count(sum, ncell) : 0.0;
+  }
+  if (face_i) fi[((long long)k * JM + j) * (IM + 1) + i] = acc[0];   // i-face (i,j,k), i in [0, IM]
+  if (face_j) fj[((long long)k * (JM + 1) + j) * IM + i] = acc[1];   // j-face (i,j,k), j in [0, JM]
+  if (face_k) fk[c] = acc[2];                                        // k-face (i,j,k), k in [0, KM]
+}
+
+
+// The volume and momentum deposit -- the sums above, bit for bit -- staged like
+// k_deposit_staged, one face role at a time: for a lower role, V/3 a and its products with the
+// three velocity components; for an upper role, V/3 (1 - a) and its three products.  Each
+// role's values for the warp's particle range go to shared memory (four arrays), and the
+// per-node loops only add them, each accumulator in the same order.
+constexpr int DEPM_WARPS = 4;
+
+__global__ void __launch_bounds__(DEPM_WARPS * 32) k_deposit_mom_staged(SwarmBuf b, GridDims g,
+                                                                         const unsigned int *__restrict__ cs,
+                                                                         double third, double *__restrict__ count,
+                                                                         double *__restrict__ avg,
+                                                                         double *__restrict__ fi,
+                                                                         double *__restrict__ fj,
+                                                                         double *__restrict__ fk,
+                                                                         double *__restrict__ mi,
+                                                                         double *__restrict__ mj,
+                                                                         double *__restrict__ mk) {
+  __shared__ double stage[DEPM_WARPS][4][DEP_CAP];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long long q = (blockIdx.x * (long long)DEPM_WARPS + wid) * 32 + lane;
+  if (q - lane >= g.Nn) return;   // the whole warp is past the last node
+  const bool node = q < g.Nn;
+  const int IM = g.IM, JM = g.JM, KM = g.KM;
+  int i = 0, j = 0, k = 0;
+  if (node) node_ijk(g, (unsigned int)q, i, j, k);
+  const long long c = ((long long)k * JM + j) * IM + i;
+  const bool face_i = node && j < JM && k < KM, face_j = node && i < IM && k < KM, face_k = node && i < IM && j < JM;
+  const bool is_cell = node && i < IM && j < JM && k < KM;
+  const unsigned int NONE = 0xffffffffu;
+  unsigned int rc[4];
+  rc[0] = (face_i && i > 0) ? (unsigned int)(c - 1) : NONE;
+  rc[1] = (face_j && j > 0) ? (unsigned int)(c - IM) : NONE;
+  rc[2] = (face_k && k > 0) ? (unsigned int)(c - (long long)IM * JM) : NONE;
+  rc[3] = is_cell ? (unsigned int)c : NONE;
+  unsigned int p0[4], p1[4];
+  bool staged = true;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const unsigned int lo = __reduce_min_sync(0xffffffffu, rc[r]);
+    const unsigned int hi = __reduce_max_sync(0xffffffffu, rc[r] == NONE ? 0u : rc[r]);
+    p0[r] = 0u;
+    p1[r] = 0u;
+    if (lo != NONE) {
+      p0[r] = __ldg(cs + lo);
+      p1[r] = __ldg(cs + hi + 1);
+      staged = staged && p1[r] - p0[r] <= (unsigned int)DEP_CAP;
+    }
+  }
+  const double *wgt[3] = {b.a1, b.a2, b.a3};
+  double acc[3] = {0.0, 0.0, 0.0}, mm[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+  double (*st)[DEP_CAP] = stage[wid];
+  // one role: the values of particle s are (x, x u, x v, x w) with x = V/3 a (lower) or
+  // V/3 (1 - a) (upper) of face f; the node's segment is [l0, l1), the warp's [r0, r1)
+  auto role = [&](int f, bool upper, unsigned int r0, unsigned int r1, unsigned int l0, unsigned int l1) {
+    if (staged) {
+      for (unsigned int s = r0 + lane; s < r1; s += 32) {
+        const double a = __ldg(wgt[f] + s);
+        const double x = mul(upper ? sub(1.0, a) : a, third);
+        st[0][s - r0] = x;
+        st[1][s - r0] = mul(x, __ldg(b.u + s));
+        st[2][s - r0] = mul(x, __ldg(b.v + s));
+        st[3][s - r0] = mul(x, __ldg(b.w + s));
+      }
+      __syncwarp();
+      for (unsigned int s = l0; s < l1; ++s) {
+        acc[f] = add(acc[f], st[0][s - r0]);
+        mm[f][0] = add(mm[f][0], st[1][s - r0]);
+        mm[f][1] = add(mm[f][1], st[2][s - r0]);
+        mm[f][2] = add(mm[f][2], st[3][s - r0]);
+      }
+      __syncwarp();
+    } else {
+      for (unsigned int s = l0; s < l1; ++s) {
+        const double a = __ldg(wgt[f] + s);
+        const double x = mul(upper ? sub(1.0, a) : a, third);
+        acc[f] = add(acc[f], x);
+        mm[f][0] = add(mm[f][0], mul(x, __ldg(b.u + s)));
+        mm[f][1] = add(mm[f][1], mul(x, __ldg(b.v + s)));
+        mm[f][2] = add(mm[f][2], mul(x, __ldg(b.w + s)));
+      }
+    }
+  };
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    unsigned int l0 = 0u, l1 = 0u;
+    if (rc[f] != NONE) { l0 = __ldg(cs + rc[f]); l1 = __ldg(cs + rc[f] + 1); }
+    role(f, false, p0[f], p1[f], l0, l1);
+  }
+  unsigned int s0 = 0u, s1 = 0u;
+  if (is_cell) { s0 = __ldg(cs + c); s1 = __ldg(cs + c + 1); }
+  double sum = 0.0;
+  for (unsigned int s = s0; s < s1; ++s) {
+    const double P = __ldg(b.P + s);
+    sum = (s == s0) ? fdfx::add0(P) : add(sum, P);
+  }
+#pragma unroll
+  for (int f = 0; f < 3; ++f) role(f, true, p0[3], p1[3], s0, s1);
+  if (!node) return;
+  {
+    const unsigned int ncell = s1 - s0;
+    count[q] = fdfx::u32_to_double(ncell);
+    avg[q] = ncell > 0 ? fdfx::div_count(sum, ncell) : 0.0;
+  }
+  const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
   auto store = [&](int f, double *vol, double *mom, long long nf, long long fidx) {
     vol[fidx] = acc[f];
-    if (MOM) { mom[fidx] = mm[f][0]; mom[nf + fidx] = mm[f][1]; mom[2 * nf + fidx] = mm[f][2]; }
+    mom[fidx] = mm[f][0]; mom[nf + fidx] = mm[f][1]; mom[2 * nf + fidx] = mm[f][2];
   };
-  if (face_i) store(0, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);   // i-face (i,j,k), i in [0, IM]
-  if (face_j) store(1, fj, mj, nfj, ((long long)k * (JM + 1) + j) * IM + i);   // j-face (i,j,k), j in [0, JM]
-  if (face_k) store(2, fk, mk, nfk, c);                                        // k-face (i,j,k), k in [0, KM]
+  if (face_i) store(0, fi, mi, nfi, ((long long)k * JM + j) * (IM + 1) + i);
+  if (face_j) store(1, fj, mj, nfj, ((long long)k * (JM + 1) + j) * IM + i);
+  if (face_k) store(2, fk, mk, nfk, c);
 }
 
 __global__ void k_from_aos(const double *__restrict__ pos, const double *__restrict__ vel,
@@ -253,10 +402,11 @@ void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_star
   long long blocks = (g.Nn + th - 1) / th;
   double third = volume / 3.0;
   if (mi)
-    k_deposit<true><<<(unsigned)blocks, th, 0, s>>>(b, g, cell_start, third, count, avg, fi, fj, fk, mi, mj, mk);
+    k_deposit_mom_staged<<<(unsigned)((g.Nn + DEPM_WARPS * 32 - 1) / (DEPM_WARPS * 32)), DEPM_WARPS * 32, 0, s>>>(
+        b, g, cell_start, third, count, avg, fi, fj, fk, mi, mj, mk);
   else
-    k_deposit<false><<<(unsigned)blocks, th, 0, s>>>(b, g, cell_start, third, count, avg, fi, fj, fk, nullptr,
-                                                     nullptr, nullptr);
+    k_deposit_staged<<<(unsigned)((g.Nn + DEP_WARPS * 32 - 1) / (DEP_WARPS * 32)), DEP_WARPS * 32, 0, s>>>(
+        b, g, cell_start, third, count, avg, fi, fj, fk);
 }
 
 void launch_swarm_from_aos(const double *pos, const double *vel, const double *wgt, const double *P,

@@ -52,7 +52,8 @@ __device__ __forceinline__ bool samef(float a, float b) {
   return (a != a && b != b) || __float_as_uint(a) == __float_as_uint(b);
 }
 
-// out[0..2]: division, d2f, split mismatches; out[4..5]: the first bad division's operands.
+// out[0..2]: division, d2f, split mismatches; out[4..5]: the first bad division's operands;
+// out[6]: scale_down mismatches.
 __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const uint64_t r1 = mix(seed ^ (2 * (uint64_t)t)), r2 = mix(seed ^ (2 * (uint64_t)t + 1)), r3 = mix(r1 ^ r2);
@@ -69,22 +70,25 @@ __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
     const float h = __double2float_rn(a);
     const float l = __double2float_rn(__dsub_rn(a, (double)h));
     if (!samef(p.x, h) || !samef(p.y, l)) atomicAdd(&out[2], 1ull);
+    const int k = (int)((r3 >> 8) % 53);
+    if (!same(fdfx::scale_down(a, k), __dmul_rn(a, __longlong_as_double((long long)((uint64_t)(1023 - k) << 52)))))
+      atomicAdd(&out[6], 1ull);
   }
 }
 
 }  // namespace
 
-// Runs n cases from the seed; writes the six counters to host memory.  Returns a CUDA error code.
+// Runs n cases from the seed; writes the seven counters to host memory.  Returns a CUDA error code.
 extern "C" int fdf_test_exact(unsigned long long seed, long long n, unsigned long long *host_out) {
   unsigned long long *d = nullptr;
-  cudaError_t e = cudaMalloc((void **)&d, 6 * sizeof(unsigned long long));
+  cudaError_t e = cudaMalloc((void **)&d, 7 * sizeof(unsigned long long));
   if (e != cudaSuccess) return (int)e;
-  e = cudaMemset(d, 0, 6 * sizeof(unsigned long long));
+  e = cudaMemset(d, 0, 7 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     k_check<<<152 * 8, 256>>>(seed, n, d);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   host_out[3] = (unsigned long long)n;
   return (int)e;
