@@ -12,6 +12,7 @@
 //   deposit (cell count / P average, face volumes) from the sorted segments
 #include "fdf_context.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -40,6 +41,7 @@ int fdf_ContextCreate(FdfContext **out, int device) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_scan, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_corner, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_xfer, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->cnt, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMemset(ctx->cnt, 0, sizeof(DevCounters));
   if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->bbox, 6 * sizeof(double));
@@ -71,6 +73,7 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->ev_scan) cudaEventDestroy(ctx->ev_scan);
   if (ctx->ev_corner) cudaEventDestroy(ctx->ev_corner);
+  if (ctx->ev_xfer) cudaEventDestroy(ctx->ev_xfer);
   if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -239,6 +242,20 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   return FDF_SUCCESS;
 }
 
+// The swarm buffers from particle `off` on.
+static SwarmBuf shifted(const SwarmBuf &b, long long off) {
+  SwarmBuf r = b;
+  auto sh = [off](auto *&p) { if (p) p += off; };
+  sh(r.x); sh(r.y); sh(r.z); sh(r.u); sh(r.v); sh(r.w); sh(r.a1); sh(r.a2); sh(r.a3); sh(r.P);
+  sh(r.uf); sh(r.vf); sh(r.wf); sh(r.a1f); sh(r.a2f); sh(r.a3f); sh(r.Pf); sh(r.pid); sh(r.cell); sh(r.status);
+  return r;
+}
+
+// Host <-> device swarm transfers run in chunks of particles on two streams: the copies of
+// one chunk (side stream) overlap the layout conversion of the previous one (context stream),
+// so a transfer costs about its copies alone.
+static int64_t transfer_chunk(int64_t n) { return std::max<int64_t>(int64_t(1) << 22, (n + 7) / 8); }
+
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity, const double *weight,
                  const double *P, const int64_t *cell_id, const int64_t *pid, const int64_t *status) {
   if (!ctx) return FDF_ERR_ARG_NULL;
@@ -255,20 +272,32 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
   if (n > 0) {
-    CU(cudaMemcpyAsync(d_pos, position, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(d_vel, velocity, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(d_wgt, weight, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(d_P, P, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(d_cell, cell_id, 24ull * n, cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(d_pid, pid, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
-    CU(cudaMemcpyAsync(d_st, status, 8ull * n, cudaMemcpyHostToDevice, ctx->stream));
     ctx->cur = 0;
-    if (form_is32(ctx->form))
-      launch_swarm_from_aos32(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
-    else
-      launch_swarm_from_aos(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, ctx->buf[0], ctx->stream);
-    CHECK_LAUNCH();
-    ctx->launches += 1;
+    // the side stream starts after everything already queued on the context stream
+    CU(cudaEventRecord(ctx->ev_xfer, ctx->stream));
+    CU(cudaStreamWaitEvent(ctx->side, ctx->ev_xfer, 0));
+    const int64_t chunk = transfer_chunk(n);
+    for (int64_t o = 0; o < n; o += chunk) {
+      const int64_t m = std::min(chunk, n - o);
+      CU(cudaMemcpyAsync(d_pos + 3 * o, position + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaMemcpyAsync(d_vel + 3 * o, velocity + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaMemcpyAsync(d_wgt + 3 * o, weight + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaMemcpyAsync(d_P + o, P + o, 8ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaMemcpyAsync(d_cell + 3 * o, cell_id + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaMemcpyAsync(d_pid + o, pid + o, 8ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaMemcpyAsync(d_st + o, status + o, 8ull * m, cudaMemcpyHostToDevice, ctx->side));
+      CU(cudaEventRecord(ctx->ev_xfer, ctx->side));
+      CU(cudaStreamWaitEvent(ctx->stream, ctx->ev_xfer, 0));
+      const SwarmBuf b = shifted(ctx->buf[0], o);
+      if (form_is32(ctx->form))
+        launch_swarm_from_aos32(d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o, d_pid + o,
+                                d_st + o, (int)m, ctx->g, b, ctx->stream);
+      else
+        launch_swarm_from_aos(d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o, d_pid + o,
+                              d_st + o, (int)m, ctx->g, b, ctx->stream);
+      CHECK_LAUNCH();
+      ctx->launches += 1;
+    }
   }
   DevCounters c{};
   c.n = (int)n;
@@ -334,21 +363,29 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *positio
   char *st = (char *)ctx->staging;
   double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
-  if (form_is32(ctx->swarm_form))
-    launch_swarm_to_aos32(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
-                          ctx->stream);
-  else
-    launch_swarm_to_aos(ctx->buf[ctx->cur], (int)n, ctx->g, d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st,
-                        ctx->stream);
-  CHECK_LAUNCH();
-  ctx->launches += 1;
-  CU(cudaMemcpyAsync(position, d_pos, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(velocity, d_vel, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(weight, d_wgt, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(P, d_P, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(cell_id, d_cell, 24ull * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(pid, d_pid, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaMemcpyAsync(status, d_st, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  const int64_t chunk = transfer_chunk(n);
+  for (int64_t o = 0; o < n; o += chunk) {
+    const int64_t m = std::min(chunk, n - o);
+    const SwarmBuf b = shifted(ctx->buf[ctx->cur], o);
+    if (form_is32(ctx->swarm_form))
+      launch_swarm_to_aos32(b, (int)m, ctx->g, d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o,
+                            d_pid + o, d_st + o, ctx->stream);
+    else
+      launch_swarm_to_aos(b, (int)m, ctx->g, d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o,
+                          d_pid + o, d_st + o, ctx->stream);
+    CHECK_LAUNCH();
+    ctx->launches += 1;
+    CU(cudaEventRecord(ctx->ev_xfer, ctx->stream));
+    CU(cudaStreamWaitEvent(ctx->side, ctx->ev_xfer, 0));
+    CU(cudaMemcpyAsync(position + 3 * o, d_pos + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
+    CU(cudaMemcpyAsync(velocity + 3 * o, d_vel + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
+    CU(cudaMemcpyAsync(weight + 3 * o, d_wgt + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
+    CU(cudaMemcpyAsync(P + o, d_P + o, 8ull * m, cudaMemcpyDeviceToHost, ctx->side));
+    CU(cudaMemcpyAsync(cell_id + 3 * o, d_cell + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
+    CU(cudaMemcpyAsync(pid + o, d_pid + o, 8ull * m, cudaMemcpyDeviceToHost, ctx->side));
+    CU(cudaMemcpyAsync(status + o, d_st + o, 8ull * m, cudaMemcpyDeviceToHost, ctx->side));
+  }
+  CU(cudaStreamSynchronize(ctx->side));
   CU(cudaStreamSynchronize(ctx->stream));
   return FDF_SUCCESS;
 }

@@ -34,7 +34,7 @@ struct LocatorState {
 struct FdfContext {
   int device = 0;
   cudaStream_t stream = nullptr, side = nullptr;
-  cudaEvent_t ev_scan = nullptr, ev_corner = nullptr;
+  cudaEvent_t ev_scan = nullptr, ev_corner = nullptr, ev_xfer = nullptr;
   GridDims g{};
   bool has_grid = false, has_ucat = false;
   double *coor = nullptr, *planes = nullptr, *ucat = nullptr, *corner = nullptr, *bbox = nullptr;
