@@ -1,16 +1,18 @@
 // fdf_mlp_tc.cu -- inference of the learned start-cell locator on the 5th-generation tensor
-// cores (tcgen05): one CTA holds the network's bfloat16 weights in shared memory and carries
-// tiles of 128 particles through the four layers; each layer is tcgen05.mma (M = 128,
-// kind::f16, bfloat16 operands from shared memory, FP32 accumulator in tensor memory),
+// cores (tcgen05): one CTA holds the network's weights in shared memory (half precision: the
+// network trains in bfloat16, and its weights and activations lie well inside half precision's
+// range) and carries tiles of 128 particles through the four layers; each layer is
+// tcgen05.mma (M = 128,
+// kind::f16, half-precision operands from shared memory, FP32 accumulator in tensor memory),
 // issued by one thread and tracked by an mbarrier; the four warps then read the accumulator
-// rows back with tcgen05.ld (one particle per thread), add the bias, apply SiLU and store the
-// bfloat16 activations as the next layer's A operand.  One CTA per SM holds the weights once
+// rows back with tcgen05.ld (one particle per thread), add the bias, apply SiLU in packed half2
+// arithmetic and store the activations as the next layer's A operand.  One CTA per SM holds the weights once
 // and runs four independent tile pipelines (one per warpgroup, each with its own activation
 // buffers, mbarrier and 128 TMEM columns), so the tensor core serves one pipeline's MMAs while
 // the others run their epilogues; each pipeline prefetches its next tile's positions while
 // the current tile computes.
 //
-// Shared-memory operand layout (no swizzle, K-major): an R x K bfloat16 matrix is stored as
+// Shared-memory operand layout (no swizzle, K-major): an R x K 16-bit matrix is stored as
 // 8-row x 16-byte core matrices; element (r, k) sits at
 //     (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2
 // with SBO = 16 * K bytes (all K / 8 core matrices of an 8-row group side by side), so the
@@ -22,7 +24,7 @@
 // frees its tensor memory and returns.
 #include "fdf_internal.cuh"
 #include "fdf_mlp.cuh"
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace {
 
@@ -38,7 +40,8 @@ constexpr int SM_W4 = SM_W3 + 32768;         // [16][128]  4096
 constexpr int SM_PIPE = SM_W4 + 4096;        // per pipeline: A1 [128][16] 4096, A [128][128] 32768
 constexpr int PIPE_BYTES = 4096 + 32768;
 constexpr int SM_BIAS = SM_PIPE + TC_PIPES * PIPE_BYTES;   // 392 floats
-constexpr int SM_BAR = SM_BIAS + 1568;       // mbarriers (8 B each), TMEM base (4 B), time-out flags
+constexpr int SM_HB2 = SM_BIAS + 1568;       // the hidden half-biases as 192 half2 pairs
+constexpr int SM_BAR = SM_HB2 + 768;         // mbarriers (8 B each), TMEM base (4 B), time-out flags
 constexpr int SM_TOTAL = SM_BAR + 8 * TC_PIPES + 8 + 4 * TC_PIPES;
 constexpr int WIMG_BYTES = SM_PIPE;          // packed weight image in global memory (73,728 B)
 constexpr unsigned long long WAIT_LIMIT = 1ull << 22;
@@ -54,9 +57,10 @@ __device__ __forceinline__ unsigned long long make_desc(unsigned addr, unsigned 
          ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
 }
 
-// Instruction descriptor of kind::f16: FP32 accumulator, bfloat16 A and B, both K-major.
+// Instruction descriptor of kind::f16: FP32 accumulator, half-precision A and B (format 0 for
+// both), both K-major.
 __host__ __device__ constexpr unsigned make_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+  return (1u << 4) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_f16(unsigned tmem_d, unsigned long long adesc, unsigned long long bdesc,
@@ -128,17 +132,21 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
 }
 
 __device__ __forceinline__ unsigned pack2(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  __half2 v = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<unsigned *>(&v);
 }
 
-// SiLU(z) = z * sigmoid(z) = h + h * tanh(h) with h = z / 2; takes the accumulator v and the
-// half-bias hb, so that h = v/2 + hb is one FMA (scaling by 1/2 is exact).
-__device__ __forceinline__ float silu_half(float v, float hb) {
-  const float h = fmaf(v, 0.5f, hb);
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
-  return fmaf(h, t, h);
+// SiLU(z) = z * sigmoid(z) = h + h * tanh(h) with h = z / 2, on a pair of columns in packed
+// half precision: the accumulator pair v rounded to half2, h = v/2 + hb (hb: the half-bias
+// pair), one tanh.approx.f16x2, h + h t -- four instructions per pair.  The epilogue is bound by
+// instruction issue, so this halves its cost against the FP32 form of the same formula.  The
+// pair is the next layer's half-precision A operand as it stands.
+__device__ __forceinline__ unsigned silu2_h2(unsigned v01, __half2 hb) {
+  const __half2 h = __hfma2(*reinterpret_cast<const __half2 *>(&v01), __float2half2_rn(0.5f), hb);
+  unsigned t;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const unsigned *>(&h)));
+  const __half2 s = __hfma2(h, *reinterpret_cast<const __half2 *>(&t), h);
+  return *reinterpret_cast<const unsigned *>(&s);
 }
 
 // byte offset of element (r, k) in the operand layout with SBO = sbo
@@ -146,9 +154,9 @@ __host__ __device__ constexpr unsigned op_off(int r, int k, unsigned sbo) {
   return (unsigned)(r / 8) * sbo + (unsigned)(k / 8) * 128u + (unsigned)(r % 8) * 16u + (unsigned)(k % 8) * 2u;
 }
 
-// Packs the FP32 parameters into the shared-memory image of the weights (bfloat16).
+// Packs the FP32 parameters into the shared-memory image of the weights (half precision).
 __global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__restrict__ img) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;   // one bfloat16 element of the image
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;   // one 16-bit element of the image
   if (q >= WIMG_BYTES / 2) return;
   const int byte = 2 * q;
   float v = 0.f;
@@ -169,7 +177,7 @@ __global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__res
     const int n = rg * 8 + rr, k = kc * 8 + kk;
     if (n < 3) v = params[MLP_OFF_W4 + n * 128 + k];
   }
-  reinterpret_cast<__nv_bfloat16 *>(img)[q] = __float2bfloat16_rn(v);
+  reinterpret_cast<__half *>(img)[q] = __float2half_rn(v);
 }
 
 __device__ __forceinline__ float load_coord(const double *a, unsigned int r, int pairs) {
@@ -190,6 +198,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int tid = threadIdx.x, warp = tid >> 5;
   const int pipe = tid >> 7, row = tid & 127;     // warpgroup = pipeline; thread = tile row
   float *bias = reinterpret_cast<float *>(smem + SM_BIAS);
+  __half2 *hb2 = reinterpret_cast<__half2 *>(smem + SM_HB2);
   unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + SM_BAR);
   unsigned *tmem_slot = reinterpret_cast<unsigned *>(smem + SM_BAR + 8 * TC_PIPES);
   volatile unsigned *tflag = reinterpret_cast<volatile unsigned *>(smem + SM_BAR + 8 * TC_PIPES + 8);
@@ -200,6 +209,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint4 *dst = reinterpret_cast<uint4 *>(smem);
     for (int q = tid; q < WIMG_BYTES / 16; q += TC_THREADS) dst[q] = src[q];
     for (int q = tid; q < MLP_BIAS_WORDS; q += TC_THREADS) bias[q] = bias_g[q];
+    for (int q = tid; q < 192; q += TC_THREADS) hb2[q] = __floats2half2_rn(bias_g[2 * q], bias_g[2 * q + 1]);
     uint4 *a1 = reinterpret_cast<uint4 *>(a1s);
     for (int q = row; q < 4096 / 16; q += 128) a1[q] = make_uint4(0, 0, 0, 0);
   }
@@ -245,16 +255,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   };
   // bias + SiLU of the 128 accumulator columns (b: half-biases), stored as the next layer's A operand
   // (the next chunk's TMEM load is in flight while a chunk is converted)
-  auto chunk = [&](const unsigned (&r)[16], const float *b, int c) {
+  auto chunk = [&](const unsigned (&r)[16], const __half2 *b, int c) {
     unsigned w[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      w[q] = pack2(silu_half(__uint_as_float(r[2 * q]), b[16 * c + 2 * q]),
-                   silu_half(__uint_as_float(r[2 * q + 1]), b[16 * c + 2 * q + 1]));
+    for (int q = 0; q < 8; ++q) {
+      unsigned v01;
+      asm("cvt.rn.f16x2.f32 %0, %1, %2;"   // column 2q in the low half
+          : "=r"(v01)
+          : "f"(__uint_as_float(r[2 * q + 1])), "f"(__uint_as_float(r[2 * q])));
+      w[q] = silu2_h2(v01, b[8 * c + q]);
+    }
     *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
     *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
   };
-  auto epilogue = [&](const float *b) {
+  auto epilogue = [&](const __half2 *b) {
     unsigned ra[16], rb[16];
     tmem_ld16_issue(tmem + lane_base, ra);
     tmem_wait_ld(ra);
@@ -308,13 +322,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     issue(0);
     load_inputs(tile + tstride, cx, cy, cz);   // the next tile's positions, while this one computes
     if (!wait_mma()) { timed_out = true; break; }
-    epilogue(bias);
+    epilogue(hb2);
     issue(1);
     if (!wait_mma()) { timed_out = true; break; }
-    epilogue(bias + 128);
+    epilogue(hb2 + 64);
     issue(2);
     if (!wait_mma()) { timed_out = true; break; }
-    epilogue(bias + 256);
+    epilogue(hb2 + 128);
     issue(3);
     if (!wait_mma()) { timed_out = true; break; }
     {

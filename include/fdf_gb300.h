@@ -234,8 +234,8 @@ int fdf_SortByCellNoAlloc(const int32_t *cell_ids, int64_t n, int64_t ncells, ui
  * (walkingsearch.c:571-626).  A 3-128-128-128-3 SiLU network maps the normalised position
  * xhat = (x - centre) * inv_half (centre and half-extent of the grid's bounding box) to
  * y, read as cell index floor((y_d + 1) N_d / 2), N = (IM, JM, KM), clamped to the grid.
- * Weights are bfloat16 in every tensor-core product (FP32 accumulation), with FP32 master
- * copies for training.  Parameters, one float vector of FDF_LOCATOR_NPARAM values:
+ * Weights are bfloat16 in every training product and half precision in inference (FP32
+ * accumulation in both), with FP32 master copies for training.  Parameters, one float vector of FDF_LOCATOR_NPARAM values:
  * W1 [128][3], b1 [128], W2 [128][128], b2, W3 [128][128], b3, W4 [3][128], b4 [3]. */
 #define FDF_LOCATOR_NPARAM 33923
 /* Weights uniform in +-1/sqrt(fan_in) from the seed, biases zero; Adam state cleared. */
