@@ -254,7 +254,12 @@ static SwarmBuf shifted(const SwarmBuf &b, long long off) {
 // Host <-> device swarm transfers run in chunks of particles on two streams: the copies of
 // one chunk (side stream) overlap the layout conversion of the previous one (context stream),
 // so a transfer costs about its copies alone.
-static int64_t transfer_chunk(int64_t n) { return std::max<int64_t>(int64_t(1) << 22, (n + 7) / 8); }
+#ifndef FDF_XFER_CHUNKS
+#define FDF_XFER_CHUNKS 8
+#endif
+static int64_t transfer_chunk(int64_t n) {
+  return std::max<int64_t>(int64_t(1) << 22, (n + FDF_XFER_CHUNKS - 1) / FDF_XFER_CHUNKS);
+}
 
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity, const double *weight,
                  const double *P, const int64_t *cell_id, const int64_t *pid, const int64_t *status) {
