@@ -194,6 +194,34 @@ __device__ __forceinline__ double scale_down(double x, int k) {
   return mul_hw(x, __longlong_as_double((long long)((unsigned long long)(1023 - k) << 52)));
 }
 
+// a * b, round to nearest even, on the integer pipe: the same bits as __dmul_rn.  GB300 issues
+// FP64 at 1/64 of the FP32 rate while the integer pipe idles in the FP64-bound kernels, so
+// routing part of a kernel's FP64 operations here runs both pipes at once.  Fast path: normal
+// or zero operands with a normal product; the rest takes the hardware multiply out of line.
+constexpr unsigned long long FRAC_MASK = 0x000fffffffffffffull, HIDDEN = 0x0010000000000000ull;
+
+// The 53 x 53-bit significand product P in [2^104, 2^106) is exact in 128 bits; its top 53 bits
+// (from bit 52 or 53) are the significand, the bits below decide the rounding (ties to even).
+__device__ __forceinline__ double mul_int(double a, double b) {
+  const unsigned long long ua = ubits(a), ub = ubits(b);
+  const unsigned long long sign = (ua ^ ub) & NEG_ZERO;
+  const int ea = (int)((ua >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff);
+  const int e = ea + eb - 1023;   // biased exponent for a significand product in [1, 2)
+  if (ea == 0 || eb == 0 || ea == 0x7ff || eb == 0x7ff || e < 1 || e > 2044) {
+    if (((ua & ABS_MASK) == 0ull && eb != 0x7ff) || ((ub & ABS_MASK) == 0ull && ea != 0x7ff))
+      return __longlong_as_double((long long)sign);   // zero times a finite value
+    return mul_hw(a, b);
+  }
+  const unsigned long long ma = (ua & FRAC_MASK) | HIDDEN, mb = (ub & FRAC_MASK) | HIDDEN;
+  const unsigned long long lo = ma * mb, hi = __umul64hi(ma, mb);
+  const unsigned int top = (unsigned int)(hi >> 41) & 1u;   // P >= 2^105
+  const int sh = 52 + (int)top;
+  const unsigned long long mant = (hi << (64 - sh)) | (lo >> sh);
+  const unsigned long long rem = lo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+  const unsigned long long up = (rem > half || (rem == half && (mant & 1ull))) ? 1ull : 0ull;
+  return __longlong_as_double((long long)(sign | (((unsigned long long)(e - 1 + (int)top) << 52) + mant + up)));
+}
+
 // x / n for an integer count n >= 1: x for n = 1, x * 2^-k (exact) for n = 2^k,
 // else the correctly rounded division -- all three equal the IEEE quotient.
 __device__ __forceinline__ double div_count(double x, unsigned int n) {

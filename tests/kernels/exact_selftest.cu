@@ -1,9 +1,10 @@
 // Self-test of the off-FP64-pipe helpers in fdf_exact.cuh against the hardware instructions
-// they replace: div_rn / div_by against __ddiv_rn, d2f_rn against __double2float_rn, split_rn
-// against (fl32(x), fl32(x - fl32(x))), bit for bit, over seeded operands from several
+// they replace: div_rn / div_by against __ddiv_rn, mul_int against __dmul_rn, d2f_rn against __double2float_rn, split_rn against (fl32(x), fl32(x - fl32(x))),
+// scale_down against the multiply by 2^-k, bit for bit, over seeded operands from several
 // distributions (random bit patterns with every exponent, the fast range, divisors near 1,
-// extreme significands, zeros, subnormals, infinities and NaNs).  Test infrastructure: built
-// by the GPU tests, not part of the library.
+// extreme significands, short significands -- whose products hit exact ties --,
+// operands a few ulps apart with opposite signs, zeros, subnormals, infinities and NaNs).  Test
+// infrastructure: built by the GPU tests, not part of the library.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -42,6 +43,13 @@ __device__ double operand(uint64_t r, int k) {
   }
 }
 
+// Keeps the top m bits of the significand (m = 1..53 from r).
+__device__ __forceinline__ double shorten(double x, uint64_t r) {
+  const int m = 1 + (int)(r % 53);
+  const uint64_t keep = ~((1ull << (53 - m)) - 1ull);
+  return __longlong_as_double((long long)((uint64_t)__double_as_longlong(x) & (0xfff0000000000000ull | (keep & 0x000fffffffffffffull))));
+}
+
 __device__ __forceinline__ bool same(double a, double b) {
   const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
   const bool na = (ua & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
@@ -53,11 +61,17 @@ __device__ __forceinline__ bool samef(float a, float b) {
 }
 
 // out[0..2]: division, d2f, split mismatches; out[4..5]: the first bad division's operands;
-// out[6]: scale_down mismatches.
+// out[6]: scale_down, out[7]: mul_int mismatches; out[8] unused.
 __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const uint64_t r1 = mix(seed ^ (2 * (uint64_t)t)), r2 = mix(seed ^ (2 * (uint64_t)t + 1)), r3 = mix(r1 ^ r2);
-    const double a = operand(r1, (int)(r3 & 7)), b = operand(r2, (int)((r3 >> 3) & 7));
+    double a = operand(r1, (int)(r3 & 7)), b = operand(r2, (int)((r3 >> 3) & 7));
+    if ((r3 >> 20) & 1) a = shorten(a, r3 >> 24);
+    if ((r3 >> 21) & 1) b = shorten(b, r3 >> 32);
+    if (((r3 >> 22) & 7) == 0) {   // b = -(a +- a few ulps): cancellation
+      const long long k = (long long)((r3 >> 40) % 9) - 4;
+      b = __longlong_as_double(__double_as_longlong(a) + k) * -1.0;
+    }
     const double q = fdfx::div_rn(a, b), qh = __ddiv_rn(a, b);
     if (!same(q, qh)) {
       if (atomicAdd(&out[0], 1ull) == 0ull) {
@@ -70,6 +84,7 @@ __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
     const float h = __double2float_rn(a);
     const float l = __double2float_rn(__dsub_rn(a, (double)h));
     if (!samef(p.x, h) || !samef(p.y, l)) atomicAdd(&out[2], 1ull);
+    if (!same(fdfx::mul_int(a, b), __dmul_rn(a, b))) atomicAdd(&out[7], 1ull);
     const int k = (int)((r3 >> 8) % 53);
     if (!same(fdfx::scale_down(a, k), __dmul_rn(a, __longlong_as_double((long long)((uint64_t)(1023 - k) << 52)))))
       atomicAdd(&out[6], 1ull);
@@ -78,17 +93,17 @@ __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
 
 }  // namespace
 
-// Runs n cases from the seed; writes the seven counters to host memory.  Returns a CUDA error code.
+// Runs n cases from the seed; writes the nine counters to host memory.  Returns a CUDA error code.
 extern "C" int fdf_test_exact(unsigned long long seed, long long n, unsigned long long *host_out) {
   unsigned long long *d = nullptr;
-  cudaError_t e = cudaMalloc((void **)&d, 7 * sizeof(unsigned long long));
+  cudaError_t e = cudaMalloc((void **)&d, 9 * sizeof(unsigned long long));
   if (e != cudaSuccess) return (int)e;
-  e = cudaMemset(d, 0, 7 * sizeof(unsigned long long));
+  e = cudaMemset(d, 0, 9 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     k_check<<<152 * 8, 256>>>(seed, n, d);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   host_out[3] = (unsigned long long)n;
   return (int)e;
