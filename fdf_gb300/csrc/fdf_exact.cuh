@@ -51,6 +51,19 @@ __device__ __forceinline__ bool le_pos(double d, unsigned long long cb) {
 
 __device__ __forceinline__ double add0(double x) { return ubits(x) == NEG_ZERO ? 0.0 : x; }
 
+// A signed integer with the order of the doubles (both zeros map to 0); for non-NaN values,
+// x <= y exactly when key(x) <= key(y).
+__device__ __forceinline__ long long order_key(double x) {
+  const unsigned long long b = ubits(x);
+  return (b >> 63) ? -(long long)(b & ABS_MASK) : (long long)b;
+}
+
+// x >= lo && x <= hi, on the integer pipe (false when any of the three is NaN).
+__device__ __forceinline__ bool in_range(double x, double lo, double hi) {
+  const long long k = order_key(x);
+  return !is_nan(x) && !is_nan(lo) && !is_nan(hi) && k >= order_key(lo) && k <= order_key(hi);
+}
+
 // (double)n for 0 <= n < 2^31, built on the integer pipe (exact: n has < 53 bits).
 __device__ __forceinline__ double u32_to_double(unsigned int n) {
   if (n == 0) return 0.0;

@@ -109,7 +109,9 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS)
       if (lost) {
         m.lost += 1;
       } else {
-        const bool inside = x >= bbox[0] && x <= bbox[3] && y >= bbox[1] && y <= bbox[4] && z >= bbox[2] && z <= bbox[5];
+        // IsParticleInBox, the six comparisons on the integer pipe
+        const bool inside = fdfx::in_range(x, bbox[0], bbox[3]) && fdfx::in_range(y, bbox[1], bbox[4]) &&
+                            fdfx::in_range(z, bbox[2], bbox[5]);
         if (!inside) { m.oob += 1; key = sentinel; }
       }
     }

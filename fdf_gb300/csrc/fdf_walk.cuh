@@ -5,10 +5,10 @@
 //
 // Each face class the walk needs -- d < 0, d == 0 (|d| < thr), d > 0 -- is decided from an
 // FP32 signed distance when that is provably the FP64 class for the position, and from the
-// exact FP64 distance (the FP64 plane table, the reference's arithmetic) otherwise.  With c0 = c0h + c0l the cell's first vertex as a float pair (exact),
-// fcr = fl32(fc - c0), pr = fl32(fl32(ph - c0h) + fl32(pl - c0l)), n32 = fl32(n) and
-// d32 = (fcr - pr) . n32 (FP32, fused), every rounding is bounded by u32 = 2^-24 times
-// the magnitudes involved:
+// exact FP64 distance (the FP64 plane table, the reference's arithmetic) otherwise.  With
+// c0 = c0h + c0l the cell's first vertex as a float pair (exact), fcr = fl32(fc - c0),
+// pr = fl32(fl32(ph - c0h) + fl32(pl - c0l)), n32 = fl32(n) and d32 = (fcr - pr) . n32 (FP32,
+// fused), every rounding is bounded by u32 = 2^-24 times the magnitudes involved:
 //     |pr_i - (p_i - c0_i)| <= u32 (2 B_i + 2 u32 (|ph_i| + |c0h_i|)),  B_i = |p_i - c0_i|
 //     |d32 - d64| <= 7.001 u32 S,   S = sum_i (A_i + B_i + u32 (|ph_i| + |c0h_i|)) |n_i|
 // with A_i = |fc_i - c0_i| (d64 is the reference's FP64 value; its own error is
@@ -27,8 +27,8 @@
 // undecided faces are computed from x itself (EXACT), so every class is x's own.
 //
 // Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32, negative for a degenerate
-// cell), c0l (3 x f32), overlap margin (f32, cell_margin in fdf_fp32.cu), then per face LEFT..BACK:
-// fcr (3 x f32), n32 (3 x f32).
+// cell), c0l (3 x f32), overlap margin (f32, cell_margin in fdf_fp32.cu), then per face
+// LEFT..BACK: fcr (3 x f32), n32 (3 x f32).
 #pragma once
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
@@ -49,6 +49,20 @@ __device__ __forceinline__ double exact_face(const double *__restrict__ row64, i
   double dd = add(add(mul(sub(p0.x, x), p1.y), mul(sub(p0.y, y), p2.x)), mul(sub(p1.x, z), p2.y));
   if (fdfx::abs_lt_bits(dd, fdfx::ubits(tf.x), fdfx::is_nan(tf.x))) dd = 0.0;
   return dd;
+}
+
+// The exact distance out of line: the face the FP32 bound cannot decide is rare (about 1e-5
+// per particle-step), and kept inline the compiler if-converts it, so every face of every
+// evaluation issues its FP64 instructions predicated off (the FP32 walk: 3.91 -> 3.65 ms per
+// 64M-particle step out of line).  The certified evaluation of the walk from a learned guess
+// keeps it inline: there the call's saved registers cost more (1.18 -> 1.34 ms).
+static __device__ __noinline__ double exact_face_call(const double *__restrict__ row64, int f, double x, double y,
+                                                      double z) {
+  return exact_face(row64, f, x, y, z);
+}
+static __device__ __noinline__ double exact_face_pair(const double *__restrict__ row64, int f, float2 px, float2 py,
+                                                      float2 pz) {
+  return exact_face(row64, f, pair_value(px), pair_value(py), pair_value(pz));
 }
 
 // One cell evaluated for the form's position: the face classes the walk needs, the
@@ -109,11 +123,12 @@ __device__ __forceinline__ void eval_cell32(const float *__restrict__ table, con
       e.dv[f] = d32;
       if (CERT) e.clear = false;
     } else {
-      const double d64 = EXACT ? exact_face(planes + cur * FDF_ROW, f, xe, ye, ze)
-                               : exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py), pair_value(pz));
+      const double d64 = EXACT  ? exact_face_call(planes + cur * FDF_ROW, f, xe, ye, ze)
+                         : CERT ? exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py), pair_value(pz))
+                                : exact_face_pair(planes + cur * FDF_ROW, f, px, py, pz);
       if (fdfx::lt0(d64)) e.neg |= 1u << f;
       e.zero = e.zero || fdfx::eq0(d64);
-      e.dv[f] = __double2float_rn(d64);
+      e.dv[f] = fdfx::d2f_rn(d64);
       if (CERT) e.clear = false;
       ++fb;
     }

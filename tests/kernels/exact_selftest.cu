@@ -1,9 +1,10 @@
 // Self-test of the off-FP64-pipe helpers in fdf_exact.cuh against the hardware instructions
-// they replace: div_rn / div_by against __ddiv_rn, mul_int against __dmul_rn, d2f_rn against __double2float_rn, split_rn against (fl32(x), fl32(x - fl32(x))),
-// scale_down against the multiply by 2^-k, bit for bit, over seeded operands from several
-// distributions (random bit patterns with every exponent, the fast range, divisors near 1,
-// extreme significands, short significands -- whose products hit exact ties --,
-// operands a few ulps apart with opposite signs, zeros, subnormals, infinities and NaNs).  Test
+// they replace, bit for bit: div_rn / div_by against __ddiv_rn, mul_int against __dmul_rn,
+// d2f_rn against __double2float_rn, split_rn against (fl32(x), fl32(x - fl32(x))), scale_down
+// against the multiply by 2^-k, in_range against the FP64 comparisons.  Operands come seeded
+// from several distributions: random bit patterns with every exponent, the fast range, divisors
+// near 1, extreme significands, short significands (whose products hit exact ties), operands a
+// few ulps apart with opposite signs, zeros, subnormals, infinities and NaNs.  Test
 // infrastructure: built by the GPU tests, not part of the library.
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -61,7 +62,7 @@ __device__ __forceinline__ bool samef(float a, float b) {
 }
 
 // out[0..2]: division, d2f, split mismatches; out[4..5]: the first bad division's operands;
-// out[6]: scale_down, out[7]: mul_int mismatches; out[8] unused.
+// out[6]: scale_down, out[7]: mul_int, out[8]: in_range mismatches.
 __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const uint64_t r1 = mix(seed ^ (2 * (uint64_t)t)), r2 = mix(seed ^ (2 * (uint64_t)t + 1)), r3 = mix(r1 ^ r2);
@@ -85,6 +86,11 @@ __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
     const float l = __double2float_rn(__dsub_rn(a, (double)h));
     if (!samef(p.x, h) || !samef(p.y, l)) atomicAdd(&out[2], 1ull);
     if (!same(fdfx::mul_int(a, b), __dmul_rn(a, b))) atomicAdd(&out[7], 1ull);
+    {   // in_range against the FP64 comparisons, with a third operand from the same distributions
+      const double c = operand(r3 ^ r1, (int)((r3 >> 48) & 7));
+      const double lo = ((r3 >> 51) & 1) ? b : c, hi = ((r3 >> 51) & 1) ? c : b;
+      if (fdfx::in_range(a, lo, hi) != (a >= lo && a <= hi)) atomicAdd(&out[8], 1ull);
+    }
     const int k = (int)((r3 >> 8) % 53);
     if (!same(fdfx::scale_down(a, k), __dmul_rn(a, __longlong_as_double((long long)((uint64_t)(1023 - k) << 52)))))
       atomicAdd(&out[6], 1ull);

@@ -1,5 +1,5 @@
 """The FP64-pipe-free helpers of the plain path (fdf_exact.cuh: div_rn / div_by, d2f_rn, split_rn)
-(and scale_down, mul_int) against the hardware instructions they replace, bit for bit, on the GPU: a small CUDA self-test
+(and scale_down, mul_int, in_range) against the hardware instructions they replace, bit for bit, on the GPU: a small CUDA self-test
 (tests/kernels/exact_selftest.cu) is compiled with the library's flags and run over seeded
 operands from random bit patterns, the fast range, divisors near 1, extreme significands,
 zeros, subnormals, infinities and NaNs."""
@@ -41,4 +41,5 @@ def test_helpers_match_the_hardware_bit_for_bit(selftest, seed):
     assert out[2] == 0, f"{out[2]} (hi, lo) splits differ"
     assert out[6] == 0, f"{out[6]} power-of-two scalings differ"
     assert out[7] == 0, f"{out[7]} integer-pipe products differ from __dmul_rn"
+    assert out[8] == 0, f"{out[8]} integer-pipe range tests differ from the FP64 comparisons"
     assert out[3] == n
