@@ -68,8 +68,8 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS)
       // (hi, lo) within 2^-48 |v| of v; a nonzero |v| below 2^-120 (where the split's error is
       // absolute) gives a NaN pair, whose faces all take the FP64 route
       auto split = [](double v) {
-        const unsigned int hw = (unsigned int)__double2hiint(v) & 0x7fffffffu;
-        if (hw < (903u << 20) && (hw | (unsigned int)__double2loint(v)) != 0u) return make_float2(__int_as_float(0x7fc00000), 0.f);
+        const unsigned long long mag = fdfx::ubits(v) & fdfx::ABS_MASK;
+        if (mag < (903ull << 52) && mag != 0ull) return make_float2(__int_as_float(0x7fc00000), 0.f);
         return fdfx::split_rn(v);
       };
       Walk32 w;

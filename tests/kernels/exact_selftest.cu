@@ -1,7 +1,8 @@
 // Self-test of the off-FP64-pipe helpers in fdf_exact.cuh against the hardware instructions
 // they replace, bit for bit: div_rn / div_by against __ddiv_rn, mul_int against __dmul_rn,
 // d2f_rn against __double2float_rn, split_rn against (fl32(x), fl32(x - fl32(x))), scale_down
-// against the multiply by 2^-k, in_range against the FP64 comparisons.  Operands come seeded
+// against the multiply by 2^-k, in_range, lt0, eq0, is_nan, abs_lt_bits, le_pos, add0 and
+// clamp01 against the C comparisons and expressions they restate.  Operands come seeded
 // from several distributions: random bit patterns with every exponent, the fast range, divisors
 // near 1, extreme significands, short significands (whose products hit exact ties), operands a
 // few ulps apart with opposite signs, zeros, subnormals, infinities and NaNs.  Test
@@ -62,7 +63,7 @@ __device__ __forceinline__ bool samef(float a, float b) {
 }
 
 // out[0..2]: division, d2f, split mismatches; out[4..5]: the first bad division's operands;
-// out[6]: scale_down, out[7]: mul_int, out[8]: in_range mismatches.
+// out[6]: scale_down, out[7]: mul_int, out[8]: in_range, out[9]: bit-predicate mismatches.
 __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const uint64_t r1 = mix(seed ^ (2 * (uint64_t)t)), r2 = mix(seed ^ (2 * (uint64_t)t + 1)), r3 = mix(r1 ^ r2);
@@ -91,6 +92,17 @@ __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
       const double lo = ((r3 >> 51) & 1) ? b : c, hi = ((r3 >> 51) & 1) ? c : b;
       if (fdfx::in_range(a, lo, hi) != (a >= lo && a <= hi)) atomicAdd(&out[8], 1ull);
     }
+    {   // the predicates on the bits against the C comparisons they restate
+      const double t = fabs(b);
+      bool bad = fdfx::lt0(a) != (a < 0.0) || fdfx::eq0(a) != (a == 0.0) || fdfx::is_nan(a) != (a != a);
+      bad = bad || fdfx::abs_lt_bits(a, fdfx::ubits(t), t != t) != (fabs(a) < t);
+      if (t == t && t > 0.0 && t < 1.0e300) bad = bad || fdfx::le_pos(a, fdfx::ubits(t)) != (a <= t);
+      bad = bad || !same(fdfx::add0(a), 0.0 + a);
+      const double m1 = (1.0 < a) ? 1.0 : a;        // PetscMin(1.0, a) = 1.0 < a ? 1.0 : a
+      const double cl = (0.0 < m1) ? m1 : 0.0;      // PetscMax(0.0, m1) = 0.0 < m1 ? m1 : 0.0
+      bad = bad || !same(fdfx::clamp01(a), cl);
+      if (bad) atomicAdd(&out[9], 1ull);
+    }
     const int k = (int)((r3 >> 8) % 53);
     if (!same(fdfx::scale_down(a, k), __dmul_rn(a, __longlong_as_double((long long)((uint64_t)(1023 - k) << 52)))))
       atomicAdd(&out[6], 1ull);
@@ -99,17 +111,17 @@ __global__ void k_check(uint64_t seed, long long n, unsigned long long *out) {
 
 }  // namespace
 
-// Runs n cases from the seed; writes the nine counters to host memory.  Returns a CUDA error code.
+// Runs n cases from the seed; writes the ten counters to host memory.  Returns a CUDA error code.
 extern "C" int fdf_test_exact(unsigned long long seed, long long n, unsigned long long *host_out) {
   unsigned long long *d = nullptr;
-  cudaError_t e = cudaMalloc((void **)&d, 9 * sizeof(unsigned long long));
+  cudaError_t e = cudaMalloc((void **)&d, 10 * sizeof(unsigned long long));
   if (e != cudaSuccess) return (int)e;
-  e = cudaMemset(d, 0, 9 * sizeof(unsigned long long));
+  e = cudaMemset(d, 0, 10 * sizeof(unsigned long long));
   if (e == cudaSuccess) {
     k_check<<<152 * 8, 256>>>(seed, n, d);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 10 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   host_out[3] = (unsigned long long)n;
   return (int)e;

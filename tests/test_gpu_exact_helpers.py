@@ -31,7 +31,7 @@ def selftest(tmp_path_factory, require_gpu):
 
 @pytest.mark.parametrize("seed", [1, 2, 3, 4])
 def test_helpers_match_the_hardware_bit_for_bit(selftest, seed):
-    out = (ctypes.c_ulonglong * 9)()
+    out = (ctypes.c_ulonglong * 10)()
     n = 1 << 27
     assert selftest.fdf_test_exact(seed, n, out) == 0
     bad_a = ctypes.c_double.from_buffer_copy(ctypes.c_ulonglong(out[4])).value
@@ -42,4 +42,5 @@ def test_helpers_match_the_hardware_bit_for_bit(selftest, seed):
     assert out[6] == 0, f"{out[6]} power-of-two scalings differ"
     assert out[7] == 0, f"{out[7]} integer-pipe products differ from __dmul_rn"
     assert out[8] == 0, f"{out[8]} integer-pipe range tests differ from the FP64 comparisons"
+    assert out[9] == 0, f"{out[9]} bit predicates (lt0, eq0, is_nan, abs_lt, le_pos, add0, clamp01) differ"
     assert out[3] == n
