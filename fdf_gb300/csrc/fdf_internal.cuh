@@ -134,9 +134,9 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_LOC_MIN_BLOCKS
 #define FDF_LOC_MIN_BLOCKS (1024 / FDF_LOC_THREADS)
 #endif
-// Resident blocks per SM of the plain walk (its steps decided from the FP32 table: latency-bound
-// like the FP32 walk; 768 and 1024 resident threads time the same, 13.3 ms per 64M-particle
-// step) and of the per-cell PID ordering (latency-bound: 2048 resident threads at 32 registers,
+// Resident blocks per SM of the plain walk (its steps decided from the FP32 table; per
+// 64M-particle step 1024 resident threads take 7.6 ms against 8.6 ms at 768 and 8.4 ms at 1280
+// or 1536, where spills grow) and of the per-cell PID ordering (latency-bound: 2048 resident threads at 32 registers,
 // 1.59 -> 1.24 ms for the 64M-particle sort stage).
 #ifndef FDF_PLAIN_MIN_BLOCKS
 #define FDF_PLAIN_MIN_BLOCKS 8
