@@ -268,12 +268,14 @@ MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, on
 # units the stage processed then: live particles, or guessed particles for the network and
 # the walk from the guess.
 TRAFFIC = {
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (8.422e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (0.596e9, "guesses", 12.92e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (3.912e9, "guesses", 12.92e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.843e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (8.069e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.842e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (8.665e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (0.597e9, "guesses", 12.92e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (3.941e9, "guesses", 12.92e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.906e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (8.314e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.906e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "advect_locate"): (14.193e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "gather_interpolate"): (10.884e9, "particles", 63.81e6),
 }
 
 
