@@ -242,6 +242,23 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   return FDF_SUCCESS;
 }
 
+// The device addresses of the caller's seven DMSwarm arrays when every one is page-locked host
+// memory (cudaHostAlloc / cudaHostRegister) and 16-byte aligned, so that the layout kernels can
+// read or write them over the host link; false otherwise.
+static bool host_views(const void *const a[7], void *v[7]) {
+  for (int q = 0; q < 7; ++q) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, a[q]) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer || (reinterpret_cast<uintptr_t>(at.devicePointer) & 15u))
+      return false;
+    v[q] = at.devicePointer;
+  }
+  return true;
+}
+
 // The swarm buffers from particle `off` on.
 static SwarmBuf shifted(const SwarmBuf &b, long long off) {
   SwarmBuf r = b;
@@ -251,9 +268,10 @@ static SwarmBuf shifted(const SwarmBuf &b, long long off) {
   return r;
 }
 
-// Host <-> device swarm transfers run in chunks of particles on two streams: the copies of
-// one chunk (side stream) overlap the layout conversion of the previous one (context stream),
-// so a transfer costs about its copies alone.
+// Host <-> device swarm transfers: page-locked arrays are read or written in place by the
+// layout kernels (coalesced 16-byte accesses over the host link, no copy calls); other arrays
+// go in chunks of particles on two streams, the copies of one chunk (side stream) overlapping
+// the layout conversion of the previous one (context stream).
 #ifndef FDF_XFER_CHUNKS
 #define FDF_XFER_CHUNKS 8
 #endif
@@ -276,7 +294,14 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   char *st = (char *)ctx->staging;
   double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
-  if (n > 0) {
+  const void *arrays[7] = {position, velocity, weight, P, cell_id, pid, status};
+  void *views[7];
+  if (n > 0 && host_views(arrays, views)) {
+    ctx->cur = 0;
+    launch_swarm_from_host(views, (int)n, ctx->g, ctx->buf[0], form_is32(ctx->form), ctx->stream);
+    CHECK_LAUNCH();
+    ctx->launches += 1;
+  } else if (n > 0) {
     ctx->cur = 0;
     // the side stream starts after everything already queued on the context stream
     CU(cudaEventRecord(ctx->ev_xfer, ctx->stream));
@@ -368,6 +393,15 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *positio
   char *st = (char *)ctx->staging;
   double *d_pos = (double *)st, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
+  const void *arrays[7] = {position, velocity, weight, P, cell_id, pid, status};
+  void *views[7];
+  if (host_views(arrays, views)) {
+    launch_swarm_to_host(ctx->buf[ctx->cur], (int)n, ctx->g, views, form_is32(ctx->swarm_form), ctx->stream);
+    CHECK_LAUNCH();
+    ctx->launches += 1;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return FDF_SUCCESS;
+  }
   const int64_t chunk = transfer_chunk(n);
   for (int64_t o = 0; o < n; o += chunk) {
     const int64_t m = std::min(chunk, n - o);

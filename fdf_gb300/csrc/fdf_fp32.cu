@@ -706,6 +706,103 @@ __global__ void k_to_aos32(SwarmBuf b, int n, GridDims g, double *__restrict__ p
   status[p] = b.status[p];
 }
 
+// Layout conversion straight from / to the caller's page-locked DMSwarm arrays over the host
+// link.  A block stages 256 particles' AoS records (15 x 8 B each: position, velocity, weights,
+// P, cell triple, PID, status) in shared memory, moving each field's contiguous range with
+// coalesced 16-byte accesses -- the access pattern that reaches the link's copy rate -- and each
+// thread converts its own particle to or from the device SoA buffers as the per-particle
+// kernels above do.  The arrays must be 16-byte aligned.
+constexpr int XF_TILE = 256;
+// field f: doubles per particle, and the field's offset in the shared tile (in doubles)
+__host__ __device__ constexpr int xf_bs(int f) { return (f < 3 || f == 4) ? 3 : 1; }
+__host__ __device__ constexpr int xf_off(int f) { return XF_TILE * (f <= 3 ? 3 * f : f == 4 ? 10 : f == 5 ? 13 : 14); }
+
+struct HostSwarm {
+  const double *f[7];   // position, velocity, weight, P, cell (int64), pid (int64), status (int64)
+};
+
+__device__ __forceinline__ void tile_in(double *dst, const double *__restrict__ src, int count) {
+  const double2 *s2 = reinterpret_cast<const double2 *>(src);
+  double2 *d2 = reinterpret_cast<double2 *>(dst);
+  for (int q = threadIdx.x; q < count / 2; q += XF_TILE) d2[q] = s2[q];
+  if ((count & 1) && threadIdx.x == 0) dst[count - 1] = src[count - 1];
+}
+__device__ __forceinline__ void tile_out(double *__restrict__ dst, const double *src, int count) {
+  const double2 *s2 = reinterpret_cast<const double2 *>(src);
+  double2 *d2 = reinterpret_cast<double2 *>(dst);
+  for (int q = threadIdx.x; q < count / 2; q += XF_TILE) d2[q] = s2[q];
+  if ((count & 1) && threadIdx.x == 0) dst[count - 1] = src[count - 1];
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(XF_TILE) k_from_host(HostSwarm h, int n, GridDims g, SwarmBuf b) {
+  __shared__ __align__(16) double sm[15 * XF_TILE];
+  const int p0 = blockIdx.x * XF_TILE, m = min(XF_TILE, n - p0);
+#pragma unroll
+  for (int f = 0; f < 7; ++f) tile_in(sm + xf_off(f), h.f[f] + (long long)xf_bs(f) * p0, xf_bs(f) * m);
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t >= m) return;
+  const int p = p0 + t;
+  const double *pos = sm + xf_off(0) + 3 * t, *vel = sm + xf_off(1) + 3 * t, *wgt = sm + xf_off(2) + 3 * t;
+  const long long *c3 = reinterpret_cast<const long long *>(sm + xf_off(4)) + 3 * t;
+  if (F32) {
+    st_pair(b.x, p, fdfx::split_rn(pos[0])); st_pair(b.y, p, fdfx::split_rn(pos[1])); st_pair(b.z, p, fdfx::split_rn(pos[2]));
+    b.uf[p] = fdfx::d2f_rn(vel[0]); b.vf[p] = fdfx::d2f_rn(vel[1]); b.wf[p] = fdfx::d2f_rn(vel[2]);
+    b.a1f[p] = fdfx::d2f_rn(wgt[0]); b.a2f[p] = fdfx::d2f_rn(wgt[1]); b.a3f[p] = fdfx::d2f_rn(wgt[2]);
+    b.Pf[p] = fdfx::d2f_rn(sm[xf_off(3) + t]);
+  } else {
+    b.x[p] = pos[0]; b.y[p] = pos[1]; b.z[p] = pos[2];
+    b.u[p] = vel[0]; b.v[p] = vel[1]; b.w[p] = vel[2];
+    b.a1[p] = wgt[0]; b.a2[p] = wgt[1]; b.a3[p] = wgt[2];
+    b.P[p] = sm[xf_off(3) + t];
+  }
+  b.pid[p] = reinterpret_cast<const long long *>(sm + xf_off(5))[t];
+  const long long i = c3[0], j = c3[1], k = c3[2];
+  int c = -1;
+  if (i >= 0 && i < g.IM && j >= 0 && j < g.JM && k >= 0 && k < g.KM) c = (int)((k * g.JM + j) * g.IM + i);
+  b.cell[p] = c;
+  const long long st = reinterpret_cast<const long long *>(sm + xf_off(6))[t];
+  b.status[p] = (unsigned char)((st >= 0 && st <= ST_UNINITIALIZED) ? st : ST_UNINITIALIZED);
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(XF_TILE) k_to_host(SwarmBuf b, int n, GridDims g, HostSwarm h) {
+  __shared__ __align__(16) double sm[15 * XF_TILE];
+  const int p0 = blockIdx.x * XF_TILE, m = min(XF_TILE, n - p0);
+  const int t = threadIdx.x;
+  if (t < m) {
+    const int p = p0 + t;
+    double *pos = sm + xf_off(0) + 3 * t, *vel = sm + xf_off(1) + 3 * t, *wgt = sm + xf_off(2) + 3 * t;
+    if (F32) {
+      pos[0] = pair_value(ld_pair(b.x, p)); pos[1] = pair_value(ld_pair(b.y, p)); pos[2] = pair_value(ld_pair(b.z, p));
+      vel[0] = b.uf[p]; vel[1] = b.vf[p]; vel[2] = b.wf[p];
+      wgt[0] = b.a1f[p]; wgt[1] = b.a2f[p]; wgt[2] = b.a3f[p];
+      sm[xf_off(3) + t] = b.Pf[p];
+    } else {
+      pos[0] = b.x[p]; pos[1] = b.y[p]; pos[2] = b.z[p];
+      vel[0] = b.u[p]; vel[1] = b.v[p]; vel[2] = b.w[p];
+      wgt[0] = b.a1[p]; wgt[1] = b.a2[p]; wgt[2] = b.a3[p];
+      sm[xf_off(3) + t] = b.P[p];
+    }
+    long long *c3 = reinterpret_cast<long long *>(sm + xf_off(4)) + 3 * t;
+    const int c = b.cell[p];
+    if (c >= 0) {
+      int i, j, k;
+      cell_ijk(g, (unsigned int)c, i, j, k);
+      c3[0] = i; c3[1] = j; c3[2] = k;
+    } else {
+      c3[0] = -1; c3[1] = -1; c3[2] = -1;
+    }
+    reinterpret_cast<long long *>(sm + xf_off(5))[t] = b.pid[p];
+    reinterpret_cast<long long *>(sm + xf_off(6))[t] = b.status[p];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int f = 0; f < 7; ++f)
+    tile_out(const_cast<double *>(h.f[f]) + (long long)xf_bs(f) * p0, sm + xf_off(f), xf_bs(f) * m);
+}
+
 __global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ out, long long n) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q < n) out[q] = (float)in[q];
@@ -816,6 +913,24 @@ void launch_swarm_to_aos32(const SwarmBuf &b, int n, GridDims g, double *pos, do
                            long long *cell3, long long *pid, long long *status, cudaStream_t s) {
   if (n <= 0) return;
   k_to_aos32<<<blocks_for(n, 256), 256, 0, s>>>(b, n, g, pos, vel, wgt, P, cell3, pid, status);
+}
+
+void launch_swarm_from_host(const void *const f[7], int n, GridDims g, const SwarmBuf &b, bool f32, cudaStream_t s) {
+  if (n <= 0) return;
+  HostSwarm h;
+  for (int q = 0; q < 7; ++q) h.f[q] = static_cast<const double *>(f[q]);
+  const unsigned blocks = (unsigned)((n + XF_TILE - 1) / XF_TILE);
+  if (f32) k_from_host<true><<<blocks, XF_TILE, 0, s>>>(h, n, g, b);
+  else k_from_host<false><<<blocks, XF_TILE, 0, s>>>(h, n, g, b);
+}
+
+void launch_swarm_to_host(const SwarmBuf &b, int n, GridDims g, void *const f[7], bool f32, cudaStream_t s) {
+  if (n <= 0) return;
+  HostSwarm h;
+  for (int q = 0; q < 7; ++q) h.f[q] = static_cast<const double *>(f[q]);
+  const unsigned blocks = (unsigned)((n + XF_TILE - 1) / XF_TILE);
+  if (f32) k_to_host<true><<<blocks, XF_TILE, 0, s>>>(b, n, g, h);
+  else k_to_host<false><<<blocks, XF_TILE, 0, s>>>(b, n, g, h);
 }
 
 void launch_f64_to_f32(const double *in, float *out, long long n, cudaStream_t s) {

@@ -247,6 +247,10 @@ void launch_swarm_from_aos32(const double *pos, const double *vel, const double 
                              const SwarmBuf &b, cudaStream_t s);
 void launch_swarm_to_aos32(const SwarmBuf &b, int n, GridDims g, double *pos, double *vel, double *wgt, double *P,
                            long long *cell3, long long *pid, long long *status, cudaStream_t s);
+// The layout conversion straight from / to page-locked host DMSwarm arrays (device addresses,
+// 16-byte aligned; f = position, velocity, weight, P, cell, pid, status), either form.
+void launch_swarm_from_host(const void *const f[7], int n, GridDims g, const SwarmBuf &b, bool f32, cudaStream_t s);
+void launch_swarm_to_host(const SwarmBuf &b, int n, GridDims g, void *const f[7], bool f32, cudaStream_t s);
 void launch_f64_to_f32(const double *in, float *out, long long n, cudaStream_t s);
 void launch_f32_to_f64(const float *in, double *out, long long n, cudaStream_t s);
 

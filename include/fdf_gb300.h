@@ -126,7 +126,11 @@ int fdf_SetForm(FdfContext *ctx, int form);
 int fdf_SetTimeStep(FdfContext *ctx, double dt);                 /* user->dt            */
 int fdf_SetParticleVolume(FdfContext *ctx, double volume);       /* face deposit V_p    */
 
-/* ---- swarm transfer (DMSwarm fields, ParticleSwarm.c:64-96, [n][bs] layout) ---- */
+/* ---- swarm transfer (DMSwarm fields, ParticleSwarm.c:64-96, [n][bs] layout) ----
+ * When all seven arrays of a call are page-locked host memory (cudaHostAlloc /
+ * cudaHostRegister) and 16-byte aligned, the layout kernels read (fdf_SetSwarm) or write
+ * (fdf_GetSwarm) them in place over the host link; otherwise they are copied through a device
+ * staging buffer.  The results are the same either way. */
 int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity);
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity,
                  const double *weight, const double *P, const int64_t *cell_id, const int64_t *pid,
