@@ -80,10 +80,10 @@ def _roundtrip(form, s, pinned, offset=0, launches=None):
     with PicContext(0) as ctx:
         ctx.set_form(form)
         ctx.set_grid(wl.coor)
-        l0 = ctx.launches()
+        l0 = ctx.launches
         ctx._check(ctx.lib.fdf_SetSwarm(ctx.h, s.n, *[_ptr(a) for a in ins]))
         if launches is not None:
-            launches.append(ctx.launches() - l0)
+            launches.append(ctx.launches - l0)
         outs = []
         for f in FIELDS:
             a = np.zeros_like(np.ascontiguousarray(getattr(s, f)))
