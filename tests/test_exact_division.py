@@ -1,4 +1,5 @@
-"""The division of fdf_exact.cuh (div_by) restated step by step in Python: FP32 steps in numpy
+"""The division (div_by) and the integer-pipe multiply (mul_int) of fdf_exact.cuh restated step by
+step in Python.  The division: FP32 steps in numpy
 float32 (round to nearest), integer steps in Python integers with the kernel's 64-bit wrap,
 the reciprocal perturbed by up to 2^-22 (the approximate reciprocal's 2 ulps) before its Newton
 step.  Checks the bounds the kernel relies on (|Q1 - Q| < 2^11, |R1| < 2^65, R2 in (-mb, mb),
@@ -120,3 +121,58 @@ def test_division_extreme_reciprocal_errors():
         for b in (1.0, 2.0 - 2.0 ** -52, 1.0 + 2.0 ** -52, 3.0, 0.1, 2e-14, 7.0):
             for e in (2.0 ** -22, -(2.0 ** -22), 0.0):
                 assert _ub(div_by(a, b, e)) == _ub(a / b)
+
+
+# ---- mul_int: the 53 x 53-bit significand product, exact in 128 bits, rounded to nearest even
+
+
+def mul_int(a, b):
+    """fdf_exact.cuh mul_int step by step (fast path: normal operands, normal product; zeros)."""
+    ua, ub = _ub(a), _ub(b)
+    sign = (ua ^ ub) & (1 << 63)
+    ea, eb = (ua >> 52) & 0x7FF, (ub >> 52) & 0x7FF
+    e = ea + eb - 1023
+    if ea == 0 or eb == 0 or ea == 0x7FF or eb == 0x7FF or e < 1 or e > 2044:
+        if ((ua & ((1 << 63) - 1)) == 0 and eb != 0x7FF) or ((ub & ((1 << 63) - 1)) == 0 and ea != 0x7FF):
+            return _fb(sign)
+        return None   # the hardware multiply
+    ma = (ua & ((1 << 52) - 1)) | (1 << 52)
+    mb = (ub & ((1 << 52) - 1)) | (1 << 52)
+    prod = ma * mb
+    lo, hi = prod & M64, prod >> 64
+    top = (hi >> 41) & 1
+    sh = 52 + top
+    mant = ((hi << (64 - sh)) & M64) | (lo >> sh)
+    assert (1 << 52) <= mant < (1 << 53)
+    rem, half = lo & ((1 << sh) - 1), 1 << (sh - 1)
+    up = 1 if (rem > half or (rem == half and (mant & 1))) else 0
+    return _fb(sign | (((e - 1 + top) << 52) + mant + up))
+
+
+def _short(x, rng):
+    m = rng.randint(1, 53)
+    keep = ~((1 << (53 - m)) - 1)
+    return _fb(_ub(x) & (0xFFF0000000000000 | (keep & ((1 << 52) - 1))))
+
+
+def test_mul_int_restatement_is_correctly_rounded():
+    rng = random.Random(21)
+    ties = 0
+    for i in range(60000):
+        a = rng.uniform(1, 2) * 2.0 ** rng.randint(-300, 300) * rng.choice([1, -1])
+        b = rng.uniform(1, 2) * 2.0 ** rng.randint(-300, 300) * rng.choice([1, -1])
+        if i % 2:
+            a, b = _short(a, rng), _short(b, rng)   # short significands: exact products and ties
+        if i % 11 == 0:
+            b = 0.0 if i % 22 == 0 else -0.0
+        q = mul_int(a, b)
+        if q is None:
+            continue
+        want = a * b
+        assert _ub(q) == _ub(want), (a, b, q, want)
+        ua, ub = _ub(a), _ub(b)
+        if a != 0 and b != 0:
+            p = ((ua & ((1 << 52) - 1)) | (1 << 52)) * ((ub & ((1 << 52) - 1)) | (1 << 52))
+            sh = 52 + ((p >> 105) & 1)
+            ties += (p & ((1 << sh) - 1)) == 1 << (sh - 1)
+    assert ties > 100   # the exact-half case is exercised
