@@ -1,9 +1,10 @@
 """The division (div_by) and the integer-pipe multiply (mul_int) of fdf_exact.cuh restated step by
-step in Python.  The division: FP32 steps in numpy
-float32 (round to nearest), integer steps in Python integers with the kernel's 64-bit wrap,
-the reciprocal perturbed by up to 2^-22 (the approximate reciprocal's 2 ulps) before its Newton
-step.  Checks the bounds the kernel relies on (|Q1 - Q| < 2^11, |R1| < 2^65, R2 in (-mb, mb),
-the 32-bit top word of R1) and that the result is Python's correctly rounded quotient."""
+step in Python.  The division: FP32 steps in numpy float32 (round to nearest), integer steps in
+Python integers with the kernel's 64-bit wrap, the reciprocal perturbed by up to 2^-22 (the
+approximate reciprocal's 2 ulps) before its Newton step.  Checks the bounds the kernel relies
+on (|Q1 - Q| < 2^11, |R1| < 2^65, R2 in (-mb, mb), the 32-bit top word of R1) and that the
+result is Python's correctly rounded quotient.  The multiply: the 128-bit significand product
+and its rounding, against Python's product, with short significands for exact ties."""
 import random
 import struct
 from fractions import Fraction
