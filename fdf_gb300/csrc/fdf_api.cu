@@ -527,7 +527,8 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
     LocatorState &L = ctx->loc;
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
                     ctx->cnt, ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, L.pflag, L.far_cells, s);
-    exclusive_scan_u32(L.pflag, (long long)ctx->cap + 1, L.scan_sums, s);
+    const long long nw = ((long long)ctx->cap + 31) / 32;   // the warps' pending counts, scanned in place
+    exclusive_scan_u32(L.pflag + nw, nw + 1, L.scan_sums, s);
     launch_compact_pending(L.pflag, ctx->cap, L.pending, ctx->cnt, s);
     eg0 = prof ? record_event(ctx, s) : 0;
     mlp_guess_tc(L.tc_img, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0, ctx->cap, g,

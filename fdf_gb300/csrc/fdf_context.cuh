@@ -22,7 +22,8 @@ struct LocatorState {
   float far_cells = 2.0f;             // particles at least this far past their cell get a guess
   // per-particle buffers of the learned form's locate
   unsigned int *pending = nullptr;    // [cap]: slots that left their previous cell, in slot order
-  unsigned int *pflag = nullptr;      // [cap+1]: their flags, then the flags' exclusive scan
+  unsigned int *pflag = nullptr;      // [2W+1], W = ceil(cap/32): per warp of slots a mask, then the
+                                      // counts' exclusive scan
   unsigned int *scan_sums = nullptr;
   int *guess = nullptr;               // [cap]: learned start cell of pending[t]
   int pending_cap = 0;

@@ -199,7 +199,8 @@ __device__ __forceinline__ float beyond_cells(const float (&dv)[6]) {
 //   FIRST == false: the reference walk from the previous cell (or cell (0,0,0)).
 //   FIRST == true:  the reference's first evaluation, in the previous cell; a particle that it
 //                   does not conclude and that lies at least far_cells past that cell is
-//                   flagged in `pending` (n_cap + 1 flags) and finished by k_locate32_guess (its
+//                   marked in `pending` (per warp of slots: a bit mask [W] and its count
+//                   [W + 1], W = ceil(n_cap / 32)) and finished by k_locate32_guess (its
 //                   key and histogram entry are written there); a nearer one continues the
 //                   reference walk here.
 template <bool FIRST>
@@ -271,24 +272,33 @@ __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_LOC_MIN_BLOCKS) k_locate3
       else if (!drop_removed) hkey = sentinel;
     }
   }
-  if (FIRST && s < n_cap) {   // flags of the pending list (compacted by an exclusive scan)
-    pending[s] = wait ? 1u : 0u;
-    if (s == n_cap - 1) pending[n_cap] = 0u;
+  if (FIRST) {   // the warp's pending slots as a bit mask and its count (scanned, then compacted)
+    const unsigned int mask = __ballot_sync(0xffffffffu, s < n_cap && wait);
+    const int W = (n_cap + 31) >> 5, w = s >> 5;
+    if ((threadIdx.x & 31) == 0 && w < W) {
+      pending[w] = mask;
+      pending[W + w] = (unsigned int)__popc(mask);
+      if (w == 0) pending[2 * W] = 0u;
+    }
   }
   const unsigned int r = warp_histogram_rank(hkey, count);
   if (hkey != 0xffffffffu) rank[s] = r;
   block_flush_counts(m, cnt);
 }
 
-// pending[0 .. n_cap] holds the exclusive scan of the flags: slot s is pending when
-// pending[s + 1] > pending[s]; list[pending[s]] = s keeps the slot (cell) order.
-__global__ void k_compact_pending(const unsigned int *__restrict__ scan, int n_cap, unsigned int *__restrict__ list,
+// pf = the warps' masks [W], then the exclusive scan of their counts [W + 1]: warp w's pending
+// slots go to list[scan[w]...] in ascending order, which keeps the slot (cell) order.
+__global__ void k_compact_pending(const unsigned int *__restrict__ pf, int n_cap, unsigned int *__restrict__ list,
                                   DevCounters *cnt) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) cnt->pending = scan[n_cap];
-  if (s < n_cap) {
-    const unsigned int a = scan[s];
-    if (scan[s + 1] != a) list[a] = (unsigned int)s;
+  const int W = (n_cap + 31) >> 5;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w == 0) cnt->pending = pf[2 * W];
+  if (w < W) {
+    unsigned int m = pf[w], o = pf[W + w];
+    while (m) {
+      list[o++] = (unsigned int)(32 * w + __ffs((int)m) - 1);
+      m &= m - 1u;
+    }
   }
 }
 
@@ -838,7 +848,7 @@ void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *tabl
 
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
                             cudaStream_t s) {
-  k_compact_pending<<<blocks_for(n_cap, 256), 256, 0, s>>>(scan, n_cap, list, cnt);
+  k_compact_pending<<<blocks_for((n_cap + 31) / 32, 256), 256, 0, s>>>(scan, n_cap, list, cnt);
 }
 
 void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,

@@ -225,7 +225,7 @@ void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *tabl
                      int advect, const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
                      unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
                      unsigned int *pending, float far_cells, cudaStream_t s);
-// The learned form's pending list from the scanned flags (sets cnt->pending).
+// The learned form's pending list from the warps' masks and scanned counts (sets cnt->pending).
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
                             cudaStream_t s);
 // The learned form's second pass over pending[0 .. cnt->pending), guess[t] = start cell:

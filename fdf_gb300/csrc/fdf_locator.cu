@@ -178,7 +178,7 @@ int locator_reserve(FdfContext *ctx) {
   L.pending_cap = 0;
   CU(cudaMalloc((void **)&L.pending, 4ull * ctx->cap));
   CU(cudaMalloc((void **)&L.guess, 4ull * ctx->cap));
-  CU(cudaMalloc((void **)&L.pflag, 4ull * (ctx->cap + 1)));
+  CU(cudaMalloc((void **)&L.pflag, 4ull * (2 * ((ctx->cap + 31) / 32) + 1)));
   CU(cudaMalloc((void **)&L.scan_sums, 4ull * scan_scratch_words(ctx->cap + 1)));
   L.pending_cap = ctx->cap;
   return FDF_SUCCESS;
