@@ -325,11 +325,12 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
     """Algorithmic bytes per launch of each stage; the momentum deposit adds the particles'
     velocities and three components per face."""
     if form == "learned_fp32":
-        # first pass: one evaluation per particle, pending flags and their scan; walk from the
-        # guess: the pending particles' state and the remaining evaluations
+        # first pass: one evaluation per particle, the per-warp pending masks and counts (under a
+        # byte per particle with their scan and compaction); walk from the guess: the pending
+        # particles' state and the remaining evaluations
         return {
             "center_to_corner": 24 * nodes_per_step,
-            "advect_locate": 86 * n_avg + 16 * n_avg + 176 * max(evals_per_step - n_avg - pending_evals, 0.0),
+            "advect_locate": 86 * n_avg + 1 * n_avg + 176 * max(evals_per_step - n_avg - pending_evals, 0.0),
             "guess_walk": 57 * pending + 176 * pending_evals,
             "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
             "wait_corner": 0,
