@@ -631,28 +631,62 @@ __global__ void __launch_bounds__(256) k_deposit32(SwarmBuf b, GridDims g, const
   const long long nfi = (IM + 1LL) * JM * KM, nfj = IM * (JM + 1LL) * KM, nfk = (long long)IM * JM * (KM + 1LL);
   const bool face_i = j < JM && k < KM, face_j = i < IM && k < KM, face_k = i < IM && j < JM;
   KSum acc[3], mm[3][3];
+  // Each segment is read in chunks of DCH particles, all loads of a chunk issued before its
+  // in-order adds, so one load latency serves the chunk instead of each particle.
+  constexpr int DCH = MOM ? 4 : 8;
   auto lower = [&](int f, const float *__restrict__ wgt, long long lc) {
     const int l0 = (int)__ldg(cs + lc), l1 = (int)__ldg(cs + lc + 1);
-    for (int s = l0; s < l1; ++s) {
-      const float fr = __ldg(wgt + s) * third;
-      acc[f].add(fr);
-      if (MOM) { mm[f][0].add(fr * __ldg(b.uf + s)); mm[f][1].add(fr * __ldg(b.vf + s)); mm[f][2].add(fr * __ldg(b.wf + s)); }
+    for (int s = l0; s < l1; s += DCH) {
+      float a[DCH], u[DCH], v[DCH], w[DCH];
+#pragma unroll
+      for (int q = 0; q < DCH; ++q) {
+        const bool in = s + q < l1;
+        a[q] = in ? __ldg(wgt + s + q) : 0.f;
+        if (MOM) {
+          u[q] = in ? __ldg(b.uf + s + q) : 0.f;
+          v[q] = in ? __ldg(b.vf + s + q) : 0.f;
+          w[q] = in ? __ldg(b.wf + s + q) : 0.f;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < DCH; ++q) {
+        if (s + q >= l1) break;
+        const float fr = a[q] * third;
+        acc[f].add(fr);
+        if (MOM) { mm[f][0].add(fr * u[q]); mm[f][1].add(fr * v[q]); mm[f][2].add(fr * w[q]); }
+      }
     }
   };
   if (face_i && i > 0) lower(0, b.a1f, c - 1);
   if (face_j && j > 0) lower(1, b.a2f, ((long long)k * JM + (j - 1)) * IM + i);
   if (face_k && k > 0) lower(2, b.a3f, ((long long)(k - 1) * JM + j) * IM + i);
   KSum sum;
-  for (int s = s0; s < s1; ++s) {
-    sum.add(__ldg(b.Pf + s));
-    const float w[3] = {__ldg(b.a1f + s), __ldg(b.a2f + s), __ldg(b.a3f + s)};
-    float u = 0.f, v = 0.f, ww = 0.f;
-    if (MOM) { u = __ldg(b.uf + s); v = __ldg(b.vf + s); ww = __ldg(b.wf + s); }
+  constexpr int OCH = 4;
+  for (int s = s0; s < s1; s += OCH) {
+    float P[OCH], w[OCH][3], u[OCH], v[OCH], ww[OCH];
 #pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      const float fr = (1.f - w[f]) * third;
-      acc[f].add(fr);
-      if (MOM) { mm[f][0].add(fr * u); mm[f][1].add(fr * v); mm[f][2].add(fr * ww); }
+    for (int q = 0; q < OCH; ++q) {
+      const bool in = s + q < s1;
+      P[q] = in ? __ldg(b.Pf + s + q) : 0.f;
+      w[q][0] = in ? __ldg(b.a1f + s + q) : 0.f;
+      w[q][1] = in ? __ldg(b.a2f + s + q) : 0.f;
+      w[q][2] = in ? __ldg(b.a3f + s + q) : 0.f;
+      if (MOM) {
+        u[q] = in ? __ldg(b.uf + s + q) : 0.f;
+        v[q] = in ? __ldg(b.vf + s + q) : 0.f;
+        ww[q] = in ? __ldg(b.wf + s + q) : 0.f;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < OCH; ++q) {
+      if (s + q >= s1) break;
+      sum.add(P[q]);
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        const float fr = (1.f - w[q][f]) * third;
+        acc[f].add(fr);
+        if (MOM) { mm[f][0].add(fr * u[q]); mm[f][1].add(fr * v[q]); mm[f][2].add(fr * ww[q]); }
+      }
     }
   }
   {
