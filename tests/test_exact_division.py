@@ -4,7 +4,9 @@ Python integers with the kernel's 64-bit wrap, the reciprocal perturbed by up to
 approximate reciprocal's 2 ulps) before its Newton step.  Checks the bounds the kernel relies
 on (|Q1 - Q| < 2^11, |R1| < 2^65, R2 in (-mb, mb), the 32-bit top word of R1) and that the
 result is Python's correctly rounded quotient.  The multiply: the 128-bit significand product
-and its rounding, against Python's product, with short significands for exact ties."""
+and its rounding, against Python's product, with short significands for exact ties.  The
+conversions: double -> float and the (hi, lo) split by rounding the bit pattern, against
+numpy's float32 rounding, and the split's 2^-48 |x| bound."""
 import random
 import struct
 from fractions import Fraction
@@ -177,3 +179,53 @@ def test_mul_int_restatement_is_correctly_rounded():
             sh = 52 + ((p >> 105) & 1)
             ties += (p & ((1 << sh) - 1)) == 1 << (sh - 1)
     assert ties > 100   # the exact-half case is exercised
+
+
+# ---- d2f_rn and split_rn: double -> float by rounding the bit pattern, and the (hi, lo) split
+
+
+def d2f_rn(x):
+    """fdf_exact.cuh d2f_rn, fast path ([2^-126, FLT_MAX) in magnitude); None for the rest."""
+    b = _ub(x)
+    mag = b & ((1 << 63) - 1)
+    if not (0x3810000000000000 <= mag < 0x47EFFFFFE0000000):
+        return None
+    r = mag + 0x0FFFFFFF + ((mag >> 29) & 1)
+    f = ((r >> 29) - ((1023 - 127) << 23)) & 0xFFFFFFFF
+    return struct.unpack("<f", struct.pack("<I", f | ((b >> 32) & 0x80000000)))[0]
+
+
+def split_rn(x):
+    """fdf_exact.cuh split_rn, fast path (2^-74 <= |x| < 2^127); None for the rest."""
+    b = _ub(x)
+    mag = b & ((1 << 63) - 1)
+    sgn = (b >> 32) & 0x80000000
+    if not (0x3B50000000000000 <= mag < 0x47E0000000000000):
+        return None
+    r = mag + 0x0FFFFFFF + ((mag >> 29) & 1)
+    hmag = r & ~0x1FFFFFFF
+    hi = struct.unpack("<f", struct.pack("<I", (((r >> 29) - ((1023 - 127) << 23)) & 0xFFFFFFFF) | sgn))[0]
+    units = mag - hmag
+    assert abs(units) <= 1 << 28
+    ulp = np.float32(2.0 ** ((mag >> 52) - 1075))
+    lo = np.float32(np.float32(units) * ulp)          # one rounding of the exact integer, then exact scaling
+    if units != 0 and sgn:
+        lo = -lo
+    return np.float32(hi), lo
+
+
+def test_conversions_restatement_match_numpy():
+    rng = random.Random(33)
+    for i in range(40000):
+        x = rng.uniform(1, 2) * 2.0 ** rng.randint(-140, 140) * rng.choice([1, -1])
+        if i % 3 == 0:
+            x = _short(x, rng)
+        f = d2f_rn(x)
+        if f is not None:
+            assert struct.pack("<f", f) == np.float32(x).tobytes(), x
+        sp = split_rn(x)
+        if sp is not None:
+            h = np.float32(x)
+            lo = np.float32(x - float(h))   # x - h is exact in double
+            assert sp[0].tobytes() == h.tobytes() and sp[1].tobytes() == lo.tobytes(), x
+            assert abs(float(sp[0]) + float(sp[1]) - x) <= 2.0 ** -48 * abs(x)
