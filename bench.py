@@ -608,45 +608,63 @@ def run_gpu(args, rank, ws, local, dist):
         if momentum_on(wl):
             mom = (pinned_like(np.zeros((KM, JM, IM + 1, 3))), pinned_like(np.zeros((KM, JM + 1, IM, 3))),
                    pinned_like(np.zeros((KM + 1, JM, IM, 3))))
-        from fdf_gb300.context import _ptr
+        from fdf_gb300.context import TRANSFER_IN_PLACE, TRANSFER_STAGED, _ptr
         lib, h = ctx.lib, ctx.h
         import ctypes
         got = ctypes.c_int64()
+
+        def e2e_steps(route: int, k: int):
+            """k steps through the C ABI with the host arrays: set, step, get (swarm and fields)."""
+            ctx.set_transfer_route(route)
+            split = {"set_swarm": 0.0, "step": 0.0, "get_swarm": 0.0, "get_fields": 0.0}
+            ps, n_cur, moved = 0, live[0], 0
+            barrier(dist)
+            t0 = time.perf_counter()
+            for _ in range(k):
+                ta = time.perf_counter()
+                ctx._check(lib.fdf_SetSwarm(h, n_cur, _ptr(bufs.position), _ptr(bufs.velocity), _ptr(bufs.weight),
+                                            _ptr(bufs.P), _ptr(bufs.cell), _ptr(bufs.pid), _ptr(bufs.status)))
+                tb = time.perf_counter()
+                ctx._check(lib.fdf_AdvanceStep(h, None))
+                ctx._check(lib.fdf_Synchronize(h))
+                tc = time.perf_counter()
+                ctx._check(lib.fdf_GetSwarm(h, n0, ctypes.byref(got), _ptr(bufs.position), _ptr(bufs.velocity),
+                                            _ptr(bufs.weight), _ptr(bufs.P), _ptr(bufs.cell), _ptr(bufs.pid),
+                                            _ptr(bufs.status)))
+                td = time.perf_counter()
+                ctx._check(lib.fdf_GetScatteredFields(h, _ptr(count), _ptr(avg)))
+                ctx._check(lib.fdf_GetFaceDeposits(h, _ptr(fi), _ptr(fj), _ptr(fk)))
+                if mom is not None:
+                    ctx._check(lib.fdf_GetFaceMomentum(h, _ptr(mom[0]), _ptr(mom[1]), _ptr(mom[2])))
+                te = time.perf_counter()
+                for key, v in zip(split, (tb - ta, tc - tb, td - tc, te - td)):
+                    split[key] += v
+                ps += n_cur
+                moved += n_cur + got.value
+                n_cur = got.value
+            live[0] = n_cur
+            el = reduce_max(dist, time.perf_counter() - t0)
+            ms = {kk: round(1000.0 * v / k, 2) for kk, v in split.items()}
+            gbs = {"set_swarm": round(120 * ps / split["set_swarm"] / 1e9, 1),
+                   "get_swarm": round(120 * (moved - ps) / split["get_swarm"] / 1e9, 1)}
+            return ps * ws / el, ms, gbs
+
+        live = [n0]
         k_e2e = max(3, min(args.steps, 10))
-        barrier(dist)
-        t0 = time.perf_counter()
-        ps = 0
-        n_cur = n0
-        split = {"set_swarm": 0.0, "step": 0.0, "get_swarm": 0.0, "get_fields": 0.0}
-        for _ in range(k_e2e):
-            ta = time.perf_counter()
-            ctx._check(lib.fdf_SetSwarm(h, n_cur, _ptr(bufs.position), _ptr(bufs.velocity), _ptr(bufs.weight),
-                                        _ptr(bufs.P), _ptr(bufs.cell), _ptr(bufs.pid), _ptr(bufs.status)))
-            tb = time.perf_counter()
-            ctx._check(lib.fdf_AdvanceStep(h, None))
-            ctx._check(lib.fdf_Synchronize(h))
-            tc = time.perf_counter()
-            ctx._check(lib.fdf_GetSwarm(h, n0, ctypes.byref(got), _ptr(bufs.position), _ptr(bufs.velocity),
-                                        _ptr(bufs.weight), _ptr(bufs.P), _ptr(bufs.cell), _ptr(bufs.pid),
-                                        _ptr(bufs.status)))
-            td = time.perf_counter()
-            ctx._check(lib.fdf_GetScatteredFields(h, _ptr(count), _ptr(avg)))
-            ctx._check(lib.fdf_GetFaceDeposits(h, _ptr(fi), _ptr(fj), _ptr(fk)))
-            if mom is not None:
-                ctx._check(lib.fdf_GetFaceMomentum(h, _ptr(mom[0]), _ptr(mom[1]), _ptr(mom[2])))
-            te = time.perf_counter()
-            for key, v in zip(split, (tb - ta, tc - tb, td - tc, te - td)):
-                split[key] += v
-            ps += n_cur
-            n_cur = got.value
-        el = reduce_max(dist, time.perf_counter() - t0)
+        # the library's default route (copy engines through the staging buffer) is the headline;
+        # the in-place route (layout kernels reading and writing the pinned arrays over the host
+        # link) is timed beside it in the same process
+        v_st, ms_st, gbs_st = e2e_steps(TRANSFER_STAGED, k_e2e)
+        v_ip, ms_ip, gbs_ip = e2e_steps(TRANSFER_IN_PLACE, max(3, k_e2e // 2))
+        ctx.set_transfer_route(TRANSFER_STAGED)
         link = host_link_gbs(local)
-        e2e = {"value": ps * ws / el, "unit": UNIT, "h2d_bytes_per_step": int(120 * n0),
+        e2e = {"value": v_st, "unit": UNIT, "h2d_bytes_per_step": int(120 * n0),
                "d2h_bytes_per_step": int(120 * n0 + 16 * Nn + 8 * Nf + (24 * Nf if mom is not None else 0)),
-               "steps": k_e2e,
+               "steps": k_e2e, "route": "staged (copy engines, the library default)",
                "path": "fdf_SetSwarm + fdf_AdvanceStep + fdf_GetSwarm/GetScatteredFields/GetFaceDeposits, "
                        "pinned host DMSwarm-layout arrays",
-               "ms_per_step": {k: round(1000.0 * v / k_e2e, 2) for k, v in split.items()},
+               "ms_per_step": ms_st, "transfer_gbs": gbs_st,
+               "in_place_route": {"value": v_ip, "ms_per_step": ms_ip, "transfer_gbs": gbs_ip},
                "host_link_gbs": link}
 
     accuracy = None

@@ -41,6 +41,7 @@ _SIGS = {
     "fdf_LocatePoints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 5),
     "fdf_Contra2CartDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fdf_SetTransferRoute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTimeStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_SetParticleVolume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_ReserveParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),
@@ -66,6 +67,8 @@ _SIGS = {
     "fdf_SortByCellNoAlloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetProfiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fdf_TestFailDeviceAllocations": (ctypes.c_int, [ctypes.c_int64]),
+    "fdf_TestLocatorWaitTimeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     "fdf_GetCounters": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p]),
     "fdf_GetStageTimes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "fdf_LocatorInit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),

@@ -23,6 +23,7 @@ ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG"
              97: "PETSC_ERR_GPU"}
 NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
 FORM_PLAIN_FP64, FORM_FP32, FORM_LEARNED_FP32 = 0, 1, 2
+TRANSFER_STAGED, TRANSFER_IN_PLACE = 0, 1
 LOCATOR_NPARAM = 33923
 
 
@@ -175,6 +176,10 @@ class PicContext:
             raise ValueError("ucont must be a contiguous CUDA float64 tensor [KM+1][JM+1][IM+1][3]")
         torch.cuda.current_stream(ucont.device).synchronize()
         self._check(self.lib.fdf_Contra2CartDevice(self.h, ctypes.c_void_p(ucont.data_ptr())))
+
+    def set_transfer_route(self, route: int):
+        """TRANSFER_STAGED (copy engines through a staging buffer, the default) or TRANSFER_IN_PLACE."""
+        self._check(self.lib.fdf_SetTransferRoute(self.h, int(route)))
 
     def set_form(self, form: int):
         """FORM_PLAIN_FP64 (bit-exact), FORM_FP32 (precision form) or FORM_LEARNED_FP32 (precision

@@ -19,14 +19,33 @@
 #include <string>
 #include <vector>
 
+#include <atomic>
+
 namespace {
 
-constexpr long long FDF_MAX_PARTICLES = 512LL * 1024 * 1024;
-
+// Allocations left before dev_alloc starts failing (fdf_TestFailDeviceAllocations); -1: no limit.
+std::atomic<long long> g_alloc_budget{-1};
 
 }  // namespace
 
+cudaError_t dev_alloc_hooked(void **p, size_t bytes) {
+  long long b = g_alloc_budget.load();
+  while (b >= 0) {
+    if (b == 0) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+    if (g_alloc_budget.compare_exchange_weak(b, b - 1)) break;
+  }
+  return cudaMalloc(p, bytes);
+}
+
 extern "C" {
+
+int fdf_TestFailDeviceAllocations(int64_t after) {
+  g_alloc_budget.store(after < 0 ? -1 : (long long)after);
+  return FDF_SUCCESS;
+}
 
 int fdf_ContextCreate(FdfContext **out, int device) {
   FdfContext *ctx = nullptr;
@@ -90,6 +109,15 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
     return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetGrid: too many cells or nodes (max 134M cells)");
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
+  // From here on the old grid is gone: until every buffer of the new one is in place the
+  // context refuses work (and the captured step graphs, which hold the old addresses, are
+  // invalidated), so a failed allocation below leaves no call able to touch freed memory.
+  ctx->has_grid = false;
+  ctx->has_ucat = false;
+  ctx->swarm_set = false;
+  ctx->layout_ok = false;
+  ctx->loc.has_params = false;   // a locator is trained for one grid
+  ctx->gen++;
   cfree(ctx->coor); cfree(ctx->planes); cfree(ctx->ucat); cfree(ctx->corner);
   cfree(ctx->count); cfree(ctx->avg); cfree(ctx->fi); cfree(ctx->fj); cfree(ctx->fk); cfree(ctx->cell_start);
   cfree(ctx->scan_sums);
@@ -102,26 +130,26 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   g.fIM.init((unsigned)IM); g.fJM.init((unsigned)JM); g.fMX.init((unsigned)(IM + 1)); g.fMY.init((unsigned)(JM + 1));
   ctx->g = g;
   long long nfi = (IM + 1) * JM * KM, nfj = IM * (JM + 1) * KM, nfk = IM * JM * (KM + 1);
-  CU(cudaMalloc((void **)&ctx->coor, 24ull * Nn));
-  CU(cudaMalloc((void **)&ctx->planes, 8ull * FDF_ROW * Nc));
-  CU(cudaMalloc((void **)&ctx->ucat, 24ull * Nc));
-  CU(cudaMalloc((void **)&ctx->corner, 24ull * Nn));
-  CU(cudaMalloc((void **)&ctx->count, 8ull * Nn));
-  CU(cudaMalloc((void **)&ctx->avg, 8ull * Nn));
-  CU(cudaMalloc((void **)&ctx->fi, 8ull * nfi));
-  CU(cudaMalloc((void **)&ctx->fj, 8ull * nfj));
-  CU(cudaMalloc((void **)&ctx->fk, 8ull * nfk));
-  CU(cudaMalloc((void **)&ctx->table32, 4ull * FDF_ROW32 * Nc));
-  CU(cudaMalloc((void **)&ctx->ucat32, 12ull * Nc));
-  CU(cudaMalloc((void **)&ctx->corner32, 12ull * Nn));
-  CU(cudaMalloc((void **)&ctx->count32, 4ull * Nn));
-  CU(cudaMalloc((void **)&ctx->avg32, 4ull * Nn));
-  CU(cudaMalloc((void **)&ctx->fi32, 4ull * nfi));
-  CU(cudaMalloc((void **)&ctx->fj32, 4ull * nfj));
-  CU(cudaMalloc((void **)&ctx->fk32, 4ull * nfk));
+  CU(dev_alloc((void **)&ctx->coor, 24ull * Nn));
+  CU(dev_alloc((void **)&ctx->planes, 8ull * FDF_ROW * Nc));
+  CU(dev_alloc((void **)&ctx->ucat, 24ull * Nc));
+  CU(dev_alloc((void **)&ctx->corner, 24ull * Nn));
+  CU(dev_alloc((void **)&ctx->count, 8ull * Nn));
+  CU(dev_alloc((void **)&ctx->avg, 8ull * Nn));
+  CU(dev_alloc((void **)&ctx->fi, 8ull * nfi));
+  CU(dev_alloc((void **)&ctx->fj, 8ull * nfj));
+  CU(dev_alloc((void **)&ctx->fk, 8ull * nfk));
+  CU(dev_alloc((void **)&ctx->table32, 4ull * FDF_ROW32 * Nc));
+  CU(dev_alloc((void **)&ctx->ucat32, 12ull * Nc));
+  CU(dev_alloc((void **)&ctx->corner32, 12ull * Nn));
+  CU(dev_alloc((void **)&ctx->count32, 4ull * Nn));
+  CU(dev_alloc((void **)&ctx->avg32, 4ull * Nn));
+  CU(dev_alloc((void **)&ctx->fi32, 4ull * nfi));
+  CU(dev_alloc((void **)&ctx->fj32, 4ull * nfj));
+  CU(dev_alloc((void **)&ctx->fk32, 4ull * nfk));
   CU(cudaMemsetAsync(ctx->ucat32, 0, 12ull * Nc, ctx->stream));
-  CU(cudaMalloc((void **)&ctx->cell_start, 4ull * (Nc + 2)));
-  CU(cudaMalloc((void **)&ctx->scan_sums, 4ull * scan_scratch_words(Nc + 2)));
+  CU(dev_alloc((void **)&ctx->cell_start, 4ull * (Nc + 2)));
+  CU(dev_alloc((void **)&ctx->scan_sums, 4ull * scan_scratch_words(Nc + 2)));
   CU(cudaMemsetAsync(ctx->cell_start, 0, 4ull * (Nc + 2), ctx->stream));
   CU(cudaMemsetAsync(ctx->ucat, 0, 24ull * Nc, ctx->stream));
   CU(cudaMemsetAsync(ctx->corner, 0, 24ull * Nn, ctx->stream));
@@ -161,11 +189,8 @@ int fdf_SetGrid(FdfContext *ctx, int64_t IM, int64_t JM, int64_t KM, const doubl
   CU(cudaMemcpyAsync(ctx->fbox, fb, sizeof(fb), cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->sentinel = (unsigned int)Nc;
-  ctx->loc.has_params = false;   // a locator is trained for one grid
   ctx->has_grid = true;
   ctx->gen++;
-  ctx->has_ucat = false;
-  ctx->swarm_set = false;
   return FDF_SUCCESS;
 }
 
@@ -191,6 +216,14 @@ int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized) {
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->has_ucat = true;
   ctx->gen++;
+  return FDF_SUCCESS;
+}
+
+int fdf_SetTransferRoute(FdfContext *ctx, int route) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (route != FDF_TRANSFER_STAGED && route != FDF_TRANSFER_IN_PLACE)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetTransferRoute: unknown route");
+  ctx->xfer_route = route;
   return FDF_SUCCESS;
 }
 
@@ -225,20 +258,28 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   if (capacity <= ctx->cap && ctx->swarm_mem) return FDF_SUCCESS;
   CU(cudaSetDevice(ctx->device));
   CU(cudaStreamSynchronize(ctx->stream));
+  // The held swarm goes with its buffers: until the new ones are all in place the context
+  // has no swarm and no capacity, and the captured step graphs (old addresses) are invalid.
+  ctx->swarm_set = false;
+  ctx->layout_ok = false;
+  ctx->cap = 0;
+  ctx->buf[0] = SwarmBuf{};
+  ctx->buf[1] = SwarmBuf{};
+  ctx->staging_bytes = 0;
+  ctx->gen++;
   cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->staging);
   int cap = (int)(capacity < 256 ? 256 : capacity);   // never zero: the sort always has scratch
   size_t per = swarm_bytes_per_buf(cap);
-  CU(cudaMalloc(&ctx->swarm_mem, 2 * per));
+  CU(dev_alloc(&ctx->swarm_mem, 2 * per));
+  CU(dev_alloc(&ctx->keys, 4ull * cap));
+  CU(dev_alloc(&ctx->perm, 4ull * cap));
+  CU(dev_alloc(&ctx->rank, 4ull * cap));
+  CU(dev_alloc(&ctx->staging, (size_t)cap * 120 + 1024));
   carve_swarm((char *)ctx->swarm_mem, cap, ctx->buf[0]);
   carve_swarm((char *)ctx->swarm_mem + per, cap, ctx->buf[1]);
-  CU(cudaMalloc((void **)&ctx->keys, 4ull * cap));
-  CU(cudaMalloc((void **)&ctx->perm, 4ull * cap));
-  CU(cudaMalloc((void **)&ctx->rank, 4ull * cap));
   ctx->staging_bytes = (size_t)cap * 120 + 1024;
-  CU(cudaMalloc(&ctx->staging, ctx->staging_bytes));
   ctx->cap = cap;
   ctx->gen++;
-  ctx->swarm_set = false;
   return FDF_SUCCESS;
 }
 
@@ -296,7 +337,7 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
   const void *arrays[7] = {position, velocity, weight, P, cell_id, pid, status};
   void *views[7];
-  if (n > 0 && host_views(arrays, views)) {
+  if (n > 0 && ctx->xfer_route == FDF_TRANSFER_IN_PLACE && host_views(arrays, views)) {
     ctx->cur = 0;
     launch_swarm_from_host(views, (int)n, ctx->g, ctx->buf[0], form_is32(ctx->form), ctx->stream);
     CHECK_LAUNCH();
@@ -395,7 +436,7 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *positio
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
   const void *arrays[7] = {position, velocity, weight, P, cell_id, pid, status};
   void *views[7];
-  if (host_views(arrays, views)) {
+  if (ctx->xfer_route == FDF_TRANSFER_IN_PLACE && host_views(arrays, views)) {
     launch_swarm_to_host(ctx->buf[ctx->cur], (int)n, ctx->g, views, form_is32(ctx->swarm_form), ctx->stream);
     CHECK_LAUNCH();
     ctx->launches += 1;
@@ -927,12 +968,15 @@ int fdf_SetMomentumDeposit(FdfContext *ctx, int enable) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_SetMomentumDeposit: call fdf_SetGrid first");
   CU(cudaSetDevice(ctx->device));
-  if (enable && !ctx->mom) {
+  if (enable && (!ctx->mom || !ctx->mom32)) {
     const GridDims &g = ctx->g;
     const long long nf = (g.IM + 1LL) * g.JM * g.KM + g.IM * (g.JM + 1LL) * g.KM + (long long)g.IM * g.JM * (g.KM + 1LL);
     CU(cudaStreamSynchronize(ctx->stream));
-    CU(cudaMalloc((void **)&ctx->mom, 24ull * nf));
-    CU(cudaMalloc((void **)&ctx->mom32, 12ull * nf));
+    ctx->momentum = false;
+    ctx->gen++;
+    cfree(ctx->mom); cfree(ctx->mom32);
+    CU(dev_alloc(&ctx->mom, 24ull * nf));
+    CU(dev_alloc(&ctx->mom32, 12ull * nf));
     CU(cudaMemset(ctx->mom, 0, 24ull * nf));
     CU(cudaMemset(ctx->mom32, 0, 12ull * nf));
   }

@@ -61,6 +61,7 @@ struct FdfContext {
   DevCounters *cnt = nullptr;
   void *staging = nullptr;
   size_t staging_bytes = 0;
+  int xfer_route = FDF_TRANSFER_STAGED;   // fdf_SetTransferRoute
   unsigned int sentinel = 0;
   bool swarm_set = false;
   bool layout_ok = false;   // the held particles are sorted by (cell, PID) and cell_start matches them
@@ -138,6 +139,15 @@ template <typename T>
 inline void cfree(T *&p) {
   if (p) cudaFree((void *)p);
   p = nullptr;
+}
+
+// Device allocations of the context's long-lived buffers go through dev_alloc, so that a test
+// can make them fail on the host (fdf_TestFailDeviceAllocations) and check that the context
+// is left refusing work instead of holding freed pointers.
+cudaError_t dev_alloc_hooked(void **p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_alloc(T **p, size_t bytes) {
+  return dev_alloc_hooked(reinterpret_cast<void **>(p), bytes);
 }
 
 

@@ -24,6 +24,7 @@
 #define FDF_DISTANCE_THRESHOLD 1e-11
 #define FDF_INTERP_DIST_TOL 1e-14
 #define FDF_BBOX_TOL 1e-6
+#define FDF_MAX_PARTICLES (512LL * 1024 * 1024)   // particle slots of one context or one sort call
 #define FDF_GUESS_WALK 4      // evaluations allowed to the walk from a learned guess
 #define FDF_GUESS_REACH 16    // largest index distance from the previous cell a guess may settle at
 

@@ -81,14 +81,18 @@ TrainScratch carve_scratch(void *base, int B) {
 
 int alloc_params(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
-  if (L.params) return FDF_SUCCESS;
-  CU(cudaMalloc((void **)&L.params, 4ull * MLP_NPARAM));
-  CU(cudaMalloc((void **)&L.grads, 4ull * MLP_NPARAM));
-  CU(cudaMalloc((void **)&L.adam_m, 4ull * MLP_NPARAM));
-  CU(cudaMalloc((void **)&L.adam_v, 4ull * MLP_NPARAM));
-  CU(cudaMalloc((void **)&L.params_bf, 2ull * MLP_NPARAM));
-  CU(cudaMalloc((void **)&L.bias, 4ull * MLP_BIAS_WORDS));
-  CU(cudaMalloc((void **)&L.tc_img, mlp_tc_image_bytes()));
+  if (L.params && L.grads && L.adam_m && L.adam_v && L.params_bf && L.bias && L.tc_img) return FDF_SUCCESS;
+  // all or none: a partial set left by a failed allocation is freed and made again
+  L.has_params = false;
+  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf); cfree(L.bias);
+  cfree(L.tc_img);
+  CU(dev_alloc(&L.params, 4ull * MLP_NPARAM));
+  CU(dev_alloc(&L.grads, 4ull * MLP_NPARAM));
+  CU(dev_alloc(&L.adam_m, 4ull * MLP_NPARAM));
+  CU(dev_alloc(&L.adam_v, 4ull * MLP_NPARAM));
+  CU(dev_alloc(&L.params_bf, 2ull * MLP_NPARAM));
+  CU(dev_alloc(&L.bias, 4ull * MLP_BIAS_WORDS));
+  CU(dev_alloc(&L.tc_img, mlp_tc_image_bytes()));
   return FDF_SUCCESS;
 }
 
@@ -97,7 +101,7 @@ int ensure_scratch(FdfContext *ctx, int B) {
   if (L.batch_cap >= B && L.scratch) return FDF_SUCCESS;
   cfree(L.scratch);
   L.batch_cap = 0;
-  CU(cudaMalloc(&L.scratch, scratch_bytes(B)));
+  CU(dev_alloc(&L.scratch, scratch_bytes(B)));
   L.batch_cap = B;
   return FDF_SUCCESS;
 }
@@ -176,10 +180,10 @@ int locator_reserve(FdfContext *ctx) {
   if (L.pending_cap >= ctx->cap && L.pending) return FDF_SUCCESS;
   cfree(L.pending); cfree(L.guess); cfree(L.pflag); cfree(L.scan_sums);
   L.pending_cap = 0;
-  CU(cudaMalloc((void **)&L.pending, 4ull * ctx->cap));
-  CU(cudaMalloc((void **)&L.guess, 4ull * ctx->cap));
-  CU(cudaMalloc((void **)&L.pflag, 4ull * (2 * ((ctx->cap + 31) / 32) + 1)));
-  CU(cudaMalloc((void **)&L.scan_sums, 4ull * scan_scratch_words(ctx->cap + 1)));
+  CU(dev_alloc(&L.pending, 4ull * ctx->cap));
+  CU(dev_alloc(&L.guess, 4ull * ctx->cap));
+  CU(dev_alloc(&L.pflag, 4ull * (2 * ((ctx->cap + 31) / 32) + 1)));
+  CU(dev_alloc(&L.scan_sums, 4ull * scan_scratch_words(ctx->cap + 1)));
   L.pending_cap = ctx->cap;
   return FDF_SUCCESS;
 }
@@ -373,7 +377,10 @@ int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t 
   return FDF_SUCCESS;
 }
 
-int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs) {
+// fdf_LocatorPredict, and with stall_test the time-out test of fdf_TestLocatorWaitTimeout.
+// The call reports only its own launch's tensor-core time-out (a word of its own, cleared first).
+static int locator_predict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs,
+                           int stall_test) {
   if (!ctx || (n > 0 && (!position || !cell_id))) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorPredict: null argument");
   if (n < 0 || n > 0x7fffffffLL) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorPredict: n out of range");
   if (!ctx->loc.has_params) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorPredict: no locator");
@@ -383,18 +390,20 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
   std::vector<double> soa(3 * (size_t)n);
   for (int64_t p = 0; p < n; ++p)
     for (int d = 0; d < 3; ++d) soa[d * (size_t)n + p] = position[3 * p + d];
-  double *d_pos = nullptr;
-  int *d_guess = nullptr;
-  float *d_out = nullptr;
-  CU(cudaMalloc((void **)&d_pos, 24ull * n));
-  if (cudaMalloc((void **)&d_guess, 4ull * n) != cudaSuccess || cudaMalloc((void **)&d_out, 12ull * n) != cudaSuccess) {
-    cudaFree(d_pos); cudaFree(d_guess);
-    return fail(ctx, FDF_ERR_MEM, "fdf_LocatorPredict: out of device memory");
-  }
+  // one buffer: positions [3][n] f64, outputs [n][3] f32, guesses [n] i32, the error word
+  const size_t off_out = 24ull * n, off_guess = off_out + (12ull * n + 255) / 256 * 256,
+               off_err = off_guess + (4ull * n + 255) / 256 * 256;
+  char *mem = nullptr;
+  CU(cudaMalloc((void **)&mem, off_err + 256));
+  double *d_pos = (double *)mem;
+  float *d_out = (float *)(mem + off_out);
+  int *d_guess = (int *)(mem + off_guess);
+  unsigned int *d_err = (unsigned int *)(mem + off_err);
   cudaError_t e = cudaMemcpyAsync(d_pos, soa.data(), 24ull * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_err, 0, sizeof(unsigned int), s);
   if (e == cudaSuccess) {
     mlp_guess_tc(ctx->loc.tc_img, ctx->loc.bias, ctx->loc.norm, d_pos, d_pos + n, d_pos + 2 * n, 0, nullptr,
-                 nullptr, (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, &ctx->cnt->err, s, d_out);
+                 nullptr, (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, d_err, s, d_out, stall_test);
     ctx->launches += 1;
     e = cudaGetLastError();
   }
@@ -402,9 +411,9 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
   if (e == cudaSuccess) e = cudaMemcpyAsync(gh.data(), d_guess, 4ull * n, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && outputs) e = cudaMemcpyAsync(outputs, d_out, 12ull * n, cudaMemcpyDeviceToHost, s);
   unsigned int errw = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&errw, &ctx->cnt->err, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&errw, d_err, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(d_pos); cudaFree(d_guess); cudaFree(d_out);
+  cudaFree(mem);
   if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_LocatorPredict: ") + cudaGetErrorString(e));
   if (errw & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "fdf_LocatorPredict: tensor-core wait timed out");
   const long long IM = ctx->g.IM, JM = ctx->g.JM;
@@ -415,6 +424,17 @@ int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64
     cell_id[3 * p + 2] = c / (IM * JM);
   }
   return FDF_SUCCESS;
+}
+
+int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs) {
+  return locator_predict(ctx, position, n, cell_id, outputs, 0);
+}
+
+int fdf_TestLocatorWaitTimeout(FdfContext *ctx, const double *position, int64_t n) {
+  if (!ctx || !position) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_TestLocatorWaitTimeout: null argument");
+  if (n < 1) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_TestLocatorWaitTimeout: n must be positive");
+  std::vector<int64_t> cells(3 * (size_t)n);
+  return locator_predict(ctx, position, n, cells.data(), nullptr, 1);
 }
 
 int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells) {

@@ -59,10 +59,11 @@ void mlp_init_params_host(unsigned long long seed, float *params);
 // arrays; list == nullptr: particles 0 .. n_host-1, positions read as FP64 from x, y, z.
 // yout (optional): the network's outputs [n][3].  The weights are packed once into the CTA's
 // shared-memory image (mlp_tc_image_bytes() bytes); a timed-out tensor-core wait sets
-// ERRBIT_TC_TIMEOUT in *err.
+// ERRBIT_TC_TIMEOUT in *err.  stall_test != 0 is for tests of that path: the kernel issues no
+// MMA, so its first bounded wait (1024 polls) runs out and the CTAs return with the error bit.
 size_t mlp_tc_image_bytes();
 void mlp_pack_tc(const float *params, unsigned char *img, cudaStream_t s);
 void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &norm, const double *x, const double *y,
                   const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count,
                   int n_host, int n_cap, GridDims g, int *guess, int num_sms, unsigned int *err, cudaStream_t s,
-                  float *yout = nullptr);
+                  float *yout = nullptr, int stall_test = 0);

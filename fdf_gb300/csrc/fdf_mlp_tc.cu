@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                    const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ pz,
                    int pairs, const unsigned int *__restrict__ list, const unsigned long long *__restrict__ list_count,
                    int n_host, GridDims g, int *__restrict__ guess, float *__restrict__ yout,
-                   unsigned int *__restrict__ err) {
+                   unsigned int *__restrict__ err, unsigned long long wait_limit, int stall_test) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5;
   const int pipe = tid >> 7, row = tid & 127;     // warpgroup = pipeline; thread = tile row
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   // waits for the MMAs this pipeline committed last; its 128 threads agree on a time-out
   auto wait_mma = [&]() -> bool {
     bool done = false;
-    for (unsigned long long it = 0; it < WAIT_LIMIT && !done; ++it) done = mbar_try_wait(bar_addr, phase);
+    for (unsigned long long it = 0; it < wait_limit && !done; ++it) done = mbar_try_wait(bar_addr, phase);
     phase ^= 1u;
     if (!done) tflag[pipe] = 1u;
     pipe_sync();
@@ -319,7 +319,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   for (long long tile = tile0; tile < ntiles; tile += tstride) {
     const long long r = tile * TC_ROWS + row;
     *reinterpret_cast<uint4 *>(a1s + op_off(row, 0, 256)) = make_uint4(pack2(cx, cy), pack2(cz, 0.f), 0u, 0u);
-    issue(0);
+    // stall_test (tests of the time-out path only): nothing is issued or committed, so the wait
+    // below runs out with no MMA in flight
+    if (!stall_test) issue(0);
     load_inputs(tile + tstride, cx, cy, cz);   // the next tile's positions, while this one computes
     if (!wait_mma()) { timed_out = true; break; }
     epilogue(hb2);
@@ -371,7 +373,7 @@ void mlp_pack_tc(const float *params, unsigned char *img, cudaStream_t s) {
 void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &norm, const double *x, const double *y,
                   const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count,
                   int n_host, int n_cap, GridDims g, int *guess, int num_sms, unsigned int *err, cudaStream_t s,
-                  float *yout) {
+                  float *yout, int stall_test) {
   static int attr_device = -1;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -385,5 +387,6 @@ void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &no
   if (blocks > cap_blocks) blocks = cap_blocks;
   if (blocks < 1) blocks = 1;
   k_mlp_guess_tc<<<(unsigned)blocks, TC_THREADS, SM_TOTAL, s>>>(img, bias, norm, x, y, z, pairs, list, list_count,
-                                                                 n_host, g, guess, yout, err);
+                                                                 n_host, g, guess, yout, err,
+                                                                 stall_test ? 1024ull : WAIT_LIMIT, stall_test);
 }

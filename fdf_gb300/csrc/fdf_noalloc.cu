@@ -12,9 +12,12 @@
 // Limits and rules:
 //  * at most FDF_NOALLOC_MAX_CELLS cells (larger requests return FDF_ERR_ARG_OUTOFRANGE
 //    and launch nothing);
+//  * at most FDF_MAX_PARTICLES particle slots, as fdf_SortByCell;
 //  * the first call on a device looks up the array's device address there
 //    (cudaGetSymbolAddress with that device current) and caches it; make that first
-//    call outside any stream capture;
+//    call outside any stream capture.  The cached address belongs to the device's
+//    primary context: a caller that resets the device (cudaDeviceReset) must not call
+//    this function afterwards in the same process;
 //  * all calls share the one array, and each call clears the part that must start at
 //    zero, so results never depend on an earlier call -- but two calls whose work
 //    overlaps on the GPU (different streams, or different host threads) race on it:
@@ -64,7 +67,7 @@ extern "C" int fdf_SortByCellNoAlloc(const int32_t *cell_ids, int64_t n, int64_t
                                      uint32_t *cell_start, void *stream) {
   if (n > 0 && (!cell_ids || !perm)) return FDF_ERR_ARG_NULL;
   if (!cell_start) return FDF_ERR_ARG_NULL;
-  if (n < 0 || n > 0x7fffffffLL || ncells < 1 || ncells > FDF_NOALLOC_MAX_CELLS) return FDF_ERR_ARG_OUTOFRANGE;
+  if (n < 0 || n > FDF_MAX_PARTICLES || ncells < 1 || ncells > FDF_NOALLOC_MAX_CELLS) return FDF_ERR_ARG_OUTOFRANGE;
   unsigned int *scratch = nullptr;
   int r = noalloc_scratch(&scratch);
   if (r) return r;

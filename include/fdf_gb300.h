@@ -127,10 +127,17 @@ int fdf_SetTimeStep(FdfContext *ctx, double dt);                 /* user->dt    
 int fdf_SetParticleVolume(FdfContext *ctx, double volume);       /* face deposit V_p    */
 
 /* ---- swarm transfer (DMSwarm fields, ParticleSwarm.c:64-96, [n][bs] layout) ----
- * When all seven arrays of a call are page-locked host memory (cudaHostAlloc /
- * cudaHostRegister) and 16-byte aligned, the layout kernels read (fdf_SetSwarm) or write
- * (fdf_GetSwarm) them in place over the host link; otherwise they are copied through a device
- * staging buffer.  The results are the same either way. */
+ * Route (fdf_SetTransferRoute): STAGED (default) copies the arrays with the copy engines, in
+ * particle chunks, through a device staging buffer, the layout conversion of one chunk
+ * overlapping the copies of the next; IN_PLACE has the layout kernels read (fdf_SetSwarm) or
+ * write (fdf_GetSwarm) the arrays over the host link when all seven arrays of a call are
+ * page-locked host memory (cudaHostAlloc / cudaHostRegister) and 16-byte aligned, and falls
+ * back to STAGED otherwise.  How fast kernels reach host memory depends on the machine (the
+ * copy engines ran at the link's rate on every GB300 tried, kernel accesses at a quarter of it
+ * on one), hence the default.  The results are the same either way. */
+#define FDF_TRANSFER_STAGED 0
+#define FDF_TRANSFER_IN_PLACE 1
+int fdf_SetTransferRoute(FdfContext *ctx, int route);
 int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity);
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity,
                  const double *weight, const double *P, const int64_t *cell_id, const int64_t *pid,
@@ -228,7 +235,9 @@ int fdf_SortByCell(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t 
  * (larger requests return FDF_ERR_ARG_OUTOFRANGE).  The first call on a device looks up
  * that array's address on the current device: make it outside stream capture.  All
  * calls share the array (each clears what must start at zero), so calls that overlap
- * on the GPU race: serialise them.  Calls no cudaMalloc/cudaFree. */
+ * on the GPU race: serialise them.  The looked-up address belongs to the device's primary
+ * context: after a cudaDeviceReset of that device, do not call it again in the process.
+ * Calls no cudaMalloc/cudaFree. */
 #define FDF_NOALLOC_MAX_CELLS 1048576
 int fdf_SortByCellNoAlloc(const int32_t *cell_ids, int64_t n, int64_t ncells, uint32_t *perm, uint32_t *cell_start,
                           void *stream);
@@ -313,6 +322,21 @@ int fdf_SetProfiling(FdfContext *ctx, int enable);
  * corner nodes computed (the steps compute only nodes next to occupied cells). */
 int fdf_GetCounters(FdfContext *ctx, int64_t *particle_steps, int64_t *walk_evals, int64_t *corner_nodes);
 int fdf_GetStageTimes(FdfContext *ctx, double *ms_total, int64_t *launches, int nstages);
+
+/* ---- testing ---- */
+/* Failure injection on the host, for tests of the error paths (no counterpart in the
+ * reference): the next `after` device allocations of the contexts' buffers succeed and every
+ * later one fails as out of memory (FDF_ERR_MEM), until called again with a negative value
+ * (no limit).  A context whose fdf_SetGrid or fdf_ReserveParticles failed this way holds no
+ * grid (or no swarm) and returns FDF_ERR_ARG_WRONGSTATE from the calls that need one.
+ * Process-wide; not for production use. */
+int fdf_TestFailDeviceAllocations(int64_t after);
+/* Time-out path of the learned locator's tensor-core kernel: fdf_LocatorPredict's launch on n
+ * positions [n][3] with no MMA issued, so that each CTA's first bounded mbarrier wait (1024
+ * polls) runs out; the CTAs free their tensor memory and return, and the call returns
+ * FDF_ERR_GPU as a real time-out would.  Nothing is left in flight: the next call works.
+ * No counterpart in the reference. */
+int fdf_TestLocatorWaitTimeout(FdfContext *ctx, const double *position, int64_t n);
 
 #ifdef __cplusplus
 }

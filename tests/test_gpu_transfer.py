@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 
 from fdf_gb300 import workloads as W
-from fdf_gb300.context import FORM_FP32, FORM_PLAIN_FP64, PicContext, SwarmArrays
+from fdf_gb300.context import (FORM_FP32, FORM_PLAIN_FP64, TRANSFER_IN_PLACE, TRANSFER_STAGED, PicContext,
+                               SwarmArrays)
 
 pytestmark = pytest.mark.gpu
 
@@ -65,7 +66,7 @@ def _pinned(a, offset=0):
     return out, t
 
 
-def _roundtrip(form, s, pinned, offset=0, launches=None):
+def _roundtrip(form, s, pinned, offset=0, launches=None, route=None):
     wl = W.config_sinusoidal(IM=8, JM=8, KM=16, n=10, cfl=1.0, steps=1)
     keep = []
     ins = []
@@ -79,6 +80,8 @@ def _roundtrip(form, s, pinned, offset=0, launches=None):
     from fdf_gb300.context import _ptr
     with PicContext(0) as ctx:
         ctx.set_form(form)
+        if route is not None:
+            ctx.set_transfer_route(route)
         ctx.set_grid(wl.coor)
         l0 = ctx.launches
         ctx._check(ctx.lib.fdf_SetSwarm(ctx.h, s.n, *[_ptr(a) for a in ins]))
@@ -99,17 +102,22 @@ def _roundtrip(form, s, pinned, offset=0, launches=None):
 
 @pytest.mark.parametrize("form", [FORM_PLAIN_FP64, FORM_FP32])
 def test_page_locked_arrays_in_place(require_gpu, form):
-    """Page-locked, 16-byte aligned arrays are read and written in place by the layout kernels;
-    the swarm is the staged route's bit for bit (and an unaligned page-locked set takes the
-    staged route).  4500003 particles: a ragged last tile, and two chunks on the staged route."""
+    """With the in-place route, page-locked, 16-byte aligned arrays are read and written in place
+    by the layout kernels; the swarm is the staged route's bit for bit (and an unaligned
+    page-locked set takes the staged route).  By default (the staged route) page-locked arrays are
+    copied by the copy engines like any other.  4500003 particles: a ragged last tile, and two
+    chunks on the staged route."""
     n = 4_500_003
     s = _swarm(n, (8, 8, 16), np.random.default_rng(4))
     s.cell[s.cell[:, 0] < 0] = -1
     counts = []
     ref = _roundtrip(form, s, pinned=False, launches=counts)
-    direct = _roundtrip(form, s, pinned=True, launches=counts)
-    skewed = _roundtrip(form, s, pinned=True, offset=8, launches=counts)
-    assert counts == [2, 1, 2]   # staged: one layout kernel per chunk; in place: one for the swarm
-    for f, a, b, c in zip(FIELDS, ref, direct, skewed):
-        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), f
-        assert np.array_equal(a.view(np.uint8), c.view(np.uint8)), f
+    direct = _roundtrip(form, s, pinned=True, launches=counts, route=TRANSFER_IN_PLACE)
+    skewed = _roundtrip(form, s, pinned=True, offset=8, launches=counts, route=TRANSFER_IN_PLACE)
+    default = _roundtrip(form, s, pinned=True, launches=counts)
+    staged = _roundtrip(form, s, pinned=True, launches=counts, route=TRANSFER_STAGED)
+    # staged: one layout kernel per chunk; in place: one for the swarm
+    assert counts == [2, 1, 2, 2, 2]
+    for f, a, b, c, d, e in zip(FIELDS, ref, direct, skewed, default, staged):
+        for x in (b, c, d, e):
+            assert np.array_equal(a.view(np.uint8), x.view(np.uint8)), f
