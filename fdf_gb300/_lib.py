@@ -39,6 +39,7 @@ _SIGS = {
     "fdf_InterpolateAllFieldsToSwarm": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_ScatterAllParticleFieldsToEulerFields": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_LocatePoints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 5),
+    "fdf_InterpolatePoints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3),
     "fdf_Contra2CartDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTransferRoute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -312,6 +312,14 @@ class PicContext:
         self._check(self.lib.fdf_LocatePoints(self.h, n, _ptr(position), _ptr(cin), _ptr(cout), _ptr(w), _ptr(st)))
         return cout, w, st
 
+    def interpolate_points(self, cell: np.ndarray, weight: np.ndarray) -> np.ndarray:
+        """The reference's interpolation for caller-held particles (cells [n][3], weights [n][3]), in order."""
+        cell = np.ascontiguousarray(cell, dtype=np.int64).reshape(-1, 3)
+        weight = np.ascontiguousarray(weight, dtype=np.float64).reshape(-1, 3)
+        vel = np.empty((len(cell), 3))
+        self._check(self.lib.fdf_InterpolatePoints(self.h, len(cell), _ptr(cell), _ptr(weight), _ptr(vel)))
+        return vel
+
     # -- the hot path
     def initial_setup(self) -> FdfStepInfo:
         info = FdfStepInfo()

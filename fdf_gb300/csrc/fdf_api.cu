@@ -852,6 +852,60 @@ int fdf_LocatePoints(FdfContext *ctx, int64_t n, const double *position, const i
   return FDF_SUCCESS;
 }
 
+int fdf_InterpolatePoints(FdfContext *ctx, int64_t n, const int64_t *cell, const double *weight, double *velocity) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (n > 0 && (!cell || !weight || !velocity)) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_InterpolatePoints: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_InterpolatePoints: call fdf_SetGrid first");
+  if (!ctx->has_ucat) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_InterpolatePoints: call fdf_SetUcat first");
+  if (n < 0 || n > FDF_MAX_PARTICLES) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_InterpolatePoints: n out of range");
+  if (n == 0) return FDF_SUCCESS;
+  CU(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const GridDims &g = ctx->g;
+  const int m = (int)n;
+  // the points as a temporary plain-form swarm in their own order (no sort): cells and weights
+  // in, velocities out; cell_start only carries the count the gather reads at [Nc], [Nc + 1]
+  void *mem = nullptr;
+  const size_t sw = swarm_bytes_per_buf(m), aos = 24ull * m, one = 8ull * m;
+  const size_t bytes = sw + 4 * aos + 3 * one + 4ull * (g.Nc + 2) + sizeof(DevCounters) + 256 * 10;
+  CU(cudaMalloc(&mem, bytes));
+  char *p = (char *)mem;
+  SwarmBuf tb;
+  carve_swarm(p, m, tb);
+  auto take = [&](size_t nb) { char *q = p; p += (nb + 255) / 256 * 256; return q; };
+  take(sw);
+  double *d_w = (double *)take(aos);
+  long long *d_cell = (long long *)take(aos);
+  double *d_zero = (double *)take(aos);     // position, velocity, P, pid, status (0 = NEEDS_LOCATION)
+  double *d_vel = (double *)take(aos);
+  double *d_P = (double *)take(one);
+  long long *d_pid = (long long *)take(one);
+  long long *d_st = (long long *)take(one);
+  unsigned int *cs = (unsigned int *)take(4ull * (g.Nc + 2));
+  DevCounters *tc = (DevCounters *)take(sizeof(DevCounters));
+  const unsigned int counts[2] = {(unsigned int)m, (unsigned int)m};
+  cudaError_t e = cudaMemcpyAsync(d_w, weight, aos, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_cell, cell, aos, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_zero, 0, aos, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cs + g.Nc, counts, sizeof(counts), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(tc, 0, sizeof(DevCounters), s);
+  if (e == cudaSuccess) {
+    // every node of the corner field (the swarm steps compute only the nodes they need)
+    launch_center_to_corner(ctx->ucat, g, ctx->corner, nullptr, nullptr, s);
+    launch_swarm_from_aos(d_zero, d_zero, d_w, d_zero, d_cell, (const long long *)d_zero, (const long long *)d_zero,
+                          m, g, tb, s);
+    launch_gather_interp(tb, tb, m, g, ctx->corner, nullptr, cs, tc, s, INTERP_KEEP);
+    launch_swarm_to_aos(tb, m, g, d_zero, d_vel, d_w, d_P, d_cell, d_pid, d_st, s);
+    ctx->launches += 4;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(velocity, d_vel, aos, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(mem);
+  if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_InterpolatePoints: ") + cudaGetErrorString(e));
+  return FDF_SUCCESS;
+}
+
 int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   FdfStepInfo local{};

@@ -216,6 +216,13 @@ int fdf_ScatterAllParticleFieldsToEulerFields(FdfContext *ctx);
 int fdf_LocatePoints(FdfContext *ctx, int64_t n, const double *position, const int64_t *cell_in, int64_t *cell_out,
                      double *weight, int64_t *status);
 
+/* InterpolateEulerFieldToSwarm (interpolation.c:1205-1399) for particles the caller holds (a
+ * DMSwarm kept on the host, probes): the velocity of n particles from their cells cell [n][3] and
+ * weights weight [n][3], in the caller's order, bit-identical to the reference; a cell index
+ * outside 0..IM-1, 0..JM-1, 0..KM-1 gives velocity zero, as the reference's stencil guard does.
+ * The corner field is made from the context's ucat (every node).  Host arrays. */
+int fdf_InterpolatePoints(FdfContext *ctx, int64_t n, const int64_t *cell, const double *weight, double *velocity);
+
 /* ---- sort by cell (the per-step re-sort of the hot path, as a standalone call) ---- */
 /* Stable counting sort of n particle slots by cell id, all pointers on the device.
  * Slots whose id is negative or >= ncells get no place.  On return cell_start[c] is the
