@@ -229,29 +229,39 @@ def time_oracle(wl, budget_s: float, max_steps: int, nthreads: int):
 
 
 def run_reference(args, rank):
+    """The reference algorithm on the host cores: the CPU restatement of the path (OpenMP over all
+    cores), on the whole workload -- every particle, the full grid -- from its initial setup, then
+    W warm-up steps and K timed steps, each one full step of the reference's loop."""
     if rank != 0:
         return
+    from fdf_gb300.context import SwarmArrays
     from oracle import oracle as O
     O.build()
     wl = workload(args.workload)
     nthreads = os.cpu_count() or 1
-    vals = []
-    samples = ""
+    pos, cell, pid = wl.sample(wl.n)
+    s0 = SwarmArrays.create(pos, cell=cell, pid=pid)
+    del pos, cell, pid
+    os_ = O.Swarm(pos=s0.position, vel=s0.velocity, weight=s0.weight, P=s0.P, cell=s0.cell, pid=s0.pid,
+                  status=s0.status, n=s0.n)
+    sim = O.Simulation(O.Grid(wl.coor), wl.ucat_node_sized(), os_, wl.dt, nthreads=nthreads)
+    sim.initial_setup()
     for _ in range(args.warmup):
-        time_oracle(wl, budget_s=2.0, max_steps=1, nthreads=nthreads)
+        sim.step()
+    psteps = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, st, el, samples = time_oracle(wl, budget_s=float(args.cpu_seconds) / max(args.steps, 1),
-                                         max_steps=1000, nthreads=nthreads)
-        vals.append(v)
+        psteps += os_.n
+        sim.step()
     total = time.perf_counter() - t0
-    value = float(np.median(vals))
+    value = psteps / total
+    sample = f"full workload: {wl.n} particles, {args.warmup} warm-up + {args.steps} timed steps"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl.name, "form": "reference algorithm (CPU restatement)", "cores": nthreads},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": samples},
+            "config": {"workload": wl.name, "form": "reference algorithm (CPU restatement, pinned bit for bit to "
+                                                    "the reference's own C compiled here)", "cores": nthreads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -438,56 +448,197 @@ def learned_identity(ctx, wl, args, steps: int) -> dict:
             "cells_differing": int(np.any(sa.cell != sb.cell, axis=1).sum()) if sa.n == sb.n else None}
 
 
-def fp32_accuracy(ctx, wl, steps: int, nthreads: int) -> dict:
-    """The precision form against the plain FP64 oracle from the same initial state, on the
-    full workload: per-field max / RMS errors over the particles present in both."""
+def _by_pid(pid: np.ndarray, a: np.ndarray, n_ids: int, fill) -> np.ndarray:
+    """a scattered into a PID-indexed array of n_ids rows (PIDs are 0 .. n_ids-1), O(n)."""
+    out = np.full((n_ids,) + a.shape[1:], fill, dtype=a.dtype)
+    out[pid] = a
+    return out
+
+
+def compare_by_pid(gpu, ref: dict, n_ids: int) -> dict:
+    """Bit-for-bit comparison of two swarms by PID (any order): the particle sets, then every field
+    (floating-point fields compared as bit patterns).  Returns per-field identical flags and the
+    number of particles that differ in each."""
+    present_g = np.zeros(n_ids, bool)
+    present_g[gpu.pid] = True
+    present_r = np.zeros(n_ids, bool)
+    present_r[ref["pid"]] = True
+    out = {"particles": int(len(gpu.pid)), "oracle_particles": int(len(ref["pid"])),
+           "same_particle_set": bool(np.array_equal(present_g, present_r))}
+    both = present_g & present_r
+    for name, g, r in (("cell", gpu.cell, ref["cell"]), ("status", gpu.status, ref["status"]),
+                       ("position", gpu.position, ref["pos"]), ("velocity", gpu.velocity, ref["vel"]),
+                       ("weight", gpu.weight, ref["weight"]), ("P", gpu.P, ref["P"])):
+        gi = g.view(np.int64) if g.dtype == np.float64 else g
+        ri = r.view(np.int64) if r.dtype == np.float64 else r
+        a = _by_pid(gpu.pid, gi, n_ids, -7)
+        b = _by_pid(ref["pid"], ri, n_ids, -7)
+        diff = (a != b).reshape(n_ids, -1).any(axis=1) & both
+        out[name] = {"identical": bool(not diff.any()), "particles_differing": int(diff.sum())}
+        del a, b, diff
+    return out
+
+
+def plain_parity_full(ctx, wl, steps: int, nthreads: int) -> dict:
+    """The plain FP64 form against the FP64 oracle on the whole workload (every particle, the full
+    grid) from the same initial state: initial setup, then `steps` steps; every swarm field, the
+    removal counts, ParticleCount, the P average and the face deposits (with momentum where the
+    workload deposits it), bit for bit."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    ctx.load_workload(wl, form=FORMS["plain_fp64"])
+    mom = momentum_on(wl)
+    if mom:
+        ctx.set_momentum_deposit(True)
+    s0 = ctx.get_swarm()
+    n0 = s0.n
+    os_ = O.Swarm(pos=s0.position, vel=s0.velocity, weight=s0.weight, P=s0.P, cell=s0.cell, pid=s0.pid,
+                  status=s0.status, n=n0)
+    del s0
+    ctx.initial_setup()
+    removed_gpu = []
+    for _ in range(steps):
+        info = ctx.step()
+        removed_gpu.append((int(info.removed_lost), int(info.removed_oob)))
+    gpu = ctx.get_swarm()
+    gcount, gavg = ctx.get_scattered()
+    gfaces = ctx.get_faces()
+    gmom = ctx.get_face_momentum() if mom else None
+    t_gpu = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    g = O.Grid(wl.coor)
+    sim = O.Simulation(g, wl.ucat_node_sized(), os_, wl.dt, nthreads=nthreads)
+    sim.initial_setup()
+    removed_ref = []
+    for _ in range(steps):
+        info = sim.step()
+        removed_ref.append((int(info.removed_lost), int(info.removed_oob)))
+    t_oracle = time.perf_counter() - t1
+    t2 = time.perf_counter()
+    out = compare_by_pid(gpu, os_.view(), n0)
+    out["removed_per_step"] = {"gpu": removed_gpu, "oracle": removed_ref, "identical": removed_gpu == removed_ref}
+    out["count"] = bool(np.array_equal(gcount.view(np.int64), sim.count.view(np.int64)))
+    out["P_avg"] = bool(np.array_equal(gavg.view(np.int64), sim.avg.view(np.int64)))
+    del gpu
+    f = O.deposit_faces(g, os_, volume=wl.volume, momentum=mom)
+    out["faces"] = all(bool(np.array_equal(a.view(np.int64), f[k].view(np.int64)))
+                       for a, k in zip(gfaces, ("fi", "fj", "fk")))
+    if mom:
+        out["momentum_faces"] = all(bool(np.array_equal(a.view(np.int64), f[k].view(np.int64)))
+                                    for a, k in zip(gmom, ("mom_i", "mom_j", "mom_k")))
+    fields = ("same_particle_set", "cell", "status", "position", "velocity", "weight", "P")
+    out["identical"] = bool(all(out[k] if isinstance(out[k], bool) else out[k]["identical"] for k in fields)
+                            and out["removed_per_step"]["identical"] and out["count"] and out["P_avg"]
+                            and out["faces"] and out.get("momentum_faces", True))
+    out.update({"workload": wl.name, "steps_after_initial_setup": steps, "initial_particles": int(n0),
+                "oracle_threads": nthreads,
+                "seconds": {"gpu_and_transfers": round(t_gpu, 1), "oracle": round(t_oracle, 1),
+                            "compare": round(time.perf_counter() - t2, 1)}})
+    return out
+
+
+def fp32_errors_full(ctx, wl, steps: int, sample: int, nthreads: int) -> dict:
+    """The precision form on the whole workload for `steps` steps, against the FP64 oracle.
+    Particles do not interact, so every particle's trajectory in the full run is its trajectory
+    alone: the per-particle errors are measured on the particles with PID < sample (an i.i.d.
+    sample of the seeded swarm, stepped by the oracle from the same initial state), and the grid
+    fields (face volume and momentum deposits, ParticleCount, P average) on a run of that sample
+    alone, whose per-particle values are checked to equal the full run's."""
     from dataclasses import replace
 
     from fdf_gb300.context import FORM_FP32, SwarmArrays
     from oracle import oracle as O
-    if wl.n > 2_000_000:    # the oracle steps the first 1M particles of the workload
-        pos_m, cell_m, _ = wl.sample(1_000_000)
-        wl = replace(wl, pos=pos_m, cell0=cell_m, seed_n=len(pos_m))
+    t0 = time.perf_counter()
+    mom = momentum_on(wl)
     ctx.load_workload(wl, form=FORM_FP32)
+    if mom:
+        ctx.set_momentum_deposit(True)
     ctx.initial_setup()
     ctx.steps(steps)
-    gpu = ctx.get_swarm().sorted_by_pid()
+    full = ctx.get_swarm()
+    keep = full.pid < sample
+    sub_full = SwarmArrays(*(getattr(full, f)[keep] for f in ("position", "velocity", "weight", "P", "cell", "pid",
+                                                               "status"))).sorted_by_pid()
+    n_full = int(full.n)
+    del full
+    pos_m, cell_m, _ = wl.sample(sample)
+    wl_s = replace(wl, pos=pos_m, cell0=cell_m, seed_n=len(pos_m))
+    ctx.load_workload(wl_s, form=FORM_FP32)
+    if mom:
+        ctx.set_momentum_deposit(True)
+    ctx.initial_setup()
+    ctx.steps(steps)
+    sub_run = ctx.get_swarm().sorted_by_pid()
     gfaces = ctx.get_faces()
+    gmom = ctx.get_face_momentum() if mom else None
     gcount, gavg = ctx.get_scattered()
+    same_as_full = all(bool(np.array_equal(getattr(sub_full, f), getattr(sub_run, f)))
+                       for f in ("position", "velocity", "weight", "P", "cell", "pid", "status"))
+    t_gpu = time.perf_counter() - t0
+    t1 = time.perf_counter()
     g = O.Grid(wl.coor)
-    s0 = SwarmArrays.create(wl.pos, cell=wl.cell0)
+    s0 = SwarmArrays.create(pos_m, cell=cell_m)
     os_ = O.Swarm(pos=s0.position, vel=s0.velocity, weight=s0.weight, P=s0.P, cell=s0.cell, pid=s0.pid,
                   status=s0.status, n=s0.n)
     sim = O.Simulation(g, wl.ucat_node_sized(), os_, wl.dt, nthreads=nthreads)
     sim.initial_setup()
     for _ in range(steps):
         sim.step()
+    t_oracle = time.perf_counter() - t1
     ref = os_.sorted_by_pid()
-    common, ia, ib = np.intersect1d(gpu.pid, ref["pid"], return_indices=True)
+    common, ia, ib = np.intersect1d(sub_run.pid, ref["pid"], return_indices=True)
 
     def stats(err):
         err = np.asarray(err, dtype=np.float64).ravel()
-        return {"max": float(err.max()) if err.size else 0.0, "rms": float(np.sqrt((err ** 2).mean())) if err.size else 0.0}
+        return {"max": float(err.max()) if err.size else 0.0,
+                "rms": float(np.sqrt((err ** 2).mean())) if err.size else 0.0}
 
-    umag = np.maximum(np.linalg.norm(ref["vel"][ib], axis=1, keepdims=True), 1e-30)
-    f = O.deposit_faces(g, os_, volume=wl.volume)
-    face_err = np.concatenate([np.abs(gf - f[k]).ravel() / wl.volume for gf, k in zip(gfaces, ("fi", "fj", "fk"))])
-    occupied = sim.count > 0
-    only_gpu = int(gpu.n - len(common))
-    only_ref = int(len(ref["pid"]) - len(common))
-    return {"steps": steps, "workload_particles": int(wl.n), "particles_compared": int(len(common)),
-            "gpu_particles": int(gpu.n),
-            "oracle_particles": int(len(ref["pid"])),
-            # a particle within ~1e-10 of a removal boundary (the box, or a k-face gap the walk
-            # cannot leave) can be removed by one side only; the grid fields then differ by it
-            "particles_removed_by_one_side_only": only_gpu + only_ref,
-            "same_cell_fraction": float(np.all(gpu.cell[ia] == ref["cell"][ib], axis=1).mean()),
-            "velocity_rel": stats(np.abs(gpu.velocity[ia] - ref["vel"][ib]) / umag),
-            "position_abs": stats(np.abs(gpu.position[ia] - ref["pos"][ib])),
-            "weight_abs": stats(np.abs(gpu.weight[ia] - ref["weight"][ib])),
-            "face_volume_abs_per_particle_volume": stats(face_err),
-            "count_abs": stats(np.abs(gcount - sim.count)),
-            "P_avg_rel": stats(np.abs(gavg[occupied] - sim.avg[occupied]) / np.abs(sim.avg[occupied]))}
+    # Particles whose FP32 trajectory (positions within ~1e-8 of the FP64 ones) crossed a cell face,
+    # a k-face gap or the box on a different side than the FP64 one: counted, and kept out of the
+    # per-particle statistics; the grid fields are compared away from the cells they touched.
+    same = np.all(sub_run.cell[ia] == ref["cell"][ib], axis=1)
+    ja, jb = ia[same], ib[same]
+    IM, JM, KM = wl.dims
+    touched = np.zeros((KM, JM, IM), bool)
+    for cells in (sub_run.cell[ia[~same]], ref["cell"][ib[~same]],
+                  sub_run.cell[np.setdiff1d(np.arange(len(sub_run.pid)), ia)],
+                  ref["cell"][np.setdiff1d(np.arange(len(ref["pid"])), ib)]):
+        cells = cells[np.all(cells >= 0, axis=1)]
+        touched[cells[:, 2], cells[:, 1], cells[:, 0]] = True
+    pad = np.pad(touched, 1)   # a face is touched when a cell on either side is
+    face_masks = (~(pad[1:-1, 1:-1, :-1] | pad[1:-1, 1:-1, 1:]), ~(pad[1:-1, :-1, 1:-1] | pad[1:-1, 1:, 1:-1]),
+                  ~(pad[:-1, 1:-1, 1:-1] | pad[1:, 1:-1, 1:-1]))
+    node_ok = np.ones(gcount.shape, bool)
+    node_ok[:KM, :JM, :IM] = ~touched
+    umag = np.maximum(np.linalg.norm(ref["vel"][jb], axis=1, keepdims=True), 1e-30)
+    f = O.deposit_faces(g, os_, volume=wl.volume, momentum=mom)
+    face_err = np.concatenate([(np.abs(a - f[k]) / wl.volume)[mk].ravel()
+                               for a, k, mk in zip(gfaces, ("fi", "fj", "fk"), face_masks)])
+    occupied = (sim.count > 0) & node_ok
+    out = {"workload": wl.name, "steps": steps, "full_run_particles": n_full, "sample_particles": int(len(pos_m)),
+           "sample": f"PID < {sample} (i.i.d. seeding): per-particle values from the full run; grid fields "
+                     f"from a run of the sample alone",
+           "sample_run_equals_full_run": same_as_full,
+           "particles_compared": int(len(common)),
+           "particles_removed_by_one_side_only": int(len(sub_run.pid) + len(ref["pid"]) - 2 * len(common)),
+           "particles_in_another_cell": int((~same).sum()),
+           "same_cell_fraction": float(same.mean()),
+           "statistics_over": "particles in the same cell on both sides; grid fields away from the cells of the "
+                              "particles counted above",
+           "velocity_rel": stats(np.abs(sub_run.velocity[ja] - ref["vel"][jb]) / umag),
+           "position_abs": stats(np.abs(sub_run.position[ja] - ref["pos"][jb])),
+           "weight_abs": stats(np.abs(sub_run.weight[ja] - ref["weight"][jb])),
+           "face_volume_abs_per_particle_volume": stats(face_err),
+           "count_abs": stats(np.abs(gcount - sim.count)[node_ok]),
+           "P_avg_rel": stats(np.abs(gavg[occupied] - sim.avg[occupied]) / np.abs(sim.avg[occupied])),
+           "oracle_threads": nthreads,
+           "seconds": {"gpu_and_transfers": round(t_gpu, 1), "oracle": round(t_oracle, 1)}}
+    if mom:
+        scale = np.abs(ref["vel"]).max() * wl.volume
+        out["face_momentum_abs_per_particle_momentum"] = stats(np.concatenate(
+            [(np.abs(a - f[k]) / scale)[mk].ravel() for a, k, mk in zip(gmom, ("mom_i", "mom_j", "mom_k"),
+                                                                         face_masks)]))
+    return out
 
 
 FP64_OPS_C2C = 21      # 3 face sums, 9 products, 6 sums, 3 scalings per interior cell
@@ -667,9 +818,20 @@ def run_gpu(args, rank, ws, local, dist):
                "in_place_route": {"value": v_ip, "ms_per_step": ms_ip, "transfer_gbs": gbs_ip},
                "host_link_gbs": link}
 
-    accuracy = None
-    if rank == 0 and ws == 1 and args.accuracy_steps > 0 and ("fp32" in forms or "learned_fp32" in forms):
-        accuracy = fp32_accuracy(ctx, wl, args.accuracy_steps, os.cpu_count() or 1)
+    # full-size checks against the FP64 oracle (all host cores): the plain form bit for bit on whole
+    # workloads, and the precision form's per-field errors
+    accuracy = fp32_cfg3 = None
+    parity = []
+    if rank == 0 and ws == 1:
+        nthreads = os.cpu_count() or 1
+        if args.parity_steps > 0:
+            for name in [args.workload] + [w for w in args.parity_workloads.split(",") if w and w != args.workload]:
+                parity.append(plain_parity_full(ctx, workload(name), args.parity_steps, nthreads))
+        if args.accuracy_steps > 0 and ("fp32" in forms or "learned_fp32" in forms):
+            accuracy = fp32_errors_full(ctx, wl, args.accuracy_steps, args.accuracy_sample, nthreads)
+        if args.cfg3_steps > 0:
+            fp32_cfg3 = fp32_errors_full(ctx, workload("sinusoidal96"), args.cfg3_steps, args.accuracy_sample,
+                                         nthreads)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -697,7 +859,11 @@ def run_gpu(args, rank, ws, local, dist):
                                  % (38 * 8 * Nc / 1e9, 2 * 93 * wl.n / 1e6),
                            "walk_evals_per_particle_step": evals / max(psteps, 1),
                            "deposits": "face volume" + (" and momentum" if momentum_on(wl) else "")},
-                "roofline": roofline, "forms": form_lines, "fp32_accuracy_vs_fp64_oracle": accuracy,
+                "roofline": roofline, "forms": form_lines,
+                "plain_vs_oracle_full": [{"config": c["workload"], "particles": c["initial_particles"],
+                                          "steps": c["steps_after_initial_setup"], "identical": c["identical"],
+                                          "detail": c} for c in parity] or None,
+                "fp32_accuracy_vs_fp64_oracle": accuracy, "fp32_errors_cfg3": fp32_cfg3,
                 "learned_vs_fp32_form": identity,
                 "cpu_baseline": cpu, "e2e": e2e, "contra2cart": c2c,
                 "gpu_launches": launches, "clocks": clk}
@@ -729,6 +895,14 @@ def main():
                     help="skip timing the Eulerian input (Contra2Cart on the workload's grid)")
     ap.add_argument("--accuracy-steps", type=int, default=10,
                     help="steps of the FP32-form vs FP64-oracle comparison on the full workload (0 = skip)")
+    ap.add_argument("--accuracy-sample", type=int, default=1_000_000,
+                    help="particles (the first PIDs, an i.i.d. sample) the oracle steps for the FP32-form errors")
+    ap.add_argument("--cfg3-steps", type=int, default=100,
+                    help="steps of the FP32-form errors on the 96x96x1536 sinusoidal grid, 16M particles (0 = skip)")
+    ap.add_argument("--parity-steps", type=int, default=2,
+                    help="steps after the initial setup of the plain-form full-size parity legs (0 = skip)")
+    ap.add_argument("--parity-workloads", default="sinusoidal96",
+                    help="workloads of the plain-form full-size parity legs besides the benchmarked one")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -40,6 +40,10 @@ _SIGS = {
     "fdf_ScatterAllParticleFieldsToEulerFields": (ctypes.c_int, [ctypes.c_void_p]),
     "fdf_LocatePoints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 5),
     "fdf_InterpolatePoints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3),
+    "fdf_ExtractParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, c_int64_p]
+                             + [ctypes.c_void_p] * 7),
+    "fdf_AddParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 7),
+    "fdf_DepositKFaceLayer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_Contra2CartDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTransferRoute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

@@ -320,6 +320,29 @@ class PicContext:
         self._check(self.lib.fdf_InterpolatePoints(self.h, len(cell), _ptr(cell), _ptr(weight), _ptr(vel)))
         return vel
 
+    # -- k-slab decomposition over several ranks (fdf_gb300/slabs.py)
+    def extract_particles(self, k_lo: int, k_hi: int) -> SwarmArrays:
+        """The held particles whose cell's k lies outside [k_lo, k_hi) leave the context."""
+        n_max = self.size()
+        out = SwarmArrays.empty(n_max)
+        got = ctypes.c_int64()
+        self._check(self.lib.fdf_ExtractParticles(self.h, int(k_lo), int(k_hi), n_max, ctypes.byref(got),
+                                                  _ptr(out.position), _ptr(out.velocity), _ptr(out.weight),
+                                                  _ptr(out.P), _ptr(out.cell), _ptr(out.pid), _ptr(out.status)))
+        return out.truncated(got.value)
+
+    def add_particles(self, s: SwarmArrays):
+        """Particles from another rank join the held swarm (their cells, weights, statuses kept)."""
+        arrs = [np.ascontiguousarray(a) for a in (s.position, s.velocity, s.weight, s.P, s.cell, s.pid, s.status)]
+        self._check(self.lib.fdf_AddParticles(self.h, s.n, *[_ptr(a) for a in arrs]))
+
+    def deposit_k_layer(self, k: int, seed: np.ndarray, seed_momentum: np.ndarray | None = None):
+        """The k-faces of layer k summed again from seed[j][i] (the lower cell's part), then the held
+        particles of layer k (plain form)."""
+        seed = np.ascontiguousarray(seed, dtype=np.float64)
+        sm = None if seed_momentum is None else np.ascontiguousarray(seed_momentum, dtype=np.float64)
+        self._check(self.lib.fdf_DepositKFaceLayer(self.h, int(k), _ptr(seed), _ptr(sm)))
+
     # -- the hot path
     def initial_setup(self) -> FdfStepInfo:
         info = FdfStepInfo()

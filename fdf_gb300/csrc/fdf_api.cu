@@ -906,6 +906,148 @@ int fdf_InterpolatePoints(FdfContext *ctx, int64_t n, const int64_t *cell, const
   return FDF_SUCCESS;
 }
 
+// ---- k-slab decomposition over several ranks (a driver that splits the swarm over GPUs) ----
+
+int fdf_ExtractParticles(FdfContext *ctx, int64_t k_lo, int64_t k_hi, int64_t n_max, int64_t *n_out,
+                         double *position, double *velocity, double *weight, double *P, int64_t *cell_id,
+                         int64_t *pid, int64_t *status) {
+  if (!ctx || !n_out) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_ExtractParticles: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_ExtractParticles: call fdf_SetGrid first");
+  if (k_lo < 0 || k_hi < k_lo || k_hi > ctx->g.KM)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_ExtractParticles: need 0 <= k_lo <= k_hi <= KM");
+  int r = ensure_layout(ctx);   // sorted by (cell, PID): the slab is one contiguous range
+  if (r) return r;
+  const GridDims &g = ctx->g;
+  const long long L = (long long)g.IM * g.JM;
+  unsigned int bound[3] = {0, 0, 0};
+  int n_held = 0;
+  cudaStream_t s = ctx->stream;
+  CU(cudaMemcpyAsync(&bound[0], ctx->cell_start + k_lo * L, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(&bound[1], ctx->cell_start + k_hi * L, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(&bound[2], ctx->cell_start + g.Nc, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(&n_held, &ctx->cnt->n_sorted, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  const int a = (int)bound[0], b = (int)bound[1], c = (int)bound[2], n = n_held;
+  const int64_t m = (int64_t)a + (c - b);   // cells below the slab, then above it
+  *n_out = m;
+  if (m > n_max) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_ExtractParticles: output arrays too small");
+  if (m == 0) return FDF_SUCCESS;
+  if (!position || !velocity || !weight || !P || !cell_id || !pid || !status)
+    return fail(ctx, FDF_ERR_ARG_NULL, "fdf_ExtractParticles: null field pointer");
+  const bool f32 = form_is32(ctx->swarm_form);
+  double *d_pos = (double *)ctx->staging, *d_vel = d_pos + 3 * m, *d_wgt = d_vel + 3 * m, *d_P = d_wgt + 3 * m;
+  long long *d_cell = (long long *)(d_P + m), *d_pid = d_cell + 3 * m, *d_st = d_pid + m;
+  const int ranges[2][2] = {{0, a}, {b, c}};
+  long long o = 0;
+  for (int q = 0; q < 2; ++q) {
+    const int r0 = ranges[q][0], cnt = ranges[q][1] - ranges[q][0];
+    if (cnt <= 0) continue;
+    const SwarmBuf src = shifted(ctx->buf[ctx->cur], r0);
+    if (f32)
+      launch_swarm_to_aos32(src, cnt, g, d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o,
+                            d_pid + o, d_st + o, s);
+    else
+      launch_swarm_to_aos(src, cnt, g, d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o,
+                          d_pid + o, d_st + o, s);
+    ctx->launches += 1;
+    o += cnt;
+  }
+  CHECK_LAUNCH();
+  CU(cudaMemcpyAsync(position, d_pos, 24ull * m, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(velocity, d_vel, 24ull * m, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(weight, d_wgt, 24ull * m, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(P, d_P, 8ull * m, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(cell_id, d_cell, 24ull * m, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(pid, d_pid, 8ull * m, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(status, d_st, 8ull * m, cudaMemcpyDeviceToHost, s));
+  // the rest stays, in its sorted order: the slab's cells, then the particles without a cell
+  launch_move_kept(ctx->buf[ctx->cur], ctx->buf[1 - ctx->cur], a, b, c, n, s);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  const int kept = n - (int)m;
+  CU(cudaMemcpyAsync(&ctx->cnt->n, &kept, sizeof(int), cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(&ctx->cnt->n_sorted, &kept, sizeof(int), cudaMemcpyHostToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  ctx->cur = 1 - ctx->cur;
+  ctx->layout_ok = false;   // cell_start no longer matches the held slots
+  ctx->gen++;
+  return FDF_SUCCESS;
+}
+
+int fdf_AddParticles(FdfContext *ctx, int64_t n, const double *position, const double *velocity,
+                     const double *weight, const double *P, const int64_t *cell_id, const int64_t *pid,
+                     const int64_t *status) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (n < 0) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_AddParticles: negative count");
+  if (n == 0) return FDF_SUCCESS;
+  if (!position || !velocity || !weight || !P || !cell_id || !pid || !status)
+    return fail(ctx, FDF_ERR_ARG_NULL, "fdf_AddParticles: null field pointer");
+  if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_AddParticles: no swarm (fdf_SetSwarm first)");
+  CU(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  int n_held = 0;
+  CU(cudaMemcpyAsync(&n_held, &ctx->cnt->n_sorted, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CU(cudaStreamSynchronize(s));
+  if ((long long)n_held + n > ctx->cap)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE,
+                "fdf_AddParticles: the swarm would exceed its capacity (fdf_ReserveParticles before fdf_SetSwarm)");
+  double *d_pos = (double *)ctx->staging, *d_vel = d_pos + 3 * n, *d_wgt = d_vel + 3 * n, *d_P = d_wgt + 3 * n;
+  long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
+  CU(cudaMemcpyAsync(d_pos, position, 24ull * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d_vel, velocity, 24ull * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d_wgt, weight, 24ull * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d_P, P, 8ull * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d_cell, cell_id, 24ull * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d_pid, pid, 8ull * n, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(d_st, status, 8ull * n, cudaMemcpyHostToDevice, s));
+  const SwarmBuf dst = shifted(ctx->buf[ctx->cur], n_held);
+  if (form_is32(ctx->swarm_form))
+    launch_swarm_from_aos32(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, dst, s);
+  else
+    launch_swarm_from_aos(d_pos, d_vel, d_wgt, d_P, d_cell, d_pid, d_st, (int)n, ctx->g, dst, s);
+  CHECK_LAUNCH();
+  ctx->launches += 1;
+  const int total = n_held + (int)n;
+  CU(cudaMemcpyAsync(&ctx->cnt->n, &total, sizeof(int), cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(&ctx->cnt->n_sorted, &total, sizeof(int), cudaMemcpyHostToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  ctx->layout_ok = false;
+  ctx->gen++;
+  return FDF_SUCCESS;
+}
+
+int fdf_DepositKFaceLayer(FdfContext *ctx, int64_t k, const double *seed, const double *seed_momentum) {
+  if (!ctx || !seed) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_DepositKFaceLayer: null argument");
+  if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_DepositKFaceLayer: call fdf_SetGrid first");
+  if (k < 0 || k > ctx->g.KM) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_DepositKFaceLayer: need 0 <= k <= KM");
+  if (ctx->out_form != FDF_FORM_PLAIN_FP64 || ctx->swarm_form != FDF_FORM_PLAIN_FP64)
+    return fail(ctx, FDF_ERR_SUP, "fdf_DepositKFaceLayer: the plain FP64 form's deposits only");
+  if (!ctx->layout_ok)
+    return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_DepositKFaceLayer: deposit the held particles first");
+  CU(cudaSetDevice(ctx->device));
+  const GridDims &g = ctx->g;
+  const long long L = (long long)g.IM * g.JM;
+  const bool mom = ctx->out_momentum && ctx->mom;
+  double *d = nullptr;
+  CU(cudaMalloc((void **)&d, 8ull * L * 4));
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(d, seed, 8ull * L, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = seed_momentum ? cudaMemcpyAsync(d + L, seed_momentum, 24ull * L, cudaMemcpyHostToDevice, s)
+                      : cudaMemsetAsync(d + L, 0, 24ull * L, s);
+  const long long nfi = (g.IM + 1LL) * g.JM * g.KM, nfj = g.IM * (g.JM + 1LL) * g.KM;
+  if (e == cudaSuccess) {
+    launch_deposit_k_layer(ctx->buf[ctx->cur], g, ctx->cell_start, (int)k, ctx->volume, d, d + L, ctx->fk,
+                           mom ? ctx->mom + 3 * (nfi + nfj) : nullptr, s);
+    ctx->launches += 1;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_DepositKFaceLayer: ") + cudaGetErrorString(e));
+  return FDF_SUCCESS;
+}
+
 int fdf_PerformInitialSetup(FdfContext *ctx, FdfStepInfo *info) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   FdfStepInfo local{};

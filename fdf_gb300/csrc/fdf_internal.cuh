@@ -145,6 +145,11 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_ORDER_MIN_BLOCKS
 #define FDF_ORDER_MIN_BLOCKS 8
 #endif
+// Table rows a block of the FP32 locate kernel stages in shared memory (the range of its
+// particles' previous cells; 0: no staging).
+#ifndef FDF_STAGE_ROWS
+#define FDF_STAGE_ROWS 0
+#endif
 // Resident 256-thread blocks per SM the learned form's guess and fallback walks are compiled for.
 #ifndef FDF_GUESS_MIN_BLOCKS
 #define FDF_GUESS_MIN_BLOCKS 3
@@ -156,6 +161,11 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #endif
 
 // ---------------------------------------------------------------- kernels (launchers)
+// Compaction of the held swarm to slots [a, b) and [c, n) of src, in that order (fdf_ExtractParticles).
+void launch_move_kept(const SwarmBuf &src, const SwarmBuf &dst, int a, int b, int c, int n, cudaStream_t s);
+// The plain form's k-faces of layer k summed again from seeds (fdf_DepositKFaceLayer).
+void launch_deposit_k_layer(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, int k, double volume,
+                            const double *seed, const double *seed_mom, double *fk, double *mk, cudaStream_t s);
 // Adds the pending block flushes to the counters and clears them (end of a pipeline run).
 void launch_fold_counts(DevCounters *cnt, cudaStream_t s);
 void launch_build_planes(const double *coor_aos, GridDims g, double *planes, unsigned int *err, cudaStream_t s);

@@ -324,6 +324,60 @@ __global__ void __launch_bounds__(DEPM_WARPS * 32) k_deposit_mom_staged(SwarmBuf
   if (face_k) store(2, fk, mk, nfk, c);
 }
 
+// Slot t of dst takes slot a + t of src for t < b - a, and slot c + (t - (b - a)) after that: the
+// held particles of a k-slab ([a, b) in the cell-sorted order) followed by those without a cell
+// ([c, n)); every field of both forms moves.
+__global__ void k_move_kept(SwarmBuf src, SwarmBuf dst, int a, int b, int c, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = (b - a) + (n - c);
+  if (t >= m) return;
+  const int p = t < b - a ? a + t : c + (t - (b - a));
+  dst.x[t] = src.x[p]; dst.y[t] = src.y[p]; dst.z[t] = src.z[p];
+  dst.u[t] = src.u[p]; dst.v[t] = src.v[p]; dst.w[t] = src.w[p];
+  dst.a1[t] = src.a1[p]; dst.a2[t] = src.a2[p]; dst.a3[t] = src.a3[p];
+  dst.P[t] = src.P[p];
+  dst.uf[t] = src.uf[p]; dst.vf[t] = src.vf[p]; dst.wf[t] = src.wf[p];
+  dst.a1f[t] = src.a1f[p]; dst.a2f[t] = src.a2f[p]; dst.a3f[t] = src.a3f[p];
+  dst.Pf[t] = src.Pf[p];
+  dst.pid[t] = src.pid[p];
+  dst.cell[t] = src.cell[p];
+  dst.status[t] = src.status[p];
+}
+
+// The k-faces of layer k (between cells k - 1 and k) summed again from seed values: seed[j][i]
+// stands for the lower cell's part of the sum (0.0 + its particles' a V/3 in (cell, PID) order,
+// made where the lower cell's particles are held), and the held particles of cell (i, j, k) add
+// their (1 - a) V/3 (and its products with the velocity) after it, in sorted order -- the
+// single-rank sum, operation for operation.  Momentum seeds are [j][i][3].
+__global__ void k_deposit_k_layer(SwarmBuf b, GridDims g, const unsigned int *__restrict__ cs, int k, double third,
+                                  const double *__restrict__ seed, const double *__restrict__ seed_mom,
+                                  double *__restrict__ fk, double *__restrict__ mk) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;   // (j, i) of the layer
+  const long long L = (long long)g.IM * g.JM;
+  if (q >= L) return;
+  const long long f = (long long)k * L + q;
+  double acc = seed[q];
+  double m0 = 0.0, m1 = 0.0, m2 = 0.0;
+  if (mk) { m0 = seed_mom[3 * q]; m1 = seed_mom[3 * q + 1]; m2 = seed_mom[3 * q + 2]; }
+  if (k < g.KM) {
+    const unsigned int s0 = __ldg(cs + f), s1 = __ldg(cs + f + 1);
+    for (unsigned int s = s0; s < s1; ++s) {
+      const double x = mul(sub(1.0, __ldg(b.a3 + s)), third);
+      acc = add(acc, x);
+      if (mk) {
+        m0 = add(m0, mul(x, __ldg(b.u + s)));
+        m1 = add(m1, mul(x, __ldg(b.v + s)));
+        m2 = add(m2, mul(x, __ldg(b.w + s)));
+      }
+    }
+  }
+  fk[f] = acc;
+  if (mk) {
+    const long long nfk = L * (g.KM + 1LL);
+    mk[f] = m0; mk[nfk + f] = m1; mk[2 * nfk + f] = m2;
+  }
+}
+
 __global__ void k_from_aos(const double *__restrict__ pos, const double *__restrict__ vel,
                            const double *__restrict__ wgt, const double *__restrict__ P,
                            const long long *__restrict__ cell3, const long long *__restrict__ pid,
@@ -412,6 +466,19 @@ void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_star
   else
     k_deposit_staged<<<(unsigned)((g.Nn + DEP_WARPS * 32 - 1) / (DEP_WARPS * 32)), DEP_WARPS * 32, 0, s>>>(
         b, g, cell_start, third, count, avg, fi, fj, fk);
+}
+
+void launch_move_kept(const SwarmBuf &src, const SwarmBuf &dst, int a, int b, int c, int n, cudaStream_t s) {
+  const int m = (b - a) + (n - c);
+  if (m <= 0) return;
+  k_move_kept<<<(m + 255) / 256, 256, 0, s>>>(src, dst, a, b, c, n);
+}
+
+void launch_deposit_k_layer(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, int k, double volume,
+                            const double *seed, const double *seed_mom, double *fk, double *mk, cudaStream_t s) {
+  const long long L = (long long)g.IM * g.JM;
+  k_deposit_k_layer<<<(unsigned)((L + 255) / 256), 256, 0, s>>>(b, g, cell_start, k, volume / 3.0, seed, seed_mom, fk,
+                                                                 mk);
 }
 
 void launch_swarm_from_aos(const double *pos, const double *vel, const double *wgt, const double *P,

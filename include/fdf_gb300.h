@@ -223,6 +223,28 @@ int fdf_LocatePoints(FdfContext *ctx, int64_t n, const double *position, const i
  * The corner field is made from the context's ucat (every node).  Host arrays. */
 int fdf_InterpolatePoints(FdfContext *ctx, int64_t n, const int64_t *cell, const double *weight, double *velocity);
 
+/* ---- k-slab decomposition over several GPUs (fdf_gb300/slabs.py drives these) ----
+ * The reference distributes particles over MPI ranks with DMSwarmMigrate
+ * (ParticleMotion.c:1931-2135, the walk-and-handoff passes).  Here each rank holds the whole grid
+ * and the particles whose cell lies in its k-slab of cells; after the walk the particles that
+ * left the slab move to their slab's rank, and the k-faces between two slabs are summed by the
+ * upper rank from the lower rank's partial sums, so the ranks' results together are the one-rank
+ * results bit for bit (plain form). */
+/* The held particles whose cell has k outside [k_lo, k_hi) leave the context into the host arrays
+ * (DMSwarm layout, in (cell, PID) order: cells below the slab, then above); particles without a
+ * cell stay.  *n = the number extracted (FDF_ERR_ARG_OUTOFRANGE, nothing moved, if > n_max). */
+int fdf_ExtractParticles(FdfContext *ctx, int64_t k_lo, int64_t k_hi, int64_t n_max, int64_t *n, double *position,
+                         double *velocity, double *weight, double *P, int64_t *cell_id, int64_t *pid, int64_t *status);
+/* Particles from another rank join the held swarm with their cells, weights and statuses (the
+ * capacity reserved before fdf_SetSwarm must hold them). */
+int fdf_AddParticles(FdfContext *ctx, int64_t n, const double *position, const double *velocity, const double *weight,
+                     const double *P, const int64_t *cell_id, const int64_t *pid, const int64_t *status);
+/* The plain form's k-faces of layer k (between cells k-1 and k) after a deposit, summed again as
+ * seed[j][i] (the lower cell's part, made by the rank holding it: that rank's own values of this
+ * layer) followed by the held particles of cells (i, j, k), in the deposit's order; momentum seeds
+ * [j][i][3] (NULL: zero) when the momentum deposit is on.  FDF_ERR_SUP in the precision forms. */
+int fdf_DepositKFaceLayer(FdfContext *ctx, int64_t k, const double *seed, const double *seed_momentum);
+
 /* ---- sort by cell (the per-step re-sort of the hot path, as a standalone call) ---- */
 /* Stable counting sort of n particle slots by cell id, all pointers on the device.
  * Slots whose id is negative or >= ncells get no place.  On return cell_start[c] is the

@@ -421,72 +421,105 @@ void o_ScatterParticleFieldToEulerField_P(const OGrid *g, const OSwarm *s, doubl
   free(sum);
 }
 
-typedef struct { int64_t cell, pid, idx; } OKey;
-
-static int o_key_cmp(const void *a, const void *b) {
-  const OKey *x = (const OKey *)a, *y = (const OKey *)b;
-  if (x->cell != y->cell) return x->cell < y->cell ? -1 : 1;
-  if (x->pid != y->pid) return x->pid < y->pid ? -1 : 1;
-  return (x->idx > y->idx) - (x->idx < y->idx);
-}
-
 /* The face deposit is defined with a fixed summation order: particles in
  * ascending (linear cell id i + IM*(j + JM*k), PID) order, each face summing its
  * contributions in that order from a starting 0.0.  A face's lower cell precedes
  * its upper cell in that order, so every face adds its lower cell's particles
  * (weight a) first and its upper cell's (weight 1-a) second. */
+/* The (cell, PID) order of the particles with a cell: a counting sort by cell (start[c] ..
+ * start[c + 1] are cell c's entries of idx), each cell's entries then in ascending PID (and slot).
+ * Returns the number of particles placed, or -1 when out of memory. */
+static int64_t o_cell_order(const OGrid *g, const OSwarm *s, int64_t *start, int64_t *idx) {
+  const int64_t IM = g->IM, JM = g->JM, KM = g->KM, Nc = IM * JM * KM;
+  for (int64_t c = 0; c <= Nc; c++) start[c] = 0;
+  for (int64_t p = 0; p < s->n; p++) {
+    int64_t i = s->cell[3 * p], j = s->cell[3 * p + 1], k = s->cell[3 * p + 2];
+    if (i < 0 || i >= IM || j < 0 || j >= JM || k < 0 || k >= KM) continue;
+    start[(k * JM + j) * IM + i + 1]++;
+  }
+  for (int64_t c = 0; c < Nc; c++) start[c + 1] += start[c];
+  int64_t *fill = (int64_t *)malloc((size_t)(Nc > 0 ? Nc : 1) * sizeof(int64_t));
+  if (!fill) return -1;
+  memcpy(fill, start, (size_t)Nc * sizeof(int64_t));
+  for (int64_t p = 0; p < s->n; p++) {   /* ascending slot within each cell */
+    int64_t i = s->cell[3 * p], j = s->cell[3 * p + 1], k = s->cell[3 * p + 2];
+    if (i < 0 || i >= IM || j < 0 || j >= JM || k < 0 || k >= KM) continue;
+    idx[fill[(k * JM + j) * IM + i]++] = p;
+  }
+  free(fill);
+  const int64_t *pid = s->pid;
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t c = 0; c < Nc; c++) {     /* then ascending PID (insertion sort: a few per cell) */
+    for (int64_t a = start[c] + 1; a < start[c + 1]; a++) {
+      const int64_t v = idx[a];
+      int64_t b = a - 1;
+      while (b >= start[c] && pid[idx[b]] > pid[v]) { idx[b + 1] = idx[b]; b--; }
+      idx[b + 1] = v;
+    }
+  }
+  return start[Nc];
+}
+
+/* One face's sum in the deposit's order: its lower cell's particles (weight a, the upper-face
+ * fraction a * V/3) from 0.0, then its upper cell's (the lower-face fraction (1 - a) * V/3);
+ * a side outside the grid contributes nothing.  comp: the weight component (0 i, 1 j, 2 k). */
+static void o_face_sum(const OSwarm *s, const int64_t *start, const int64_t *idx, int64_t lower, int64_t upper,
+                       int comp, double third, double *vol, double *mom3, double *absum) {
+  double v = 0.0, ab = 0.0, m0 = 0.0, m1 = 0.0, m2 = 0.0;
+  for (int side = 0; side < 2; side++) {
+    const int64_t c = side == 0 ? lower : upper;
+    if (c < 0) continue;
+    for (int64_t q = start[c]; q < start[c + 1]; q++) {
+      const int64_t p = idx[q];
+      const double a = s->weight[3 * p + comp];
+      const double frac = side == 0 ? a * third : (1.0 - a) * third;
+      v += frac;
+      ab += fabs(frac);
+      if (mom3) {
+        const double *u = &s->vel[3 * p];
+        m0 += frac * u[0]; m1 += frac * u[1]; m2 += frac * u[2];
+      }
+    }
+  }
+  *vol = v;
+  if (absum) *absum = ab;
+  if (mom3) { mom3[0] = m0; mom3[1] = m1; mom3[2] = m2; }
+}
+
 void o_DepositParticlesToFaces(const OGrid *g, const OSwarm *s, double volume,
                                double *fi, double *fj, double *fk,
                                double *mom_i, double *mom_j, double *mom_k,
                                double *abs_i, double *abs_j, double *abs_k) {
-  const int64_t IM = g->IM, JM = g->JM, KM = g->KM;
-  const int64_t nfi = (IM + 1) * JM * KM, nfj = IM * (JM + 1) * KM, nfk = IM * JM * (KM + 1);
-  memset(fi, 0, (size_t)nfi * sizeof(double));
-  memset(fj, 0, (size_t)nfj * sizeof(double));
-  memset(fk, 0, (size_t)nfk * sizeof(double));
-  if (mom_i) { memset(mom_i, 0, (size_t)nfi * 3 * sizeof(double)); }
-  if (mom_j) { memset(mom_j, 0, (size_t)nfj * 3 * sizeof(double)); }
-  if (mom_k) { memset(mom_k, 0, (size_t)nfk * 3 * sizeof(double)); }
-  if (abs_i) memset(abs_i, 0, (size_t)nfi * sizeof(double));
-  if (abs_j) memset(abs_j, 0, (size_t)nfj * sizeof(double));
-  if (abs_k) memset(abs_k, 0, (size_t)nfk * sizeof(double));
+  const int64_t IM = g->IM, JM = g->JM, KM = g->KM, Nc = IM * JM * KM;
   const double third = volume / 3.0;
-  OKey *order = (OKey *)malloc((size_t)(s->n > 0 ? s->n : 1) * sizeof(OKey));
-  int64_t m = 0;
-  for (int64_t p = 0; p < s->n; p++) {
-    int64_t i = s->cell[3 * p], j = s->cell[3 * p + 1], k = s->cell[3 * p + 2];
-    if (i < 0 || i >= IM || j < 0 || j >= JM || k < 0 || k >= KM) continue;
-    order[m].cell = (k * JM + j) * IM + i; order[m].pid = s->pid[p]; order[m].idx = p; m++;
+  int64_t *start = (int64_t *)malloc((size_t)(Nc + 1) * sizeof(int64_t));
+  int64_t *idx = (int64_t *)malloc((size_t)(s->n > 0 ? s->n : 1) * sizeof(int64_t));
+  if (!start || !idx || o_cell_order(g, s, start, idx) < 0) { free(start); free(idx); return; }
+  /* i-face (i, j, k): cells (i-1, j, k) and (i, j, k) */
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < (IM + 1) * JM * KM; f++) {
+    const int64_t i = f % (IM + 1), jk = f / (IM + 1);
+    const int64_t c = jk * IM + i;
+    o_face_sum(s, start, idx, i > 0 ? c - 1 : -1, i < IM ? c : -1, 0, third, &fi[f], mom_i ? &mom_i[3 * f] : NULL,
+               abs_i ? &abs_i[f] : NULL);
   }
-  qsort(order, (size_t)m, sizeof(OKey), o_key_cmp);
-  for (int64_t q = 0; q < m; q++) {
-    const int64_t p = order[q].idx;
-    int64_t i = s->cell[3 * p], j = s->cell[3 * p + 1], k = s->cell[3 * p + 2];
-    const double *a = &s->weight[3 * p];
-    const double *u = &s->vel[3 * p];
-    int64_t fidx[6];
-    double frac[6];
-    fidx[0] = (k * JM + j) * (IM + 1) + i;       frac[0] = (1.0 - a[0]) * third;
-    fidx[1] = fidx[0] + 1;                         frac[1] = a[0] * third;
-    fidx[2] = (k * (JM + 1) + j) * IM + i;        frac[2] = (1.0 - a[1]) * third;
-    fidx[3] = fidx[2] + IM;                        frac[3] = a[1] * third;
-    fidx[4] = (k * JM + j) * IM + i;              frac[4] = (1.0 - a[2]) * third;
-    fidx[5] = fidx[4] + IM * JM;                   frac[5] = a[2] * third;
-    double *vol[3] = {fi, fj, fk};
-    double *mom[3] = {mom_i, mom_j, mom_k};
-    double *ab[3] = {abs_i, abs_j, abs_k};
-    for (int f = 0; f < 6; f++) {
-      int fam = f >> 1;
-      vol[fam][fidx[f]] += frac[f];
-      if (ab[fam]) ab[fam][fidx[f]] += fabs(frac[f]);
-      if (mom[fam]) {
-        mom[fam][3 * fidx[f] + 0] += frac[f] * u[0];
-        mom[fam][3 * fidx[f] + 1] += frac[f] * u[1];
-        mom[fam][3 * fidx[f] + 2] += frac[f] * u[2];
-      }
-    }
+  /* j-face (i, j, k): cells (i, j-1, k) and (i, j, k) */
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < IM * (JM + 1) * KM; f++) {
+    const int64_t i = f % IM, j = (f / IM) % (JM + 1), k = f / (IM * (JM + 1));
+    const int64_t c = (k * JM + j) * IM + i;
+    o_face_sum(s, start, idx, j > 0 ? c - IM : -1, j < JM ? c : -1, 1, third, &fj[f], mom_j ? &mom_j[3 * f] : NULL,
+               abs_j ? &abs_j[f] : NULL);
   }
-  free(order);
+  /* k-face (i, j, k): cells (i, j, k-1) and (i, j, k) */
+#pragma omp parallel for schedule(static)
+  for (int64_t f = 0; f < IM * JM * (KM + 1); f++) {
+    const int64_t k = f / (IM * JM);
+    o_face_sum(s, start, idx, k > 0 ? f - IM * JM : -1, k < KM ? f : -1, 2, third, &fk[f],
+               mom_k ? &mom_k[3 * f] : NULL, abs_k ? &abs_k[f] : NULL);
+  }
+  free(start);
+  free(idx);
 }
 
 /* simulation.c:240-311 (one step, one rank, steady ucat). */
