@@ -270,7 +270,9 @@ def run_reference(args, rank):
 
 FORMS = {"plain_fp64": 0, "fp32": 1, "learned_fp32": 2}
 FORM_DTYPE = {"plain_fp64": "f64", "fp32": "f32 (positions and walk decisions f64)",
-              "learned_fp32": "f32 (positions and walk decisions f64; bf16 MLP, f32 accumulate)"}
+              "learned_fp32": "f32 (positions and walk decisions f64; MLP trained in bf16, inference {} "
+                              "operands, f32 accumulate)"}
+LOCATOR_TYPES = {"bf16": 0, "f16": 1}
 MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, one inference
 
 # DRAM bytes (read + write) per launch of a stage's kernels, measured by ncu
@@ -315,6 +317,7 @@ def prepare(ctx, wl, form, args):
         return
     if args.guess_min_cells is not None:
         ctx.locator_min_distance(args.guess_min_cells)
+    ctx.locator_inference_type(LOCATOR_TYPES[args.locator_type])
     if wl.name not in _TRAINED:
         import torch
         torch.cuda.synchronize()
@@ -420,10 +423,10 @@ def time_form(ctx, wl, form, args, dist, local, with_clocks):
         mlp_ms = per.get("learned_guess", 0.0)
         tfl = MLP_FLOPS * asked / K / (mlp_ms / 1000.0) / 1e12 if mlp_ms > 0 else None
         learned = {"guesses_per_step": asked / K, "guess_fraction": asked / max(psteps, 1),
-                   "guesses_kept": taken / max(asked, 1), "guess_walk_evals_per_guess": gev / max(asked, 1),
-                   "fallback_evals_per_guess": fev / max(asked, 1),
+                   "walk_evals_from_P1_per_guess": gev / max(asked, 1),
+                   "evals_after_P1_on_predicted_path": taken / max(gev - asked, 1),
                    "mlp_tflops": tfl, "mlp_flops_per_particle": MLP_FLOPS,
-                   "training": _TRAINED[wl.name][1]}
+                   "inference_operands": args.locator_type, "training": _TRAINED[wl.name][1]}
     traffic = {k: stage_traffic(wl, form, k, n_avg, asked / K) for k in per}
     return dict(form=form, psteps=psteps, evals=evals, ms=ms_max, launches=launches, clocks=clk, per=per, alg=alg,
                 learned=learned, traffic=traffic,
@@ -848,7 +851,7 @@ def run_gpu(args, rank, ws, local, dist):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": FORM_DTYPE[forms[0]], "data": "synthetic",
+                "scaling": "weak", "vs_baseline": None, "dtype": FORM_DTYPE[forms[0]].format(args.locator_type), "data": "synthetic",
                 "config": {"workload": wl.name, "form": forms[0], "grid": f"{IM}x{JM}x{KM}",
                            "particles": wl.n, "cfl": wl.meta.get("cfl"), "dt": wl.dt,
                            "parallelism": "replicas" if ws > 1 else "single",
@@ -884,6 +887,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=16000)
     ap.add_argument("--train-batch", type=int, default=8192)
     ap.add_argument("--train-lr", type=float, default=2e-3)
+    ap.add_argument("--locator-type", default="bf16", choices=sorted(LOCATOR_TYPES),
+                    help="learned form: operand type of the network's tensor-core inference")
     ap.add_argument("--guess-min-cells", type=float, default=None,
                     help="learned form: particles at least this many cells past their cell get a guess")
     ap.add_argument("--identity-steps", type=int, default=3,

@@ -88,6 +88,7 @@ _SIGS = {
                                           ctypes.c_void_p]),
     "fdf_LocatorGetStats": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p, c_int64_p]),
     "fdf_LocatorSetMinDistance": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "fdf_LocatorSetInferenceType": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_ReadGridFile": (ctypes.c_int, [ctypes.c_char_p, c_int64_p, c_int64_p, c_int64_p, ctypes.c_void_p,
                                         ctypes.c_int64]),
     "fdf_WriteGridFile": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,

@@ -24,6 +24,7 @@ ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG"
 NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
 FORM_PLAIN_FP64, FORM_FP32, FORM_LEARNED_FP32 = 0, 1, 2
 TRANSFER_STAGED, TRANSFER_IN_PLACE = 0, 1
+LOCATOR_BF16, LOCATOR_F16 = 0, 1
 LOCATOR_NPARAM = 33923
 
 
@@ -433,13 +434,17 @@ class PicContext:
         self._check(self.lib.fdf_LocatorPredict(self.h, _ptr(p), len(p), _ptr(cells), _ptr(out)))
         return cells, out
 
+    def locator_inference_type(self, kind: int):
+        """Inference operands: LOCATOR_BF16 (default) or LOCATOR_F16."""
+        self._check(self.lib.fdf_LocatorSetInferenceType(self.h, int(kind)))
+
     def locator_min_distance(self, cells: float):
         """Particles at least `cells` cells past their previous cell get a network guess."""
         self._check(self.lib.fdf_LocatorSetMinDistance(self.h, float(cells)))
 
     def locator_stats(self) -> tuple[int, int, int, int]:
-        """(particles given a guess, guesses kept, evaluations of the walks from the guesses,
-        evaluations of the reference walks that finished the guesses not kept)."""
+        """(particles given a prediction, evaluations of their walks from P1 on the predicted path,
+        evaluations of those walks, 0)."""
         a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         self._check(self.lib.fdf_LocatorGetStats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
                                                  ctypes.byref(d)))

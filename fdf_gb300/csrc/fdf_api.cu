@@ -528,10 +528,10 @@ int fdf_GetFaceDeposits(FdfContext *ctx, double *fi, double *fj, double *fk) {
 namespace {
 
 // Kernels one pipeline run launches: locate, 3 scan kernels, corner, slots, order, gather,
-// deposit; the learned form adds the flag scan (3), the compaction, the network, the walk
-// from the guess and the fallback walk.
+// deposit; the learned form adds the flag scan (3), the compaction, the network and the walk
+// from P1.
 long long launches_per_step(const FdfContext *ctx) {
-  return 10 + (ctx->swarm_form == FDF_FORM_LEARNED_FP32 ? 7 : 0);
+  return 10 + (ctx->swarm_form == FDF_FORM_LEARNED_FP32 ? 6 : 0);
 }
 
 // The shared pipeline of the initial setup (advect=0, drop=0) and a step (1, 1); locate_only:
@@ -563,8 +563,9 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
   const bool learned = ctx->swarm_form == FDF_FORM_LEARNED_FP32;
   size_t e0 = prof ? record_event(ctx, s) : 0, eg0 = 0, eg1 = 0;
   if (learned) {
-    // one evaluation in the previous cell; the particles that left it get a learned
-    // start cell and walk from there (k_locate32_guess)
+    // one evaluation in the previous cell; the particles that left it for a cell at least
+    // far_cells away get a learned guess, and the reference walk from P1 (k_locate32_path)
+    // fetches the rows of the path toward the guess ahead of its evaluations
     LocatorState &L = ctx->loc;
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
                     ctx->cnt, ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, L.pflag, L.far_cells, s);
@@ -572,11 +573,11 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
     exclusive_scan_u32(L.pflag + nw, nw + 1, L.scan_sums, s);
     launch_compact_pending(L.pflag, ctx->cap, L.pending, ctx->cnt, s);
     eg0 = prof ? record_event(ctx, s) : 0;
-    mlp_guess_tc(L.tc_img, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0, ctx->cap, g,
-                 L.guess, ctx->num_sms, &ctx->cnt->err, s);
+    mlp_guess_tc(L.tc_img, L.infer_bf16, L.bias, L.norm, src.x, src.y, src.z, 1, L.pending, &ctx->cnt->pending, 0,
+                 ctx->cap, g, L.guess, ctx->num_sms, &ctx->cnt->err, s);
     eg1 = prof ? record_event(ctx, s) : 0;
-    launch_locate32_guess(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
-                          ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
+    launch_locate32_path(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->bbox, ctx->fbox, drop, ctx->cnt,
+                         ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, L.pending, L.guess, ctx->num_sms, s);
   } else if (f32) {
     launch_locate32(src, ctx->cap, g, ctx->table32, ctx->planes, ctx->dt, advect, ctx->bbox, ctx->fbox, drop,
                     ctx->cnt, ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, nullptr, 0.f, s);

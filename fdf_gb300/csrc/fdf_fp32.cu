@@ -22,62 +22,6 @@ using fdfx::add;
 using fdfx::mul;
 using fdfx::sub;
 
-// Overlap margin of cell c (FP64): an upper bound on |d_f(p) - d'(p)| over the six faces f
-// of the cell, every plane P' of the same grid surface on the 3x3 patches around face f
-// (the same face of the in-surface neighbours and the opposite face of the cells across
-// those patches, oriented like f), for p within R = 2.2 max_v |v - centroid| of the face
-// centroid:  |(fc - fc') . n'| + R |n - n'|,  plus twice the largest distance threshold
-// involved.  A point whose six distances all exceed thr + margin lies on the negative side
-// of one face, by more than its threshold, of each of the 26 neighbouring cells.
-// Degenerate rows in the neighbourhood give an infinite margin.
-__device__ double cell_margin(const double *__restrict__ planes, const double *__restrict__ coor, GridDims g, int i,
-                              int j, int k) {
-  double cen[3] = {0.0, 0.0, 0.0}, v[8][3];
-  for (int q = 0; q < 8; ++q) {
-    const long long node = ((long long)(k + (q >> 2)) * (g.JM + 1) + (j + ((q >> 1) & 1))) * (long long)(g.IM + 1) +
-                           (i + (q & 1));
-    for (int d = 0; d < 3; ++d) { v[q][d] = coor[3 * node + d]; cen[d] += v[q][d]; }
-  }
-  double rv = 0.0;
-  for (int q = 0; q < 8; ++q) {
-    const double dx = v[q][0] - cen[0] / 8.0, dy = v[q][1] - cen[1] / 8.0, dz = v[q][2] - cen[2] / 8.0;
-    rv = fmax(rv, sqrt(dx * dx + dy * dy + dz * dz));
-  }
-  const double R = 2.2 * rv;
-  const long long c = ((long long)k * g.JM + j) * g.IM + i;
-  const int idx[3] = {i, j, k}, dims[3] = {g.IM, g.JM, g.KM};
-  // face -> (axis, upper side), partner face
-  const int axis[6] = {0, 0, 1, 1, 2, 2};
-  const int upper[6] = {0, 1, 0, 1, 1, 0};           // LEFT, RIGHT, BOTTOM, TOP, FRONT (k+1), BACK (k)
-  const int partner[6] = {F_RIGHT, F_LEFT, F_TOP, F_BOTTOM, F_BACK, F_FRONT};
-  double worst = 0.0, thr_max = planes[c * FDF_ROW + 36];
-  for (int f = 0; f < 6; ++f) {
-    const double *pf = planes + c * FDF_ROW + 6 * f;
-    const int a = axis[f], b1 = (a + 1) % 3, b2 = (a + 2) % 3;
-    for (int side = 0; side < 2; ++side) {           // 0: same face of in-surface neighbours, 1: across
-      const int da = side == 0 ? 0 : (upper[f] ? 1 : -1);
-      const int face = side == 0 ? f : partner[f];
-      const double sg = side == 0 ? 1.0 : -1.0;
-      for (int o1 = -1; o1 <= 1; ++o1)
-        for (int o2 = -1; o2 <= 1; ++o2) {
-          int n[3] = {idx[0], idx[1], idx[2]};
-          n[a] += da; n[b1] += o1; n[b2] += o2;
-          if (n[0] < 0 || n[0] >= dims[0] || n[1] < 0 || n[1] >= dims[1] || n[2] < 0 || n[2] >= dims[2]) continue;
-          const long long cn = ((long long)n[2] * g.JM + n[1]) * g.IM + n[0];
-          const double *rn = planes + cn * FDF_ROW;
-          if (fdfx::ubits(rn[37]) != 0ULL) return INFINITY;
-          thr_max = fmax(thr_max, rn[36]);
-          const double *q = rn + 6 * face;
-          const double nx = sg * q[3], ny = sg * q[4], nz = sg * q[5];
-          const double off = fabs((pf[0] - q[0]) * nx + (pf[1] - q[1]) * ny + (pf[2] - q[2]) * nz);
-          const double dnx = pf[3] - nx, dny = pf[4] - ny, dnz = pf[5] - nz;
-          worst = fmax(worst, off + R * sqrt(dnx * dnx + dny * dny + dnz * dnz));
-        }
-    }
-  }
-  return worst * (1.0 + 1e-6) + 2.0 * thr_max + 1e-12 * R;
-}
-
 __global__ void k_build_table32(const double *__restrict__ planes, const double *__restrict__ coor, GridDims g,
                                 float *__restrict__ table) {
   const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -101,7 +45,7 @@ __global__ void k_build_table32(const double *__restrict__ planes, const double 
   float thr32 = __double2float_ru(mul(thr, 1.0 + 0x1p-22));
   if (fdfx::ubits(row[37]) != 0ULL) thr32 = -fabsf(thr32) - 1.0f;
   t[3] = thr32;
-  t[7] = __double2float_ru(cell_margin(planes, coor, g, i, j, k));
+  t[7] = 0.0f;
   for (int f = 0; f < 6; ++f) {
     const double *p = row + 6 * f;
     float *o = t + 8 + 6 * f;
@@ -200,9 +144,10 @@ __device__ __forceinline__ float beyond_cells(const float (&dv)[6]) {
 //   FIRST == true:  the reference's first evaluation, in the previous cell; a particle that it
 //                   does not conclude and that lies at least far_cells past that cell is
 //                   marked in `pending` (per warp of slots: a bit mask [W] and its count
-//                   [W + 1], W = ceil(n_cap / 32)) and finished by k_locate32_guess (its
-//                   key and histogram entry are written there); a nearer one continues the
-//                   reference walk here.
+//                   [W + 1], W = ceil(n_cap / 32)) with its cell field set to P1, the
+//                   walk's second cell, and finished by k_locate32_path (its key and
+//                   histogram entry are written there); a nearer one continues the reference
+//                   walk here.
 template <bool FIRST>
 __global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_LOC_MIN_BLOCKS) k_locate32(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                   const double *__restrict__ planes, float dt32, int advect,
@@ -302,15 +247,21 @@ __global__ void k_compact_pending(const unsigned int *__restrict__ pf, int n_cap
   }
 }
 
-// The particles that left their previous cell (the list from k_locate32<true>, whose
-// cell field now holds the reference walk's second cell P1): the walk starts in the
-// learned guess and runs for at most FDF_GUESS_WALK evaluations.  Its cell C is taken
-// when C == P1 (the reference evaluates P1 next and concludes there with the same exact
-// decisions), or when it ends with every face positive by more than thr + C's overlap
-// margin, within FDF_GUESS_REACH cells (in each index) of P1.  Otherwise guess[t] becomes
-// -1 and k_locate32_fallback continues the reference walk from P1.  Grid-stride over the
-// list, warp-uniform trip count.
-__global__ void __launch_bounds__(FDF_GUESS_THREADS, FDF_GUESS_MIN_BLOCKS) k_locate32_guess(SwarmBuf b, GridDims g, const float *__restrict__ table,
+// The pending particles of the learned form (the list from k_locate32<true>; b.cell[s] holds P1,
+// the reference walk's second cell): the reference walk from P1, exactly as the FP32 form walks
+// it, with the plane-table rows of the path the network predicts -- P1 stepping one index per
+// axis toward the guessed cell -- prefetched into L1 ahead of the walk (`lookahead` cells after
+// P1).  Whatever the guess, the cells, weights and statuses are the reference walk's; a good
+// guess turns the walk's dependent row loads into L1 hits.  Grid-stride over the list with a
+// warp-uniform trip count; path_hits counts the evaluations whose row was prefetched.
+__device__ __forceinline__ void prefetch_row_l1(const float *row) {
+  const char *p = reinterpret_cast<const char *>(row);
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 88));
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 4 * FDF_ROW32 - 4));
+}
+
+__global__ void __launch_bounds__(FDF_GUESS_THREADS, FDF_GUESS_MIN_BLOCKS) k_locate32_path(SwarmBuf b, GridDims g, const float *__restrict__ table,
                                                         const double *__restrict__ planes,
                                                         const double *__restrict__ bbox,
                                                         const float *__restrict__ fbox, int drop_removed,
@@ -318,12 +269,12 @@ __global__ void __launch_bounds__(FDF_GUESS_THREADS, FDF_GUESS_MIN_BLOCKS) k_loc
                                                         unsigned int *__restrict__ rank,
                                                         unsigned int *__restrict__ count, unsigned int sentinel,
                                                         const unsigned int *__restrict__ pending,
-                                                        int *__restrict__ guess) {
+                                                        const int *__restrict__ guess, int lookahead) {
   const long long npend = (long long)cnt->pending;
   const long long stride = (long long)gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
-  unsigned int acc = 0, gev = 0;
-  LocCounts m;   // this thread's counters over all its list entries
+  unsigned int pev = 0, hits = 0;
+  LocCounts m;
   for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < npend; base += stride) {
     const long long t = base + lane;
     unsigned int hkey = 0xffffffffu;
@@ -331,119 +282,39 @@ __global__ void __launch_bounds__(FDF_GUESS_THREADS, FDF_GUESS_MIN_BLOCKS) k_loc
     if (t < npend) {
       s = (int)pending[t];
       const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
-      int pi, pj, pk;
-      cell_ijk(g, (unsigned int)b.cell[s], pi, pj, pk);
-      Eval32 e;
+      Walk32 w;
+      w.err = 0u;
+      cell_ijk(g, (unsigned int)b.cell[s], w.i, w.j, w.k);
       int gi, gj, gk;
       cell_ijk(g, (unsigned int)guess[t], gi, gj, gk);
-      const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
-      bool taken = false;
-      for (int step = 0; step < FDF_GUESS_WALK; ++step) {
-        if (gi < 0 || gi >= g.IM || gj < 0 || gj >= g.JM || gk < 0 || gk >= g.KM) break;
-        const long long cur = ((long long)gk * g.JM + gj) * g.IM + gi;
-        eval_cell32<true>(table, planes, cur, px, py, pz, sx, sy, sz, e, m.fb);
-        if (e.degenerate) break;
-        ++m.done; ++m.evals; ++gev;
-        if (!e.neg || e.zero) {
-          taken = (gi == pi && gj == pj && gk == pk) ||
-                  (e.clear && abs(gi - pi) <= FDF_GUESS_REACH && abs(gj - pj) <= FDF_GUESS_REACH &&
-                   abs(gk - pk) <= FDF_GUESS_REACH);
-          break;
-        }
-        const unsigned int ng = e.neg;
-        if (ng & (1u << F_FRONT)) gk += 1; else if (ng & (1u << F_BACK)) gk -= 1;
-        if (ng & (1u << F_LEFT)) gi -= 1; else if (ng & (1u << F_RIGHT)) gi += 1;
-        if (ng & (1u << F_BOTTOM)) gj -= 1; else if (ng & (1u << F_TOP)) gj += 1;
+      // P1 and the guess lie in the grid, so does every cell of the path between them
+      for (int q = 1; q <= lookahead; ++q) {
+        const int ci = path_index(w.i, gi, q), cj = path_index(w.j, gj, q), ck = path_index(w.k, gk, q);
+        prefetch_row_l1(table + (((long long)ck * g.JM + cj) * g.IM + ci) * FDF_ROW32);
+        if (ci == gi && cj == gj && ck == gk) break;   // the predicted path has reached the guess
       }
-      if (taken) {
-        ++acc;
-        store_located32(b, s, g, false, gi, gj, gk, e.dv);
-        const int cell = (int)(((long long)gk * g.JM + gj) * g.IM + gi);
-        const unsigned int key =
-            settle_key32(false, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
-        keys[s] = key;
-        if (key < sentinel) hkey = key;
-        else if (!drop_removed) hkey = sentinel;
-      } else {
-        guess[t] = -1;   // the reference walk from P1 decides (k_locate32_fallback)
-      }
+      walk_ref32<false, true>(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w, m.fb, 0.0, 0.0, 0.0, gi, gj,
+                              gk, &hits);
+      m.err |= w.err;
+      m.done += (unsigned int)w.evaluated;
+      m.evals += (unsigned int)w.evaluated;
+      pev += (unsigned int)w.evaluated;
+      const bool lost = w.lost || !w.concluded;
+      store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
+      const int cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
+      const unsigned int key =
+          settle_key32(lost, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
+      keys[s] = key;
+      if (key < sentinel) hkey = key;
+      else if (!drop_removed) hkey = sentinel;
     }
     const unsigned int r = warp_histogram_rank(hkey, count);
     if (hkey != 0xffffffffu) rank[s] = r;
   }
   block_flush_counts(m, cnt);
-  block_add_u64(acc, &cnt->guess_taken_total);
-  block_add_u64(gev, &cnt->guess_evals_total);
+  block_add_u64(hits, &cnt->guess_taken_total);
+  block_add_u64(pev, &cnt->guess_evals_total);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&cnt->guess_asked_total, (unsigned long long)npend);
-}
-
-// The pending particles whose guess was not taken (guess[t] < 0): the reference walk from its
-// second cell P1 (b.cell[s]), the remaining MAX_TRAVERSAL - 1 evaluations allowed.  Each warp
-// scans a chunk of FDF_FB_CHUNK list entries, queues the failed ones in shared memory and walks
-// them 32 at a time, so every lane has a particle.  Failures cluster in space (hence in the
-// list), so chunks of 256 rather than 1024 entries spread them over more warps: the guess walks
-// took 1.38 -> 1.28 ms at 64M particles and 0.13 -> 0.075 ms at 2M.
-#ifndef FDF_FB_CHUNK
-#define FDF_FB_CHUNK 256
-#endif
-constexpr int FB_CHUNK = FDF_FB_CHUNK;
-__global__ void __launch_bounds__(256, 3) k_locate32_fallback(SwarmBuf b, GridDims g, const float *__restrict__ table,
-                                                           const double *__restrict__ planes,
-                                                           const double *__restrict__ bbox,
-                                                           const float *__restrict__ fbox, int drop_removed,
-                                                           DevCounters *cnt, unsigned int *__restrict__ keys,
-                                                           unsigned int *__restrict__ rank,
-                                                           unsigned int *__restrict__ count, unsigned int sentinel,
-                                                           const unsigned int *__restrict__ pending,
-                                                           const int *__restrict__ guess) {
-  __shared__ unsigned int queue[8][FB_CHUNK];
-  const long long npend = (long long)cnt->pending;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
-  LocCounts m;
-  unsigned int fev = 0;
-  unsigned int *q = queue[wib];
-  for (long long chunk = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; chunk * FB_CHUNK < npend;
-       chunk += warps) {
-    int nq = 0;
-    for (int i = 0; i < FB_CHUNK / 32; ++i) {
-      const long long t = chunk * FB_CHUNK + i * 32 + lane;
-      const bool fail = t < npend && guess[t] < 0;
-      const unsigned int bal = __ballot_sync(0xffffffffu, fail);
-      if (fail) q[nq + __popc(bal & ((1u << lane) - 1u))] = (unsigned int)t;
-      nq += __popc(bal);
-    }
-    __syncwarp();
-    for (int base = 0; base < nq; base += 32) {
-      unsigned int hkey = 0xffffffffu;
-      int s = 0;
-      if (base + lane < nq) {
-        s = (int)pending[q[base + lane]];
-        const float2 px = ld_pair(b.x, s), py = ld_pair(b.y, s), pz = ld_pair(b.z, s);
-        Walk32 w;
-        w.err = 0u;
-        cell_ijk(g, (unsigned int)b.cell[s], w.i, w.j, w.k);
-        walk_ref32(table, planes, g, px, py, pz, FDF_MAX_TRAVERSAL - 1, w, m.fb);
-        m.err |= w.err;
-        m.done += (unsigned int)w.evaluated;
-        m.evals += (unsigned int)w.evaluated;
-        fev += (unsigned int)w.evaluated;
-        const bool lost = w.lost || !w.concluded;
-        store_located32(b, s, g, lost, w.i, w.j, w.k, w.e.dv);
-        const int cell = lost ? -1 : (int)(((long long)w.k * g.JM + w.j) * g.IM + w.i);
-        const unsigned int key =
-            settle_key32(lost, cell, px, py, pz, drop_removed, bbox, fbox, sentinel, m.lost, m.oob, m.lost_total);
-        keys[s] = key;
-        if (key < sentinel) hkey = key;
-        else if (!drop_removed) hkey = sentinel;
-      }
-      const unsigned int r = warp_histogram_rank(hkey, count);
-      if (hkey != 0xffffffffu) rank[s] = r;
-    }
-    __syncwarp();
-  }
-  block_flush_counts(m, cnt);
-  block_add_u64(fev, &cnt->fallback_evals_total);
 }
 
 // UpdateAllParticlePositions in the precision form: fl32(v dt) added to the (hi, lo) position,
@@ -885,29 +756,24 @@ void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *l
   k_compact_pending<<<blocks_for((n_cap + 31) / 32, 256), 256, 0, s>>>(scan, n_cap, list, cnt);
 }
 
-void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
-                           const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                           unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
-                           const unsigned int *pending, int *guess, int num_sms, cudaStream_t s) {
-  // grid-stride kernels: one wave of resident blocks, so that no SM runs a partial last wave
-  static int resident[2] = {0, 0}, res_device = -1;
+void launch_locate32_path(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
+                          const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
+                          unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
+                          const unsigned int *pending, const int *guess, int num_sms, cudaStream_t s) {
+  // grid-stride kernel: one wave of resident blocks, so that no SM runs a partial last wave
+  static int resident = 0, res_device = -1;
   int dev = 0;
   cudaGetDevice(&dev);
   if (res_device != dev) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_locate32_guess, FDF_GUESS_THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_locate32_fallback, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_locate32_path, FDF_GUESS_THREADS, 0);
     res_device = dev;
   }
-  auto wave = [&](int r, int th) {
-    const long long need = ((long long)n_cap + th - 1) / th;
-    long long blocks = (long long)num_sms * (r > 0 ? r : 1);
-    if (blocks > need) blocks = need;
-    return (unsigned)(blocks < 1 ? 1 : blocks);
-  };
-  k_locate32_guess<<<wave(resident[0], FDF_GUESS_THREADS), FDF_GUESS_THREADS, 0, s>>>(
-      b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, rank, count, sentinel, pending, guess);
-  k_locate32_fallback<<<wave(resident[1], 256), 256, 0, s>>>(b, g, table, planes, bbox, fbox, drop_removed, cnt, keys,
-                                                        rank, count, sentinel, pending, guess);
+  const long long need = ((long long)n_cap + FDF_GUESS_THREADS - 1) / FDF_GUESS_THREADS;
+  long long blocks = (long long)num_sms * (resident > 0 ? resident : 1);
+  if (blocks > need) blocks = need;
+  k_locate32_path<<<(unsigned)(blocks < 1 ? 1 : blocks), FDF_GUESS_THREADS, 0, s>>>(
+      b, g, table, planes, bbox, fbox, drop_removed, cnt, keys, rank, count, sentinel, pending, guess,
+      FDF_PATH_LOOKAHEAD);
 }
 
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,

@@ -19,14 +19,13 @@
 #include <cuda_runtime.h>
 
 #define FDF_ROW 38            // doubles per plane-table row (36 plane values + thr + flag)
-#define FDF_ROW32 44          // floats per precision-form row (c0 pair, thr32, overlap margin, 36 face values)
+#define FDF_ROW32 44          // floats per precision-form row (c0 pair, thr32, a zero, 36 face values)
 #define FDF_MAX_TRAVERSAL 1000
 #define FDF_DISTANCE_THRESHOLD 1e-11
 #define FDF_INTERP_DIST_TOL 1e-14
 #define FDF_BBOX_TOL 1e-6
 #define FDF_MAX_PARTICLES (512LL * 1024 * 1024)   // particle slots of one context or one sort call
-#define FDF_GUESS_WALK 4      // evaluations allowed to the walk from a learned guess
-#define FDF_GUESS_REACH 16    // largest index distance from the previous cell a guess may settle at
+#define FDF_PATH_LOOKAHEAD 2  // cells of the learned path whose table rows the walk from P1 prefetches
 
 // Face order of the reference (common.h Face enum).
 enum { F_LEFT = 0, F_RIGHT = 1, F_BOTTOM = 2, F_TOP = 3, F_FRONT = 4, F_BACK = 5 };
@@ -62,10 +61,10 @@ struct DevCounters {
   unsigned long long evals_total;   // walk evaluations actually made, all pipeline runs (never reset per step)
   unsigned long long nodes_total;   // corner nodes computed by the steps (never reset per step)
   unsigned long long fallbacks_total;
-  unsigned long long guess_asked_total;   // learned form: particles given a learned start cell
-  unsigned long long guess_taken_total;   // ... whose walk from the guess was accepted
-  unsigned long long guess_evals_total;   // ... evaluations made by the walks from the guess
-  unsigned long long fallback_evals_total;   // ... by the reference walks of the guesses not taken
+  unsigned long long guess_asked_total;   // learned form: particles given a guess (walked from P1)
+  unsigned long long guess_taken_total;   // ... their walks' evaluations after P1 whose cell lay on the guessed path
+  unsigned long long guess_evals_total;   // ... evaluations made by their walks from P1
+  unsigned long long fallback_evals_total;   // (unused: zero)
   unsigned long long stripes[FDF_CNT_STRIPES][CNT_SLOTS];   // pending block flushes (k_fold_counts)
 };
 // The counters without the flush rows (what the host reads back).
@@ -145,17 +144,11 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_ORDER_MIN_BLOCKS
 #define FDF_ORDER_MIN_BLOCKS 8
 #endif
-// Table rows a block of the FP32 locate kernel stages in shared memory (the range of its
-// particles' previous cells; 0: no staging).
-#ifndef FDF_STAGE_ROWS
-#define FDF_STAGE_ROWS 0
-#endif
-// Resident 256-thread blocks per SM the learned form's guess and fallback walks are compiled for.
+// Resident 256-thread blocks per SM the learned form's walk from P1 is compiled for.
 #ifndef FDF_GUESS_MIN_BLOCKS
 #define FDF_GUESS_MIN_BLOCKS 3
 #endif
-// Threads per block of the walk from the guess (the fallback walk keeps 256: its queues are per
-// block of 8 warps).
+// Threads per block of the learned form's walk from P1.
 #ifndef FDF_GUESS_THREADS
 #define FDF_GUESS_THREADS 256
 #endif
@@ -239,13 +232,12 @@ void launch_locate32(const SwarmBuf &b, int n_cap, GridDims g, const float *tabl
 // The learned form's pending list from the warps' masks and scanned counts (sets cnt->pending).
 void launch_compact_pending(const unsigned int *scan, int n_cap, unsigned int *list, DevCounters *cnt,
                             cudaStream_t s);
-// The learned form's second pass over pending[0 .. cnt->pending), guess[t] = start cell:
-// the walk from the guess, then the reference walk for the guesses not taken (guess[t] set
-// to -1 in between).
-void launch_locate32_guess(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
-                           const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
-                           unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
-                           const unsigned int *pending, int *guess, int num_sms, cudaStream_t s);
+// The learned form's second pass over pending[0 .. cnt->pending): the reference walk from P1 (the
+// particle's cell field), with the table rows of the path toward guess[t] prefetched.
+void launch_locate32_path(const SwarmBuf &b, int n_cap, GridDims g, const float *table, const double *planes,
+                          const double *bbox, const float *fbox, int drop_removed, DevCounters *cnt,
+                          unsigned int *keys, unsigned int *rank, unsigned int *count, unsigned int sentinel,
+                          const unsigned int *pending, const int *guess, int num_sms, cudaStream_t s);
 void launch_center_to_corner32(const float *ucat, GridDims g, float *corner, const unsigned int *cell_start,
                                unsigned long long *nodes_done, cudaStream_t s);
 void launch_gather_interp32(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, GridDims g, const float *corner,

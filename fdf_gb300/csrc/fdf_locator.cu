@@ -7,7 +7,7 @@
 //   samples   n points seeded like the volumetric initialisation (random cell, random
 //             logical coordinates), each located by the plain FP64 walk from its generating
 //             cell; the located (position, cell) pairs become (xhat, target) in FP32
-//   step t    minibatch by counter hash -> forward (4 tensor-core GEMMs, bias + SiLU) ->
+//   step t    minibatch by counter hash -> forward (4 tcgen05 GEMMs, bias + SiLU) ->
 //             loss and dloss/dy -> backward (dW by split-K GEMMs reduced in fixed order,
 //             dH by GEMMs, SiLU', bias sums) -> Adam on the FP32 master weights ->
 //             bfloat16 copy for the next step
@@ -21,8 +21,10 @@
 namespace {
 
 struct TrainScratch {
-  __nv_bfloat16 *X, *H[4], *Gb, *Gb4;
+  __nv_bfloat16 *X, *H[4], *Gb, *Gb4;   // X [B][6]: the inputs' bfloat16 pairs
   float *T, *C, *Z[4], *dH, *G, *Y, *G4, *loss_part, *partials;
+  float *dW1x;                          // [128][6] gradient of W1x = [W1 | W1]
+  unsigned int *err;                    // the GEMMs' tensor-core time-out bit
   int splits;
 };
 
@@ -38,7 +40,7 @@ size_t scratch_bytes(int B) {
   auto up = [&](size_t b) { return (b + r - 1) / r * r; };
   const size_t bh = (size_t)B * MLP_H;
   size_t t = 0;
-  t += up(2 * 3 * (size_t)B);                      // X
+  t += up(2 * 6 * (size_t)B);                      // X
   t += 3 * up(2 * bh);                             // H1..H3
   t += up(2 * bh) + up(2 * 3 * (size_t)B);         // Gb, Gb4
   t += up(4 * 3 * (size_t)B);                      // T
@@ -48,6 +50,7 @@ size_t scratch_bytes(int B) {
   t += 2 * up(4 * 3 * (size_t)B);                  // Y, G4
   t += up(4 * ((size_t)B / 256 + 2));              // loss partials
   t += up(4 * (size_t)splits_for(B) * MLP_H * MLP_H);
+  t += up(4 * MLP_H * 6) + up(4);                  // dW1x, err
   return t;
 }
 
@@ -60,7 +63,7 @@ TrainScratch carve_scratch(void *base, int B) {
   };
   const size_t bh = (size_t)B * MLP_H;
   TrainScratch s{};
-  s.X = (__nv_bfloat16 *)take(2 * 3 * (size_t)B);
+  s.X = (__nv_bfloat16 *)take(2 * 6 * (size_t)B);
   s.H[0] = s.X;
   for (int l = 1; l < 4; ++l) s.H[l] = (__nv_bfloat16 *)take(2 * bh);
   s.Gb = (__nv_bfloat16 *)take(2 * bh);
@@ -76,21 +79,24 @@ TrainScratch carve_scratch(void *base, int B) {
   s.loss_part = (float *)take(4 * ((size_t)B / 256 + 2));
   s.splits = splits_for(B);
   s.partials = (float *)take(4 * (size_t)s.splits * MLP_H * MLP_H);
+  s.dW1x = (float *)take(4 * MLP_H * 6);
+  s.err = (unsigned int *)take(4);
   return s;
 }
 
 int alloc_params(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
-  if (L.params && L.grads && L.adam_m && L.adam_v && L.params_bf && L.bias && L.tc_img) return FDF_SUCCESS;
+  if (L.params && L.grads && L.adam_m && L.adam_v && L.params_bf && L.w1x && L.bias && L.tc_img) return FDF_SUCCESS;
   // all or none: a partial set left by a failed allocation is freed and made again
   L.has_params = false;
-  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf); cfree(L.bias);
-  cfree(L.tc_img);
+  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf); cfree(L.w1x);
+  cfree(L.bias); cfree(L.tc_img);
   CU(dev_alloc(&L.params, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.grads, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.adam_m, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.adam_v, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.params_bf, 2ull * MLP_NPARAM));
+  CU(dev_alloc(&L.w1x, 2ull * MLP_H * 6));
   CU(dev_alloc(&L.bias, 4ull * MLP_BIAS_WORDS));
   CU(dev_alloc(&L.tc_img, mlp_tc_image_bytes()));
   return FDF_SUCCESS;
@@ -115,30 +121,38 @@ void set_norm(FdfContext *ctx) {
   }
 }
 
-// Makes the bfloat16 copy of the weights and the inference packing.
-void refresh_weights(FdfContext *ctx, cudaStream_t s) {
+// Makes the bfloat16 copies of the weights the training GEMMs read.
+void training_weights(FdfContext *ctx, cudaStream_t s) {
   LocatorState &L = ctx->loc;
   mlp_to_bf16(L.params, L.params_bf, MLP_NPARAM, s);
+  mlp_split_w1(L.params_bf + MLP_OFF_W1, L.w1x, s);
+  ctx->launches += 2;
+}
+
+// The training copies and the inference packing.
+void refresh_weights(FdfContext *ctx, cudaStream_t s) {
+  LocatorState &L = ctx->loc;
+  training_weights(ctx, s);
   mlp_pack_bias(L.params, L.bias, s);
-  mlp_pack_tc(L.params, L.tc_img, s);
-  ctx->launches += 3;
+  mlp_pack_tc(L.params, L.tc_img, L.infer_bf16, s);
+  ctx->launches += 2;
 }
 
 // Loss and gradients (into L.grads) of the batch in scratch (X, T), current weights.
 void forward_backward(FdfContext *ctx, const TrainScratch &S, int B, float *loss_out, cudaStream_t s) {
   LocatorState &L = ctx->loc;
-  const __nv_bfloat16 *Wb[4] = {L.params_bf + MLP_OFF_W1, L.params_bf + MLP_OFF_W2, L.params_bf + MLP_OFF_W3,
+  const __nv_bfloat16 *Wb[4] = {L.w1x, L.params_bf + MLP_OFF_W2, L.params_bf + MLP_OFF_W3,
                                 L.params_bf + MLP_OFF_W4};
   const float *bvec[4] = {L.params + MLP_OFF_B1, L.params + MLP_OFF_B2, L.params + MLP_OFF_B3, L.params + MLP_OFF_B4};
-  float *dW[4] = {L.grads + MLP_OFF_W1, L.grads + MLP_OFF_W2, L.grads + MLP_OFF_W3, L.grads + MLP_OFF_W4};
+  float *dW[4] = {S.dW1x, L.grads + MLP_OFF_W2, L.grads + MLP_OFF_W3, L.grads + MLP_OFF_W4};
   float *db[4] = {L.grads + MLP_OFF_B1, L.grads + MLP_OFF_B2, L.grads + MLP_OFF_B3, L.grads + MLP_OFF_B4};
-  const int fin[4] = {3, MLP_H, MLP_H, MLP_H};
+  const int fin[4] = {6, MLP_H, MLP_H, MLP_H};   // layer 1 reads the inputs' (hi, lo) pairs against W1x
   // forward: C = H_{l} W_l^T (A = H [B][fin], B(k, n) = W[n][k])
   for (int l = 0; l < 3; ++l) {
-    mlp_gemm(S.H[l], fin[l], 1, Wb[l], 1, fin[l], S.C, MLP_H, 1, B, MLP_H, fin[l], 1, nullptr, s);
+    mlp_gemm(S.H[l], fin[l], 1, Wb[l], 1, fin[l], S.C, MLP_H, 1, B, MLP_H, fin[l], 1, nullptr, S.err, s);
     mlp_bias_silu(S.C, bvec[l], B, MLP_H, S.Z[l + 1], S.H[l + 1], s);
   }
-  mlp_gemm(S.H[3], MLP_H, 1, Wb[3], 1, MLP_H, S.C, 3, 1, B, 3, MLP_H, 1, nullptr, s);
+  mlp_gemm(S.H[3], MLP_H, 1, Wb[3], 1, MLP_H, S.C, 3, 1, B, 3, MLP_H, 1, nullptr, S.err, s);
   float sc[3];
   const int N[3] = {ctx->g.IM, ctx->g.JM, ctx->g.KM};
   for (int d = 0; d < 3; ++d) sc[d] = 0.5f * (float)N[d];
@@ -150,24 +164,25 @@ void forward_backward(FdfContext *ctx, const TrainScratch &S, int B, float *loss
   int nout = 3;
   for (int l = 3; l >= 0; --l) {
     // dW_l [nout][fin] = sum_b gb[b][o] h_l[b][i]: A(m = o, k = b) = gb[b*nout + o], B(k = b, n = i) = h[b*fin + i]
-    mlp_gemm(gb, 1, nout, S.H[l], fin[l], 1, dW[l], fin[l], 1, nout, fin[l], B, S.splits, S.partials, s);
+    mlp_gemm(gb, 1, nout, S.H[l], fin[l], 1, dW[l], fin[l], 1, nout, fin[l], B, S.splits, S.partials, S.err, s);
     mlp_colsum(g, B, nout, db[l], s);
     if (l == 0) break;
     // dH_l [B][fin] = gb @ W_l: A(m = b, k = o) = gb[b*nout + o], B(k = o, n = i) = W[o*fin + i]
-    mlp_gemm(gb, nout, 1, Wb[l], fin[l], 1, S.dH, MLP_H, 1, B, MLP_H, nout, 1, nullptr, s);
+    mlp_gemm(gb, nout, 1, Wb[l], fin[l], 1, S.dH, MLP_H, 1, B, MLP_H, nout, 1, nullptr, S.err, s);
     mlp_silu_bwd(S.dH, S.Z[l], (long long)B * MLP_H, S.G, S.Gb, s);
     gb = S.Gb;
     g = S.G;
     nout = MLP_H;
   }
-  ctx->launches += 2 * 3 + 1 + 2 + 4 * 2 + 3 * 2 + 4 * (S.splits > 1 ? 1 : 0);
+  mlp_fold_w1(S.dW1x, L.grads + MLP_OFF_W1, s);
+  ctx->launches += 2 * 3 + 1 + 2 + 4 * 2 + 3 * 2 + 4 * (S.splits > 1 ? 1 : 0) + 1;
 }
 
 }  // namespace
 
 void locator_free(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
-  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf);
+  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf); cfree(L.w1x);
   cfree(L.bias); cfree(L.tc_img); cfree(L.pending); cfree(L.guess); cfree(L.scratch); cfree(L.pflag);
   cfree(L.scan_sums);
   L.pending_cap = 0;
@@ -260,16 +275,20 @@ int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target
   if (r) return r;
   TrainScratch S = carve_scratch(ctx->loc.scratch, ctx->loc.batch_cap);
   cudaStream_t s = ctx->stream;
-  // xhat goes through the G buffer (FP32) into X (bfloat16)
+  // xhat goes through the G buffer (FP32) into X (its bfloat16 pairs)
   CU(cudaMemcpyAsync(S.G, xhat, 12ull * B, cudaMemcpyHostToDevice, s));
   CU(cudaMemcpyAsync(S.T, target, 12ull * B, cudaMemcpyHostToDevice, s));
-  mlp_to_bf16(S.G, S.X, 3 * B, s);
+  CU(cudaMemsetAsync(S.err, 0, 4, s));
+  mlp_split_inputs(S.G, B, S.X, s);
   float *d_loss = S.loss_part + (B + 255) / 256;
   forward_backward(ctx, S, B, d_loss, s);
   CHECK_LAUNCH();
+  unsigned int errw = 0;
   CU(cudaMemcpyAsync(grads, ctx->loc.grads, 4ull * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
   CU(cudaMemcpyAsync(loss, d_loss, 4, cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(&errw, S.err, 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
+  if (errw & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "fdf_LocatorGradients: tensor-core wait timed out");
   return FDF_SUCCESS;
 }
 
@@ -354,6 +373,7 @@ int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t 
   if (r) { release(); return r; }
   TrainScratch S = carve_scratch(L.scratch, L.batch_cap);
   CUT(cudaMalloc((void **)&hist_loss, 4ull * (steps > 0 ? steps : 1)));
+  CUT(cudaMemsetAsync(S.err, 0, 4, s));
   const double pi = 3.14159265358979323846;
   for (long long t = 0; t < steps; ++t) {
     mlp_gather_batch(xs, ts, m, seed ^ 0x5DEECE66DULL, t, B, S.X, S.T, s);
@@ -362,18 +382,21 @@ int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t 
     L.adam_t += 1;
     const double c1 = 1.0 - std::pow(0.9, (double)L.adam_t), c2 = 1.0 - std::pow(0.999, (double)L.adam_t);
     mlp_adam(L.params, L.grads, L.adam_m, L.adam_v, MLP_NPARAM, (float)lr_t, (float)c1, (float)c2, s);
-    mlp_to_bf16(L.params, L.params_bf, MLP_NPARAM, s);
-    ctx->launches += 3;
+    training_weights(ctx, s);
+    ctx->launches += 2;
     if ((t & 255) == 255) CUT(cudaGetLastError());
   }
   refresh_weights(ctx, s);
   CUT(cudaGetLastError());
   if (loss_history && steps > 0)
     CUT(cudaMemcpyAsync(loss_history, hist_loss, 4ull * steps, cudaMemcpyDeviceToHost, s));
+  unsigned int errw = 0;
+  CUT(cudaMemcpyAsync(&errw, S.err, 4, cudaMemcpyDeviceToHost, s));
   CUT(cudaStreamSynchronize(s));
 #undef CUT
   release();
-  L.has_params = true;
+  L.has_params = !(errw & ERRBIT_TC_TIMEOUT);   // weights from a step that timed out are not kept as valid
+  if (errw & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "fdf_LocatorTrain: tensor-core wait timed out");
   return FDF_SUCCESS;
 }
 
@@ -402,8 +425,9 @@ static int locator_predict(FdfContext *ctx, const double *position, int64_t n, i
   cudaError_t e = cudaMemcpyAsync(d_pos, soa.data(), 24ull * n, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_err, 0, sizeof(unsigned int), s);
   if (e == cudaSuccess) {
-    mlp_guess_tc(ctx->loc.tc_img, ctx->loc.bias, ctx->loc.norm, d_pos, d_pos + n, d_pos + 2 * n, 0, nullptr,
-                 nullptr, (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, d_err, s, d_out, stall_test);
+    mlp_guess_tc(ctx->loc.tc_img, ctx->loc.infer_bf16, ctx->loc.bias, ctx->loc.norm, d_pos, d_pos + n,
+                 d_pos + 2 * n, 0, nullptr, nullptr, (int)n, (int)n, ctx->g, d_guess, ctx->num_sms, d_err, s, d_out,
+                 stall_test);
     ctx->launches += 1;
     e = cudaGetLastError();
   }
@@ -437,6 +461,25 @@ int fdf_TestLocatorWaitTimeout(FdfContext *ctx, const double *position, int64_t 
   return locator_predict(ctx, position, n, cells.data(), nullptr, 1);
 }
 
+int fdf_LocatorSetInferenceType(FdfContext *ctx, int type) {
+  if (!ctx) return FDF_ERR_ARG_NULL;
+  if (type != FDF_LOCATOR_BF16 && type != FDF_LOCATOR_F16)
+    return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorSetInferenceType: FDF_LOCATOR_BF16 or FDF_LOCATOR_F16");
+  LocatorState &L = ctx->loc;
+  const int bf16 = type == FDF_LOCATOR_BF16 ? 1 : 0;
+  if (bf16 == L.infer_bf16) return FDF_SUCCESS;
+  CU(cudaSetDevice(ctx->device));
+  L.infer_bf16 = bf16;
+  ctx->gen++;   // a captured step holds the launch's operand type
+  if (L.has_params) {
+    mlp_pack_tc(L.params, L.tc_img, L.infer_bf16, ctx->stream);
+    ctx->launches += 1;
+    CHECK_LAUNCH();
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+  return FDF_SUCCESS;
+}
+
 int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells) {
   if (!ctx) return FDF_ERR_ARG_NULL;
   if (!(cells >= 0.0)) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorSetMinDistance: cells must be >= 0");
@@ -447,6 +490,7 @@ int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells) {
 
 int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals,
                         int64_t *fallback_evals) {
+  // taken: evaluations on the predicted path; guess_evals: evaluations of the walks from P1
   if (!ctx || !asked || !taken || !guess_evals || !fallback_evals) return FDF_ERR_ARG_NULL;
   CU(cudaSetDevice(ctx->device));
   DevCounters c{};

@@ -4,39 +4,26 @@
 // prediction is only a starting cell (the learned walk in fdf_fp32.cu); inference runs on
 // tcgen05 (fdf_mlp_tc.cu).
 //
-// Every training GEMM is mma.sync m16n8k16 with bfloat16 operands and FP32 accumulation: a
-// generic warp-tile GEMM (16x8 output tile per warp, operands read with arbitrary strides, so
-// the same kernel serves X W^T, G W and G^T H), plus elementwise kernels for bias + SiLU, the
-// loss, SiLU', bias sums and Adam (FP32 master weights).  Each output is computed by one warp
-// in a fixed k order, and the sums run in fixed order, so training is deterministic.  The
-// training matrices are small (batch x 128 x 128); the hot path is inference.
+// Every training GEMM runs on the 5th-generation tensor cores (tcgen05.mma, kind::f16,
+// bfloat16 operands, FP32 accumulator in tensor memory): one generic GEMM kernel whose CTAs
+// stage 128-row tiles of both operands -- read with arbitrary strides, so the same kernel
+// serves X W^T, G W and G^T H -- into shared memory in the K-major core-matrix layout
+// (fdf_tc.cuh), 64 K columns at a time, and let one thread issue the chunk's four MMAs; plus
+// elementwise kernels for bias + SiLU, the loss, SiLU', bias sums and Adam (FP32 master
+// weights).  Each output is accumulated by one CTA in a fixed K order, split-K partials and
+// the other sums are added in fixed order, so training is deterministic.  The training
+// matrices are small (batch x 128 x 128); the hot path is inference.
 //
-// Fragment layouts of mma.m16n8k16 (g = lane/4, c = lane%4):
-//   A (16x16, row): a0 = A[g][2c..2c+1], a1 = A[g+8][2c..2c+1], a2 = A[g][2c+8..9], a3 = A[g+8][2c+8..9]
-//   B (16x8, col):  b0 = B[2c..2c+1][g],  b1 = B[2c+8..9][g]
-//   C (16x8, f32):  c0 = C[g][2c], c1 = C[g][2c+1], c2 = C[g+8][2c], c3 = C[g+8][2c+1]
+// Input layer.  Each normalised coordinate enters as the bfloat16 pair hi = bf16(x),
+// lo = bf16(x - hi) (K = 6: hi x, y, z, lo x, y, z) against W1 repeated in both column groups,
+// as in inference; the W1 gradient is the sum of the two groups' gradients.
 #include "fdf_internal.cuh"
 #include "fdf_mlp.cuh"
+#include "fdf_tc.cuh"
 #include <cuda_bf16.h>
 #include <cmath>
 
 namespace {
-
-__device__ __forceinline__ void mma_bf16(float &d0, float &d1, float &d2, float &d3, unsigned a0, unsigned a1,
-                                         unsigned a2, unsigned a3, unsigned b0, unsigned b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<unsigned *>(&v);
-}
-
-__device__ __forceinline__ float bf(const __nv_bfloat16 *p, long long i) { return __bfloat162float(p[i]); }
 
 // SiLU and its derivative in FP32 (training).
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
@@ -47,49 +34,136 @@ __device__ __forceinline__ float silu_grad(float z) {
 
 // ---------------------------------------------------------------- training GEMM
 // C(m, n) = sum_k A(m, k) B(k, n), A(m, k) = A[m*sam + k*sak], B(k, n) = B[k*sbk + n*sbn],
-// C(m, n) at C[m*scm + n*scn]; one warp per 16x8 tile and K slice of kc (a multiple of 16),
-// zero padding outside (M, N, K).  With more than one slice the warps write partial tiles
+// C(m, n) at C[m*scm + n*scn].  One CTA per 128 x NT output tile (NT = 16 for N <= 16, else
+// 128) and K slice [kb, kb + kc): its 128 threads stage A's rows and B's columns for 64 K at a
+// time (zeros outside M, N, K) as the A [128][64] and B [NT][64] operands, thread 0 issues
+// four M = 128 MMAs of K = 16 into the CTA's 128 TMEM columns, and everyone waits on the
+// mbarrier before the next chunk overwrites the operands.  The four warps then read their
+// 32 accumulator lanes (rows).  With more than one slice the CTAs write partial tiles
 // [split][M][N] that k_splitk_reduce adds in slice order, so the result does not depend on
-// scheduling.
-__global__ void k_gemm(const __nv_bfloat16 *__restrict__ A, long long sam, long long sak,
-                       const __nv_bfloat16 *__restrict__ B, long long sbk, long long sbn, float *__restrict__ C,
-                       long long scm, long long scn, int M, int N, int K, int kc, int splits,
-                       float *__restrict__ partials) {
-  const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  const int tiles_n = (N + 7) / 8, tiles_m = (M + 15) / 16;
-  const long long tiles = (long long)tiles_m * tiles_n;
-  const int split = (int)(warp / tiles);
-  if (split >= splits) return;
-  const int t = (int)(warp % tiles);
-  const int tm = t / tiles_n, tn = t % tiles_n;
-  const int g = lane >> 2, c = lane & 3;
-  const int m0 = tm * 16, n0 = tn * 8;
+// scheduling.  A wait that runs out sets ERRBIT_TC_TIMEOUT in *err; the CTA then frees its
+// tensor memory and returns without writing.
+constexpr int GT_KC = 64;
+constexpr int GT_THREADS = 128;
+constexpr int GT_SM_A = 0;               // [128][64] bfloat16, 16 KB
+constexpr int GT_SM_B = 16384;           // [128][64] bfloat16, 16 KB
+constexpr int GT_SM_BAR = 32768;         // mbarrier (8 B), TMEM base (4 B), time-out flag (4 B)
+// dynamic shared memory asked per CTA: at most three CTAs share an SM, 3 x 128 of its 512 TMEM
+// columns, so no allocation ever waits
+constexpr int GT_SM_LAUNCH = 72 * 1024;
+constexpr unsigned long long GT_WAIT_LIMIT = 1ull << 22;
+
+__device__ __forceinline__ unsigned short bf_bits(const __nv_bfloat16 *p, long long i) {
+  return reinterpret_cast<const unsigned short *>(p)[i];
+}
+
+__global__ void __launch_bounds__(GT_THREADS)
+    k_gemm_tc(const __nv_bfloat16 *__restrict__ A, long long sam, long long sak, const __nv_bfloat16 *__restrict__ B,
+              long long sbk, long long sbn, float *__restrict__ C, long long scm, long long scn, int M, int N, int K,
+              int kc, int splits, float *__restrict__ partials, unsigned int *__restrict__ err,
+              unsigned long long wait_limit) {
+  using namespace fdftc;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nt = N <= 16 ? 16 : 128;
+  const int tiles_n = (N + nt - 1) / nt, tiles_m = (M + 127) / 128;
+  const int t = (int)(blockIdx.x % (unsigned)(tiles_m * tiles_n)), split = (int)(blockIdx.x / (unsigned)(tiles_m * tiles_n));
+  const int m0 = (t / tiles_n) * 128, n0 = (t % tiles_n) * nt;
   const int kb = split * kc, ke = min(K, kb + kc);
-  float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
-  auto Av = [&](int m, int k) -> float { return (m < M && k < ke) ? bf(A, m * sam + k * sak) : 0.f; };
-  auto Bv = [&](int k, int n) -> float { return (k < ke && n < N) ? bf(B, k * sbk + n * sbn) : 0.f; };
-  for (int k0 = kb; k0 < ke; k0 += 16) {
-    const unsigned a0 = pack_bf16(Av(m0 + g, k0 + 2 * c), Av(m0 + g, k0 + 2 * c + 1));
-    const unsigned a1 = pack_bf16(Av(m0 + g + 8, k0 + 2 * c), Av(m0 + g + 8, k0 + 2 * c + 1));
-    const unsigned a2 = pack_bf16(Av(m0 + g, k0 + 2 * c + 8), Av(m0 + g, k0 + 2 * c + 9));
-    const unsigned a3 = pack_bf16(Av(m0 + g + 8, k0 + 2 * c + 8), Av(m0 + g + 8, k0 + 2 * c + 9));
-    const unsigned b0 = pack_bf16(Bv(k0 + 2 * c, n0 + g), Bv(k0 + 2 * c + 1, n0 + g));
-    const unsigned b1 = pack_bf16(Bv(k0 + 2 * c + 8, n0 + g), Bv(k0 + 2 * c + 9, n0 + g));
-    mma_bf16(d0, d1, d2, d3, a0, a1, a2, a3, b0, b1);
+  unsigned *tmem_slot = reinterpret_cast<unsigned *>(smem + GT_SM_BAR + 8);
+  volatile unsigned *tflag = reinterpret_cast<volatile unsigned *>(smem + GT_SM_BAR + 12);
+  const unsigned bar_addr = smem_u32(smem + GT_SM_BAR);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar_addr) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    *tflag = 0u;
   }
-  const int r0 = m0 + g, r1 = m0 + g + 8, q0 = n0 + 2 * c, q1 = q0 + 1;
-  if (splits == 1) {
-    if (r0 < M && q0 < N) C[r0 * scm + q0 * scn] = d0;
-    if (r0 < M && q1 < N) C[r0 * scm + q1 * scn] = d1;
-    if (r1 < M && q0 < N) C[r1 * scm + q0 * scn] = d2;
-    if (r1 < M && q1 < N) C[r1 * scm + q1 * scn] = d3;
-  } else {
-    float *P = partials + (long long)split * M * N;
-    if (r0 < M && q0 < N) P[(long long)r0 * N + q0] = d0;
-    if (r0 < M && q1 < N) P[(long long)r0 * N + q1] = d1;
-    if (r1 < M && q0 < N) P[(long long)r1 * N + q0] = d2;
-    if (r1 < M && q1 < N) P[(long long)r1 * N + q1] = d3;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(128)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const unsigned tmem = *tmem_slot;
+  const unsigned a_addr = smem_u32(smem + GT_SM_A), b_addr = smem_u32(smem + GT_SM_B);
+  const unsigned idesc = make_idesc(128, nt, true);
+  unsigned phase = 0;
+  bool ok = true;
+#pragma unroll 1
+  for (int k0 = kb; k0 < ke && ok; k0 += GT_KC) {
+    // 8 consecutive K columns of one row per item, stored as one 16-B line of a core matrix
+#pragma unroll 1
+    for (int q = tid; q < 128 * 8; q += GT_THREADS) {
+      const int r = q >> 3, kg = (q & 7) * 8, m = m0 + r;
+      unsigned short v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int k = k0 + kg + e;
+        v[e] = (m < M && k < ke) ? bf_bits(A, m * sam + k * sak) : (unsigned short)0;
+      }
+      *reinterpret_cast<uint4 *>(smem + GT_SM_A + op_off(r, kg, 16 * GT_KC)) =
+          make_uint4(v[0] | ((unsigned)v[1] << 16), v[2] | ((unsigned)v[3] << 16), v[4] | ((unsigned)v[5] << 16),
+                     v[6] | ((unsigned)v[7] << 16));
+    }
+#pragma unroll 1
+    for (int q = tid; q < nt * 8; q += GT_THREADS) {
+      const int r = q >> 3, kg = (q & 7) * 8, n = n0 + r;
+      unsigned short v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const int k = k0 + kg + e;
+        v[e] = (n < N && k < ke) ? bf_bits(B, k * sbk + n * sbn) : (unsigned short)0;
+      }
+      *reinterpret_cast<uint4 *>(smem + GT_SM_B + op_off(r, kg, 16 * GT_KC)) =
+          make_uint4(v[0] | ((unsigned)v[1] << 16), v[2] | ((unsigned)v[3] << 16), v[4] | ((unsigned)v[5] << 16),
+                     v[6] | ((unsigned)v[7] << 16));
+    }
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+#pragma unroll
+      for (int s = 0; s < GT_KC / 16; ++s)
+        mma_f16(tmem, make_desc(a_addr + 256 * s, 128, 16 * GT_KC), make_desc(b_addr + 256 * s, 128, 16 * GT_KC),
+                idesc, (k0 > kb || s > 0) ? 1u : 0u);
+      mma_commit(bar_addr);
+    }
+    // the chunk's MMAs read the staged operands: they finish before the next chunk is staged
+    bool done = false;
+    for (unsigned long long it = 0; it < wait_limit && !done; ++it) done = mbar_try_wait(bar_addr, phase);
+    phase ^= 1u;
+    if (!done) *tflag = 1u;
+    __syncthreads();
+    ok = *tflag == 0u;
+    fence_after_sync();
+  }
+  if (ok) {
+    const int m = m0 + 32 * warp + lane;   // warp w reads TMEM lanes 32w .. 32w + 31
+#pragma unroll 1
+    for (int c = 0; c < nt; c += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((unsigned)(32 * warp) << 16) + (unsigned)c, v);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int n = n0 + c + q;
+        if (m < M && n < N) {
+          if (splits == 1) C[m * scm + n * scn] = v[q];
+          else partials[((long long)split * M + m) * N + n] = v[q];
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicOr(err, (unsigned)ERRBIT_TC_TIMEOUT);
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128) : "memory");
   }
 }
 
@@ -110,6 +184,15 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 
+// The bfloat16 pair (hi, lo) of a normalised coordinate: X row [hi x, y, z, lo x, y, z].
+__device__ __forceinline__ void split_row(const float *x, __nv_bfloat16 *X) {
+  for (int d = 0; d < 3; ++d) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x[d]);
+    X[d] = h;
+    X[3 + d] = __float2bfloat16_rn(x[d] - __bfloat162float(h));
+  }
+}
+
 // Minibatch `step`: sample b is mix64(seed, step, b) mod n (with replacement).
 __global__ void k_gather_batch(const float *__restrict__ xs, const float *__restrict__ ts, long long n,
                                unsigned long long seed, long long step, int B, __nv_bfloat16 *__restrict__ X,
@@ -119,10 +202,24 @@ __global__ void k_gather_batch(const float *__restrict__ xs, const float *__rest
   const unsigned long long h =
       mix64(mix64(seed * 0xD1B54A32D192ED03ULL + (unsigned long long)step) + (unsigned long long)b * 0x9E3779B97F4A7C15ULL);
   const long long s = (long long)(h % (unsigned long long)n);
-  for (int d = 0; d < 3; ++d) {
-    X[b * 3 + d] = __float2bfloat16_rn(xs[3 * s + d]);
-    T[b * 3 + d] = ts[3 * s + d];
-  }
+  split_row(xs + 3 * s, X + 6 * b);
+  for (int d = 0; d < 3; ++d) T[b * 3 + d] = ts[3 * s + d];
+}
+
+__global__ void k_split_inputs(const float *__restrict__ xs, int B, __nv_bfloat16 *__restrict__ X) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < B) split_row(xs + 3 * b, X + 6 * b);
+}
+
+// W1 [128][3] (bfloat16) repeated as W1x [128][6] = [W1 | W1]; and the W1 gradient as the sum of
+// the two column groups' gradients dW1x [128][6].
+__global__ void k_split_w1(const __nv_bfloat16 *__restrict__ w1, __nv_bfloat16 *__restrict__ w1x) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < MLP_H * 6) w1x[q] = w1[(q / 6) * 3 + (q % 6) % 3];
+}
+__global__ void k_fold_w1(const float *__restrict__ dw1x, float *__restrict__ dw1) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < MLP_H * 3) dw1[q] = dw1x[(q / 3) * 6 + q % 3] + dw1x[(q / 3) * 6 + 3 + q % 3];
 }
 
 __global__ void k_bias_silu(const float *__restrict__ Cin, const float *__restrict__ bias, int B, int N,
@@ -250,15 +347,23 @@ inline unsigned blocks_for(long long n, int th) { return (unsigned)(n > 0 ? (n +
 // ---------------------------------------------------------------- host side
 void mlp_gemm(const __nv_bfloat16 *A, long long sam, long long sak, const __nv_bfloat16 *B, long long sbk,
               long long sbn, float *C, long long scm, long long scn, int M, int N, int K, int splits,
-              float *partials, cudaStream_t s) {
+              float *partials, unsigned int *err, cudaStream_t s) {
+  static int attr_device = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (attr_device != dev) {
+    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SM_LAUNCH);
+    attr_device = dev;
+  }
   if (splits < 1 || partials == nullptr) splits = 1;
   int kc = (K + splits - 1) / splits;
-  kc = (kc + 15) / 16 * 16;
+  kc = (kc + GT_KC - 1) / GT_KC * GT_KC;
   splits = (K + kc - 1) / kc;
   if (splits < 1) splits = 1;
-  const long long warps = (long long)((M + 15) / 16) * ((N + 7) / 8) * splits;
-  k_gemm<<<blocks_for(warps * 32, 256), 256, 0, s>>>(A, sam, sak, B, sbk, sbn, C, scm, scn, M, N, K, kc, splits,
-                                                     partials);
+  const int nt = N <= 16 ? 16 : 128;
+  const long long ctas = (long long)((M + 127) / 128) * ((N + nt - 1) / nt) * splits;
+  k_gemm_tc<<<(unsigned)ctas, GT_THREADS, GT_SM_LAUNCH, s>>>(A, sam, sak, B, sbk, sbn, C, scm, scn, M, N, K, kc,
+                                                             splits, partials, err, GT_WAIT_LIMIT);
   if (splits > 1)
     k_splitk_reduce<<<blocks_for((long long)M * N, 256), 256, 0, s>>>(partials, splits, M, N, C, scm, scn);
 }
@@ -282,6 +387,15 @@ void mlp_colsum(const float *G, int B, int N, float *db, cudaStream_t s) {
 }
 void mlp_adam(float *w, const float *g, float *m, float *v, int n, float lr, float c1, float c2, cudaStream_t s) {
   k_adam<<<blocks_for(n, 256), 256, 0, s>>>(w, g, m, v, n, lr, c1, c2);
+}
+void mlp_split_inputs(const float *xs, int B, __nv_bfloat16 *X, cudaStream_t s) {
+  k_split_inputs<<<blocks_for(B, 256), 256, 0, s>>>(xs, B, X);
+}
+void mlp_split_w1(const __nv_bfloat16 *w1, __nv_bfloat16 *w1x, cudaStream_t s) {
+  k_split_w1<<<blocks_for(MLP_H * 6, 256), 256, 0, s>>>(w1, w1x);
+}
+void mlp_fold_w1(const float *dw1x, float *dw1, cudaStream_t s) {
+  k_fold_w1<<<blocks_for(MLP_H * 3, 256), 256, 0, s>>>(dw1x, dw1);
 }
 void mlp_to_bf16(const float *in, __nv_bfloat16 *out, int n, cudaStream_t s) {
   k_to_bf16<<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);

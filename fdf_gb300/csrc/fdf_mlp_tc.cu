@@ -1,32 +1,36 @@
 // fdf_mlp_tc.cu -- inference of the learned start-cell locator on the 5th-generation tensor
-// cores (tcgen05): one CTA holds the network's weights in shared memory (half precision: the
-// network trains in bfloat16, and its weights and activations lie well inside half precision's
-// range) and carries tiles of 128 particles through the four layers; each layer is
-// tcgen05.mma (M = 128,
-// kind::f16, half-precision operands from shared memory, FP32 accumulator in tensor memory),
-// issued by one thread and tracked by an mbarrier; the four warps then read the accumulator
-// rows back with tcgen05.ld (one particle per thread), add the bias, apply SiLU in packed half2
-// arithmetic and store the activations as the next layer's A operand.  One CTA per SM holds the weights once
-// and runs four independent tile pipelines (one per warpgroup, each with its own activation
-// buffers, mbarrier and 128 TMEM columns), so the tensor core serves one pipeline's MMAs while
-// the others run their epilogues; each pipeline prefetches its next tile's positions while
-// the current tile computes.
+// cores (tcgen05): one CTA holds the network's weights in shared memory as 16-bit values
+// (bfloat16 by default, as the network trains; half precision on request) and carries tiles
+// of 128 particles through the four layers; each layer is tcgen05.mma (M = 128, kind::f16,
+// 16-bit operands from shared memory, FP32 accumulator in tensor memory), issued by one thread
+// and tracked by an mbarrier; the four warps then read the accumulator rows back with
+// tcgen05.ld (one particle per thread), add the bias, apply SiLU in packed 16-bit pair
+// arithmetic and store the activations as the next layer's A operand.  One CTA per SM holds
+// the weights once and runs four independent tile pipelines (one per warpgroup, each with its
+// own activation buffers, mbarrier and 128 TMEM columns), so the tensor core serves one
+// pipeline's MMAs while the others run their epilogues; each pipeline prefetches its next
+// tile's positions while the current tile computes.
 //
-// Shared-memory operand layout (no swizzle, K-major): an R x K 16-bit matrix is stored as
-// 8-row x 16-byte core matrices; element (r, k) sits at
-//     (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2
-// with SBO = 16 * K bytes (all K / 8 core matrices of an 8-row group side by side), so the
-// core matrices adjacent in K are 128 B apart (the descriptor's leading byte offset) and the
-// 8-row groups SBO apart (its stride byte offset).  The MMA of K-slice s (16 elements) starts
-// at byte 256 s.
+// Input layer.  A bfloat16 coordinate carries 8 significant bits, coarser than a cell of a
+// long grid (1536 cells over the normalised range [-1, 1] are 0.0013 wide; bfloat16's spacing
+// near 1 is 0.0078).  The bfloat16 form therefore feeds each normalised coordinate as a pair
+// hi = bf16(x), lo = bf16(x - hi) (16 significant bits) in K columns 0-2 and 3-5 of the
+// first layer, whose weight image repeats W1 in both column groups: W1 (hi + lo) is summed in
+// the FP32 accumulator.  The half-precision form feeds x, y, z once (11 significant bits).
+//
+// Shared-memory operands use the K-major core-matrix layout of fdf_tc.cuh.
 //
 // Every wait on an mbarrier is bounded: past the limit the CTA records ERRBIT_TC_TIMEOUT,
 // frees its tensor memory and returns.
 #include "fdf_internal.cuh"
 #include "fdf_mlp.cuh"
+#include "fdf_tc.cuh"
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 namespace {
+
+using namespace fdftc;
 
 constexpr int TC_ROWS = 128;                 // particles per tile (MMA M)
 constexpr int TC_PIPES = 4;                  // warpgroups per CTA, one tile pipeline each
@@ -40,131 +44,54 @@ constexpr int SM_W4 = SM_W3 + 32768;         // [16][128]  4096
 constexpr int SM_PIPE = SM_W4 + 4096;        // per pipeline: A1 [128][16] 4096, A [128][128] 32768
 constexpr int PIPE_BYTES = 4096 + 32768;
 constexpr int SM_BIAS = SM_PIPE + TC_PIPES * PIPE_BYTES;   // 392 floats
-constexpr int SM_HB2 = SM_BIAS + 1568;       // the hidden half-biases as 192 half2 pairs
+constexpr int SM_HB2 = SM_BIAS + 1568;       // the hidden half-biases as 192 16-bit pairs
 constexpr int SM_BAR = SM_HB2 + 768;         // mbarriers (8 B each), TMEM base (4 B), time-out flags
 constexpr int SM_TOTAL = SM_BAR + 8 * TC_PIPES + 8 + 4 * TC_PIPES;
 constexpr int WIMG_BYTES = SM_PIPE;          // packed weight image in global memory (73,728 B)
 constexpr unsigned long long WAIT_LIMIT = 1ull << 22;
 
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-
-// Shared-memory matrix descriptor: start address, leading (K) and stride (8-row) byte
-// offsets, descriptor version 1, no swizzle.
-__device__ __forceinline__ unsigned long long make_desc(unsigned addr, unsigned lbo, unsigned sbo) {
-  return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)(lbo >> 4) << 16) |
-         ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46);
-}
-
-// Instruction descriptor of kind::f16: FP32 accumulator, half-precision A and B (format 0 for
-// both), both K-major.
-__host__ __device__ constexpr unsigned make_idesc(int M, int N) {
-  return (1u << 4) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_f16(unsigned tmem_d, unsigned long long adesc, unsigned long long bdesc,
-                                        unsigned idesc, unsigned accumulate) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-      :
-      : "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(unsigned bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
-  unsigned ok;
-  asm volatile(
-      "{\n.reg .pred P1;\nmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\nselp.b32 %0, 1, 0, P1;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(phase)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ void fence_before_sync() {
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-}
-__device__ __forceinline__ void fence_after_sync() {
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-}
-__device__ __forceinline__ void fence_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-}
-
-// Issues the load of 16 consecutive FP32 accumulator columns of this thread's TMEM lane; r is
-// undefined until tmem_wait_ld(r).
-__device__ __forceinline__ void tmem_ld16_issue(unsigned taddr, unsigned (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
-
-// Waits for this thread's outstanding tcgen05.ld; r passes through the wait so that the compiler
-// schedules no use of it before.
-__device__ __forceinline__ void tmem_wait_ld(unsigned (&r)[16]) {
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n"
-               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
-                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
-                 "+r"(r[15])
-               :
-               : "memory");
-}
-
-// 16 consecutive FP32 accumulator columns of this thread's TMEM lane.
-__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
-  unsigned r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
-}
-
+// Two FP32 values rounded to a 16-bit pair, lo in the low half.
+template <bool BF16>
 __device__ __forceinline__ unsigned pack2(float lo, float hi) {
-  __half2 v = __floats2half2_rn(lo, hi);
-  return *reinterpret_cast<unsigned *>(&v);
+  unsigned v;
+  if constexpr (BF16) asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(v) : "f"(hi), "f"(lo));
+  else asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(v) : "f"(hi), "f"(lo));
+  return v;
 }
 
 // SiLU(z) = z * sigmoid(z) = h + h * tanh(h) with h = z / 2, on a pair of columns in packed
-// half precision: the accumulator pair v rounded to half2, h = v/2 + hb (hb: the half-bias
-// pair), one tanh.approx.f16x2, h + h t -- four instructions per pair.  The epilogue is bound by
-// instruction issue, so this halves its cost against the FP32 form of the same formula.  The
-// pair is the next layer's half-precision A operand as it stands.
-__device__ __forceinline__ unsigned silu2_h2(unsigned v01, __half2 hb) {
-  const __half2 h = __hfma2(*reinterpret_cast<const __half2 *>(&v01), __float2half2_rn(0.5f), hb);
-  unsigned t;
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const unsigned *>(&h)));
-  const __half2 s = __hfma2(h, *reinterpret_cast<const __half2 *>(&t), h);
-  return *reinterpret_cast<const unsigned *>(&s);
+// 16-bit arithmetic: the accumulator pair v01 rounded to the operand type, h = v/2 + hb (hb:
+// the half-bias pair), one tanh.approx of the pair, h + h t -- four instructions per pair.
+// The epilogue is bound by instruction issue, so this halves its cost against the FP32 form
+// of the same formula.  The pair is the next layer's A operand as it stands.
+template <bool BF16>
+__device__ __forceinline__ unsigned silu2(unsigned v01, unsigned hb) {
+  unsigned h, t, s;
+  if constexpr (BF16) {
+    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(h) : "r"(v01), "r"(0x3F003F00u), "r"(hb));   // 0.5 in both halves
+    asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(s) : "r"(h), "r"(t), "r"(h));
+  } else {
+    asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(h) : "r"(v01), "r"(0x38003800u), "r"(hb));
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(s) : "r"(h), "r"(t), "r"(h));
+  }
+  return s;
 }
 
-// byte offset of element (r, k) in the operand layout with SBO = sbo
-__host__ __device__ constexpr unsigned op_off(int r, int k, unsigned sbo) {
-  return (unsigned)(r / 8) * sbo + (unsigned)(k / 8) * 128u + (unsigned)(r % 8) * 16u + (unsigned)(k % 8) * 2u;
-}
-
-// Packs the FP32 parameters into the shared-memory image of the weights (half precision).
-__global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__restrict__ img) {
+// Packs the FP32 parameters into the shared-memory image of the weights (bfloat16 or half
+// precision); the bfloat16 image repeats W1 in K columns 3-5 for the inputs' low parts.
+__global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__restrict__ img, int bf16) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;   // one 16-bit element of the image
   if (q >= WIMG_BYTES / 2) return;
   const int byte = 2 * q;
   float v = 0.f;
-  if (byte < SM_W2) {                                   // W1 [128][16], K padded from 3
+  if (byte < SM_W2) {                                   // W1 [128][16], K padded from 3 (or 6)
     const int o = byte - SM_W1;
     const int rg = o / 256, kc = (o % 256) / 128, rr = (o % 128) / 16, kk = (o % 16) / 2;
     const int n = rg * 8 + rr, k = kc * 8 + kk;
     if (k < 3) v = params[MLP_OFF_W1 + n * 3 + k];
+    else if (bf16 && k < 6) v = params[MLP_OFF_W1 + n * 3 + k - 3];
   } else if (byte < SM_W4) {                            // W2, W3 [128][128]
     const bool second = byte >= SM_W3;
     const int o = byte - (second ? SM_W3 : SM_W2);
@@ -177,7 +104,15 @@ __global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__res
     const int n = rg * 8 + rr, k = kc * 8 + kk;
     if (n < 3) v = params[MLP_OFF_W4 + n * 128 + k];
   }
-  reinterpret_cast<__half *>(img)[q] = __float2half_rn(v);
+  unsigned short bits;
+  if (bf16) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    bits = *reinterpret_cast<const unsigned short *>(&b);
+  } else {
+    const __half h = __float2half_rn(v);
+    bits = *reinterpret_cast<const unsigned short *>(&h);
+  }
+  reinterpret_cast<unsigned short *>(img)[q] = bits;
 }
 
 __device__ __forceinline__ float load_coord(const double *a, unsigned int r, int pairs) {
@@ -188,6 +123,7 @@ __device__ __forceinline__ float load_coord(const double *a, unsigned int r, int
   return (float)a[r];
 }
 
+template <bool BF16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_mlp_guess_tc(const unsigned char *__restrict__ wimg, const float *__restrict__ bias_g, MlpNorm norm,
                    const double *__restrict__ px, const double *__restrict__ py, const double *__restrict__ pz,
@@ -198,7 +134,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int tid = threadIdx.x, warp = tid >> 5;
   const int pipe = tid >> 7, row = tid & 127;     // warpgroup = pipeline; thread = tile row
   float *bias = reinterpret_cast<float *>(smem + SM_BIAS);
-  __half2 *hb2 = reinterpret_cast<__half2 *>(smem + SM_HB2);
+  unsigned *hb2 = reinterpret_cast<unsigned *>(smem + SM_HB2);
   unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + SM_BAR);
   unsigned *tmem_slot = reinterpret_cast<unsigned *>(smem + SM_BAR + 8 * TC_PIPES);
   volatile unsigned *tflag = reinterpret_cast<volatile unsigned *>(smem + SM_BAR + 8 * TC_PIPES + 8);
@@ -209,7 +145,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     uint4 *dst = reinterpret_cast<uint4 *>(smem);
     for (int q = tid; q < WIMG_BYTES / 16; q += TC_THREADS) dst[q] = src[q];
     for (int q = tid; q < MLP_BIAS_WORDS; q += TC_THREADS) bias[q] = bias_g[q];
-    for (int q = tid; q < 192; q += TC_THREADS) hb2[q] = __floats2half2_rn(bias_g[2 * q], bias_g[2 * q + 1]);
+    for (int q = tid; q < 192; q += TC_THREADS) hb2[q] = pack2<BF16>(bias_g[2 * q], bias_g[2 * q + 1]);
     uint4 *a1 = reinterpret_cast<uint4 *>(a1s);
     for (int q = row; q < 4096 / 16; q += 128) a1[q] = make_uint4(0, 0, 0, 0);
   }
@@ -232,7 +168,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const unsigned tmem = *tmem_slot + (unsigned)(128 * pipe);
   const unsigned lane_base = (unsigned)((warp & 3) * 32) << 16;
   const unsigned sbase = smem_u32(smem), a1_addr = smem_u32(a1s), a_addr = smem_u32(as);
-  const unsigned id_hidden = make_idesc(TC_ROWS, 128), id_out = make_idesc(TC_ROWS, 16);
+  const unsigned id_hidden = make_idesc(TC_ROWS, 128, BF16), id_out = make_idesc(TC_ROWS, 16, BF16);
   const unsigned pipe_bar = 1 + pipe;   // named barrier of this warpgroup (0 is __syncthreads)
 
   const long long n = list_count ? (long long)*list_count : (long long)n_host;
@@ -255,20 +191,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   };
   // bias + SiLU of the 128 accumulator columns (b: half-biases), stored as the next layer's A operand
   // (the next chunk's TMEM load is in flight while a chunk is converted)
-  auto chunk = [&](const unsigned (&r)[16], const __half2 *b, int c) {
+  auto chunk = [&](const unsigned (&r)[16], const unsigned *b, int c) {
     unsigned w[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      unsigned v01;
-      asm("cvt.rn.f16x2.f32 %0, %1, %2;"   // column 2q in the low half
-          : "=r"(v01)
-          : "f"(__uint_as_float(r[2 * q + 1])), "f"(__uint_as_float(r[2 * q])));
-      w[q] = silu2_h2(v01, b[8 * c + q]);
-    }
+    for (int q = 0; q < 8; ++q)
+      w[q] = silu2<BF16>(pack2<BF16>(__uint_as_float(r[2 * q]), __uint_as_float(r[2 * q + 1])), b[8 * c + q]);
     *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
     *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
   };
-  auto epilogue = [&](const __half2 *b) {
+  auto epilogue = [&](const unsigned *b) {
     unsigned ra[16], rb[16];
     tmem_ld16_issue(tmem + lane_base, ra);
     tmem_wait_ld(ra);
@@ -318,7 +249,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll 1
   for (long long tile = tile0; tile < ntiles; tile += tstride) {
     const long long r = tile * TC_ROWS + row;
-    *reinterpret_cast<uint4 *>(a1s + op_off(row, 0, 256)) = make_uint4(pack2(cx, cy), pack2(cz, 0.f), 0u, 0u);
+    if constexpr (BF16) {   // hi parts in K columns 0-2, lo parts in 3-5
+      const float hx = __bfloat162float(__float2bfloat16_rn(cx)), hy = __bfloat162float(__float2bfloat16_rn(cy)),
+                  hz = __bfloat162float(__float2bfloat16_rn(cz));
+      *reinterpret_cast<uint4 *>(a1s + op_off(row, 0, 256)) =
+          make_uint4(pack2<true>(hx, hy), pack2<true>(hz, cx - hx), pack2<true>(cy - hy, cz - hz), 0u);
+    } else {
+      *reinterpret_cast<uint4 *>(a1s + op_off(row, 0, 256)) =
+          make_uint4(pack2<false>(cx, cy), pack2<false>(cz, 0.f), 0u, 0u);
+    }
     // stall_test (tests of the time-out path only): nothing is issued or committed, so the wait
     // below runs out with no MMA in flight
     if (!stall_test) issue(0);
@@ -366,19 +305,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 size_t mlp_tc_image_bytes() { return WIMG_BYTES; }
 
-void mlp_pack_tc(const float *params, unsigned char *img, cudaStream_t s) {
-  k_pack_tc<<<(WIMG_BYTES / 2 + 255) / 256, 256, 0, s>>>(params, img);
+void mlp_pack_tc(const float *params, unsigned char *img, int bf16, cudaStream_t s) {
+  k_pack_tc<<<(WIMG_BYTES / 2 + 255) / 256, 256, 0, s>>>(params, img, bf16);
 }
 
-void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &norm, const double *x, const double *y,
-                  const double *z, int pairs, const unsigned int *list, const unsigned long long *list_count,
-                  int n_host, int n_cap, GridDims g, int *guess, int num_sms, unsigned int *err, cudaStream_t s,
-                  float *yout, int stall_test) {
+void mlp_guess_tc(const unsigned char *img, int bf16, const float *bias, const MlpNorm &norm, const double *x,
+                  const double *y, const double *z, int pairs, const unsigned int *list,
+                  const unsigned long long *list_count, int n_host, int n_cap, GridDims g, int *guess, int num_sms,
+                  unsigned int *err, cudaStream_t s, float *yout, int stall_test) {
   static int attr_device = -1;
   int dev = 0;
   cudaGetDevice(&dev);
   if (attr_device != dev) {
-    cudaFuncSetAttribute(k_mlp_guess_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
+    cudaFuncSetAttribute(k_mlp_guess_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
+    cudaFuncSetAttribute(k_mlp_guess_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
     attr_device = dev;
   }
   const long long tiles = ((long long)n_cap + TC_ROWS - 1) / TC_ROWS;
@@ -386,7 +326,13 @@ void mlp_guess_tc(const unsigned char *img, const float *bias, const MlpNorm &no
   const long long cap_blocks = (long long)num_sms;
   if (blocks > cap_blocks) blocks = cap_blocks;
   if (blocks < 1) blocks = 1;
-  k_mlp_guess_tc<<<(unsigned)blocks, TC_THREADS, SM_TOTAL, s>>>(img, bias, norm, x, y, z, pairs, list, list_count,
-                                                                 n_host, g, guess, yout, err,
-                                                                 stall_test ? 1024ull : WAIT_LIMIT, stall_test);
+  const unsigned long long limit = stall_test ? 1024ull : WAIT_LIMIT;
+  if (bf16)
+    k_mlp_guess_tc<true><<<(unsigned)blocks, TC_THREADS, SM_TOTAL, s>>>(img, bias, norm, x, y, z, pairs, list,
+                                                                        list_count, n_host, g, guess, yout, err,
+                                                                        limit, stall_test);
+  else
+    k_mlp_guess_tc<false><<<(unsigned)blocks, TC_THREADS, SM_TOTAL, s>>>(img, bias, norm, x, y, z, pairs, list,
+                                                                         list_count, n_host, g, guess, yout, err,
+                                                                         limit, stall_test);
 }

@@ -27,8 +27,7 @@
 // undecided faces are computed from x itself (EXACT), so every class is x's own.
 //
 // Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32, negative for a degenerate
-// cell), c0l (3 x f32), overlap margin (f32, cell_margin in fdf_fp32.cu), then per face
-// LEFT..BACK: fcr (3 x f32), n32 (3 x f32).
+// cell), c0l (3 x f32), a zero, then per face LEFT..BACK: fcr (3 x f32), n32 (3 x f32).
 #pragma once
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
@@ -54,8 +53,7 @@ __device__ __forceinline__ double exact_face(const double *__restrict__ row64, i
 // The exact distance out of line: the face the FP32 bound cannot decide is rare (about 1e-5
 // per particle-step), and kept inline the compiler if-converts it, so every face of every
 // evaluation issues its FP64 instructions predicated off (the FP32 walk: 3.91 -> 3.65 ms per
-// 64M-particle step out of line).  The certified evaluation of the walk from a learned guess
-// keeps it inline: there the call's saved registers cost more (1.18 -> 1.34 ms).
+// 64M-particle step out of line).
 static __device__ __noinline__ double exact_face_call(const double *__restrict__ row64, int f, double x, double y,
                                                       double z) {
   return exact_face(row64, f, x, y, z);
@@ -65,21 +63,19 @@ static __device__ __noinline__ double exact_face_pair(const double *__restrict__
   return exact_face(row64, f, pair_value(px), pair_value(py), pair_value(pz));
 }
 
-// One cell evaluated for the form's position: the face classes the walk needs, the
-// distances the weights use, and (CERT) whether every face is positive by more than
-// thr + the cell's overlap margin, which the FP32 bound certifies without FP64.
+// One cell evaluated for the form's position: the face classes the walk needs and the
+// distances the weights use.
 struct Eval32 {
   unsigned int neg;   // bit f: face f negative
   bool zero;          // some face within its threshold
   bool degenerate;
-  bool clear;
   float dv[6];
 };
 
 // EXACT: the position is the FP64 (xe, ye, ze) and the pairs are its split (hi = fl32(x),
 // lo = fl32(x - hi), within 2^-48 |x| of it, which the margin's slack covers); the faces the
 // FP32 bound cannot decide are then computed from the FP64 position itself.
-template <bool CERT, bool EXACT = false>
+template <bool EXACT = false>
 __device__ __forceinline__ void eval_cell32(const float *__restrict__ table, const double *__restrict__ planes,
                                             long long cur, float2 px, float2 py, float2 pz, float sx, float sy,
                                             float sz, Eval32 &e, unsigned int &fb, double xe = 0.0,
@@ -88,7 +84,6 @@ __device__ __forceinline__ void eval_cell32(const float *__restrict__ table, con
   const float4 h0 = __ldg(row), h1 = __ldg(row + 1);
   e.neg = 0u;
   e.zero = false;
-  e.clear = CERT;
   e.degenerate = (__float_as_uint(h0.w) >> 31) != 0u;
   if (e.degenerate) return;
   const float thr32 = h0.w;
@@ -117,19 +112,15 @@ __device__ __forceinline__ void eval_cell32(const float *__restrict__ table, con
     const float M = __fadd_rn(__fmul_rn(S, 12.0f * 5.9604644775390625e-8f), thr32);
     if (d32 > M) {
       e.dv[f] = d32;
-      if (CERT) e.clear = e.clear && d32 > __fadd_ru(M, h1.w);
     } else if (d32 < -M) {
       e.neg |= 1u << f;
       e.dv[f] = d32;
-      if (CERT) e.clear = false;
     } else {
-      const double d64 = EXACT  ? exact_face_call(planes + cur * FDF_ROW, f, xe, ye, ze)
-                         : CERT ? exact_face(planes + cur * FDF_ROW, f, pair_value(px), pair_value(py), pair_value(pz))
-                                : exact_face_pair(planes + cur * FDF_ROW, f, px, py, pz);
+      const double d64 = EXACT ? exact_face_call(planes + cur * FDF_ROW, f, xe, ye, ze)
+                               : exact_face_pair(planes + cur * FDF_ROW, f, px, py, pz);
       if (fdfx::lt0(d64)) e.neg |= 1u << f;
       e.zero = e.zero || fdfx::eq0(d64);
       e.dv[f] = fdfx::d2f_rn(d64);
-      if (CERT) e.clear = false;
       ++fb;
     }
   }
@@ -145,13 +136,21 @@ struct Walk32 {
   Eval32 e;
 };
 
-template <bool EXACT = false>
+// The cell a walk from (i0, j0, k0) toward (ti, tj, tk) reaches after q steps if every step moves
+// each index one closer (the reference's steps move each index by at most one).
+__device__ __forceinline__ int path_index(int a0, int t, int q) { return a0 + max(-q, min(q, t - a0)); }
+
+// TRACK: counts in *hits the evaluations after the first whose cell is the one the predicted
+// path from the start toward (ti, tj, tk) reaches after as many steps (the rows fetched ahead).
+template <bool EXACT = false, bool TRACK = false>
 __device__ __forceinline__ void walk_ref32(const float *__restrict__ table, const double *__restrict__ planes,
                                            const GridDims &g, float2 px, float2 py, float2 pz, int limit, Walk32 &w,
-                                           unsigned int &fb, double xe = 0.0, double ye = 0.0, double ze = 0.0) {
+                                           unsigned int &fb, double xe = 0.0, double ye = 0.0, double ze = 0.0,
+                                           int ti = 0, int tj = 0, int tk = 0, unsigned int *hits = nullptr) {
   const float sx = fabsf(px.x), sy = fabsf(py.x), sz = fabsf(pz.x);
   long long saved = -1;
   int power = 1, lam = 0;
+  const int i0 = w.i, j0 = w.j, k0 = w.k;
   w.steps = 0; w.evaluated = 0;
   w.concluded = false; w.lost = false; w.cycle = false;
   while (!w.concluded && w.steps < limit) {
@@ -160,7 +159,11 @@ __device__ __forceinline__ void walk_ref32(const float *__restrict__ table, cons
     const long long cur = ((long long)w.k * g.JM + w.j) * g.IM + w.i;
     if (cur == saved) { w.cycle = true; w.lost = true; break; }
     if (++lam == power) { saved = cur; power <<= 1; lam = 0; }
-    eval_cell32<false, EXACT>(table, planes, cur, px, py, pz, sx, sy, sz, w.e, fb, xe, ye, ze);
+    if (TRACK && w.steps > 1) {
+      const int q = w.steps - 1;
+      *hits += (w.i == path_index(i0, ti, q) && w.j == path_index(j0, tj, q) && w.k == path_index(k0, tk, q)) ? 1u : 0u;
+    }
+    eval_cell32<EXACT>(table, planes, cur, px, py, pz, sx, sy, sz, w.e, fb, xe, ye, ze);
     if (w.e.degenerate) { w.err |= ERRBIT_DEGENERATE; w.lost = true; break; }
     ++w.evaluated;
     if (!w.e.neg || w.e.zero) {

@@ -70,16 +70,15 @@ typedef struct {
  * with a rigorous error bound, exact FP64 distance where the bound cannot decide). */
 #define FDF_FORM_PLAIN_FP64 0
 #define FDF_FORM_FP32 1
-/* LEARNED_FP32: the FP32 form whose walk, for a particle that has left its previous cell,
- * starts in the cell a trained network predicts (fdf_Locator*).  The walk from the guess
- * is kept only when it ends with every face of its cell positive by more than the
- * threshold plus the cell's overlap margin (the largest gap between the cell's face planes
- * and the planes of the same grid surfaces on the neighbouring patches), within
- * FDF_GUESS_REACH = 16 cells of the previous cell in each index; otherwise the reference
- * walk from the previous cell decides.  Particles that stay within about two cells of their
- * previous cell skip the network (fdf_LocatorSetMinDistance).  Cells, weights and statuses are
- * then those of the FP32 form except where the reference's own result depends on where its
- * walk starts. */
+/* LEARNED_FP32: the FP32 form with a trained network (fdf_Locator*) in its walk.  After the
+ * reference's first evaluation (in the previous cell), a particle estimated at least two cells
+ * away (fdf_LocatorSetMinDistance) gets a predicted cell from the network, and the reference
+ * walk continues from its second cell P1 with the plane-table rows of the path from P1 toward
+ * the predicted cell fetched ahead of its evaluations.  The walk itself is the reference's, so
+ * cells, weights and statuses are the FP32 form's for every input, whatever the network
+ * predicts: a walk that started at the prediction could end elsewhere, because the reference
+ * accepts any cell whose extended face plane passes within 1e-11 h of the point
+ * (walkingsearch.c:427-459), and which such cell it meets depends on its path. */
 #define FDF_FORM_LEARNED_FP32 2
 
 /* ---- context, grid and fields (replace UserCtx set-up: setup.c:197-290, grid.c:34-160) ---- */
@@ -276,8 +275,9 @@ int fdf_SortByCellNoAlloc(const int32_t *cell_ids, int64_t n, int64_t ncells, ui
  * (walkingsearch.c:571-626).  A 3-128-128-128-3 SiLU network maps the normalised position
  * xhat = (x - centre) * inv_half (centre and half-extent of the grid's bounding box) to
  * y, read as cell index floor((y_d + 1) N_d / 2), N = (IM, JM, KM), clamped to the grid.
- * Weights are bfloat16 in every training product and half precision in inference (FP32
- * accumulation in both), with FP32 master copies for training.  Parameters, one float vector of FDF_LOCATOR_NPARAM values:
+ * Weights are bfloat16 in every training product and, by default, in inference (FP32
+ * accumulation in both; fdf_LocatorSetInferenceType), with FP32 master copies for training.
+ * Parameters, one float vector of FDF_LOCATOR_NPARAM values:
  * W1 [128][3], b1 [128], W2 [128][128], b2, W3 [128][128], b3, W4 [3][128], b4 [3]. */
 #define FDF_LOCATOR_NPARAM 33923
 /* Weights uniform in +-1/sqrt(fan_in) from the seed, biases zero; Adam state cleared. */
@@ -299,17 +299,22 @@ int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target
                          float *loss);
 /* Predicted cells (i, j, k) of n host positions [n][3]; outputs (optional) [n][3] = y. */
 int fdf_LocatorPredict(FdfContext *ctx, const double *position, int64_t n, int64_t *cell_id, float *outputs);
+/* Operand type of inference on the tensor cores: FDF_LOCATOR_BF16 (default; each normalised
+ * coordinate enters as a bfloat16 pair hi + lo) or FDF_LOCATOR_F16 (half precision).  Only the
+ * predictions, never the cells, depend on it. */
+#define FDF_LOCATOR_BF16 0
+#define FDF_LOCATOR_F16 1
+int fdf_LocatorSetInferenceType(FdfContext *ctx, int type);
 /* Which particles the learned form asks the network: after the reference's first evaluation
  * (in the previous cell), a particle estimated at least `cells` cells past that cell (from the
- * evaluation's face distances) gets a guess; a nearer one continues the reference walk at once.
- * Default 2.0 (nearer particles cost more walk evaluations from a guess than from their previous
- * cell); 0 asks for every particle that left its cell.  Results do not depend on it. */
+ * evaluation's face distances) gets a prediction and is walked from P1 in a second pass; a
+ * nearer one continues the reference walk at once.  Default 2.0; 0 asks for every particle
+ * that left its cell.  Results do not depend on it. */
 int fdf_LocatorSetMinDistance(FdfContext *ctx, double cells);
-/* Running totals of the learned form: particles given a guess, guesses whose walk was
- * kept, evaluations made by the walks from the guesses, and by the reference walks that
- * finished the guesses not kept. */
-int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *taken, int64_t *guess_evals,
-                        int64_t *fallback_evals);
+/* Running totals of the learned form: particles given a prediction (asked); evaluations of their
+ * walks from P1 whose cell lay on the predicted path, i.e. whose row was fetched ahead (on_path);
+ * evaluations of those walks (walk_evals); and zero (unused). */
+int fdf_LocatorGetStats(FdfContext *ctx, int64_t *asked, int64_t *on_path, int64_t *walk_evals, int64_t *unused);
 
 /* ---- the reference's on-disk formats (host-side; no GPU work except the swarm transfers) ----
  * FDFGRID grid file (io.c:101-170 ReadGridFile, grid.c:356-383 AssignGridCoordinates): an

@@ -12,8 +12,11 @@ network is defined by this build:
     loss = mean over samples of sum_d (s_d (y_d - t_d))^2 / 3,  s_d = N_d / 2   (cell units)
 
 The GPU rounds GEMM operands to bfloat16 and accumulates in FP32; `forward` and
-`backward` here round at the same points (bf16=True) so the two can be compared
-closely, and without rounding (bf16=False, FP64) for the finite-difference check.
+`backward` here round at the same points (use_bf16=True) so the two can be compared
+closely, and without rounding (use_bf16=False, FP64) for the finite-difference check.
+A bfloat16 input coordinate enters as the pair hi = bf16(x), lo = bf16(x - hi) (its value
+hi + lo has 16 significant bits); `forward(..., f16=True)` rounds inputs, weights and
+activations to half precision instead (the locator's half-precision inference).
 """
 from __future__ import annotations
 
@@ -32,6 +35,18 @@ def bf16(x: np.ndarray) -> np.ndarray:
     out = r.astype(np.uint32).view(np.float32).astype(np.float64)
     out[nan] = np.nan
     return out
+
+
+def f16(x: np.ndarray) -> np.ndarray:
+    """Round to IEEE half precision (nearest even) and return as float64."""
+    return np.asarray(x, dtype=np.float64).astype(np.float16).astype(np.float64)
+
+
+def split_bf16(x: np.ndarray) -> np.ndarray:
+    """hi + lo with hi = bf16(x), lo = bf16(x - hi), x taken as float32 (the network's input pair)."""
+    x32 = np.asarray(x, dtype=np.float32).astype(np.float64)
+    hi = bf16(x32)
+    return hi + bf16(x32 - hi)
 
 
 def silu(z):
@@ -64,9 +79,14 @@ def targets(cells, dims):
     return 2.0 * (np.asarray(cells, dtype=np.float64) + 0.5) / N - 1.0
 
 
-def forward(params, xhat, use_bf16: bool = True):
-    r = bf16 if use_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
-    cache = {"h0": r(xhat)}
+def forward(params, xhat, use_bf16: bool = True, f16: bool = False):
+    if f16:
+        r, r_in = globals()["f16"], globals()["f16"]
+    elif use_bf16:
+        r, r_in = bf16, split_bf16
+    else:
+        r = r_in = (lambda a: np.asarray(a, dtype=np.float64))
+    cache = {"h0": r_in(xhat)}
     h = cache["h0"]
     for L in range(3):
         W, b = params[L]

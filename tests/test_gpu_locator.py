@@ -4,8 +4,9 @@
 * Gradients of the tensor-core forward/backward kernels match the oracle's backward
   with the same bfloat16 rounding points (relative L2 error per block <= 5e-3), and
   match it far more closely than they match the unrounded FP64 gradient.
-* Inference (fused kernel, SiLU by tanh.approx) matches the oracle's bfloat16 forward to
-  0.02 (outputs are O(1)), and its cells are floor((y + 1) N / 2) of its outputs.
+* Inference (fused kernel, SiLU by tanh.approx) matches the oracle's forward with the same
+  operand type (bfloat16 by default, half precision on request) to a few units in the last
+  place of the type, and its cells are floor((y + 1) N / 2) of its outputs.
 * Training on walk-produced pairs is deterministic and reduces the loss.
 * The learned form gives the FP32 form's swarm, fields and deposits bit for bit, with a
   trained and with an untrained network, with either guess policy, and the trained network
@@ -15,7 +16,7 @@ import numpy as np
 import pytest
 
 from fdf_gb300 import workloads as W
-from fdf_gb300.context import FORM_FP32, FORM_LEARNED_FP32, LOCATOR_NPARAM, PicContext
+from fdf_gb300.context import FORM_FP32, FORM_LEARNED_FP32, LOCATOR_BF16, LOCATOR_F16, LOCATOR_NPARAM, PicContext
 from oracle import mlp_oracle as M
 
 pytestmark = pytest.mark.gpu
@@ -23,6 +24,9 @@ pytestmark = pytest.mark.gpu
 OFFS = [(0, 384), (384, 512), (512, 16896), (16896, 17024), (17024, 33408), (33408, 33536), (33536, 33920),
         (33920, 33923)]
 NAMES = ["W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4"]
+# (max, mean) |y - y_oracle| of inference by operand type, outputs |y| <= 0.44 here; measured
+# on GB300: bfloat16 7.4e-4 / 1.5e-4, half 9.6e-5 / 1.9e-5
+PREDICT_TOL = {"bf16": (3e-3, 6e-4), "f16": (5e-4, 1e-4)}
 
 
 def flat(params):
@@ -82,19 +86,30 @@ def test_gradients_match_oracle(small):
             assert e_ref <= 0.3 * e_exact, (name, e_ref, e_exact)
 
 
-def test_predict_matches_oracle_forward(small):
+@pytest.mark.parametrize("kind", ["bf16", "f16"])
+def test_predict_matches_oracle_forward(small, kind):
+    """Inference against the oracle's forward with the kernel's operand type (bfloat16: input
+    pairs, bfloat16 weights and activations; half: all in half precision).  The kernel rounds
+    the SiLU's intermediate values to the operand type as well (h = z/2 + b/2, tanh.approx,
+    h + h tanh(h)), so it differs from the oracle's single rounding per activation by a few
+    units in the last place of the type: bfloat16 keeps 8 significant bits, half 11."""
     ctx, wl = small
     rng = np.random.default_rng(5)
     params = [(W_, (0.2 * rng.standard_normal(b.shape)).astype(np.float32)) for W_, b in M.init_params(seed=6)]
     ctx.locator_set_params(flat(params))
-    pos, _ = W.volumetric_particles(wl.coor, 5000, seed=9)
-    cells, y = ctx.locator_predict(pos)
+    ctx.locator_inference_type(LOCATOR_BF16 if kind == "bf16" else LOCATOR_F16)
+    try:
+        pos, _ = W.volumetric_particles(wl.coor, 5000, seed=9)
+        cells, y = ctx.locator_predict(pos)
+    finally:
+        ctx.locator_inference_type(LOCATOR_BF16)
     c, ih = ctx.locator_normalization()
     xhat = (pos.astype(np.float32) - c) * ih
-    y_ref, _ = M.forward(params, xhat.astype(np.float64), use_bf16=True)
+    y_ref, _ = M.forward(params, xhat.astype(np.float64), use_bf16=True, f16=(kind == "f16"))
     err = np.abs(y.astype(np.float64) - y_ref)
-    print(f"[predict] max |dy| {err.max():.3e} mean {err.mean():.3e} (|y| max {np.abs(y_ref).max():.2f})")
-    assert err.max() <= 0.02 and err.mean() <= 2e-3
+    print(f"[predict {kind}] max |dy| {err.max():.3e} mean {err.mean():.3e} (|y| max {np.abs(y_ref).max():.2f})")
+    tol_max, tol_mean = PREDICT_TOL[kind]
+    assert err.max() <= tol_max and err.mean() <= tol_mean
     N = np.array(wl.dims, dtype=np.float32)
     want = np.clip(np.floor((y + np.float32(1.0)) * np.float32(0.5) * N), 0, N - 1).astype(np.int64)
     assert np.array_equal(cells, want)
@@ -176,20 +191,20 @@ def test_learned_form_identical_to_fp32_form(pipe_runs):
         _same(r["fp32"], r[key])
 
 
-def test_trained_locator_shortens_walk(pipe_runs):
-    """Asking the network for every particle that left its cell: the trained network needs far
-    fewer walk evaluations than the untrained one; the default policy asks only for particles
-    two cells or more away and makes fewer walk evaluations than the FP32 form's walk."""
+def test_trained_locator_predicts_the_walk(pipe_runs):
+    """The learned form's walk is the reference's, so every form makes the FP32 form's walk
+    evaluations whatever the network; what the network gains is the path of the walk from P1 known
+    ahead, its rows fetched before the walk reaches them.  With the trained network far more of
+    those walks' evaluations lie on the predicted path than with an untrained one."""
     _, r = pipe_runs
-    ps = r["fp32"][3]
-    e = {k: r[k][4] / ps for k in ("fp32", "learned", "learned_all", "untrained")}
-    st = {k: r[k][5] for k in ("learned", "learned_all", "untrained")}
-    print("[gain] walk evaluations per particle-step: " + ", ".join(f"{k} {v:.3f}" for k, v in e.items()))
-    for k, (asked, taken, gev, _) in st.items():
-        print(f"[gain] {k}: guesses {asked}, kept {taken / max(asked, 1):.3f}, "
-              f"evaluations per guess {gev / max(asked, 1):.2f}")
-    asked, taken, _, _ = st["learned_all"]
-    assert taken > 0.5 * asked
-    assert e["learned_all"] < e["untrained"]
-    assert st["learned"][0] < st["learned_all"][0]
-    assert e["learned"] < e["fp32"]
+    ev = {k: r[k][4] for k in ("fp32", "learned", "learned_all", "untrained")}
+    assert len(set(ev.values())) == 1, ev
+    frac = {}
+    for k in ("learned", "learned_all", "untrained"):
+        asked, on_path, walk_evals, unused = r[k][5]
+        frac[k] = on_path / max(walk_evals - asked, 1)   # evaluations after P1's
+        print(f"[gain] {k}: walks from P1 {asked}, evaluations {walk_evals}, on the predicted path {on_path} "
+              f"({frac[k]:.3f} of those after P1)")
+        assert unused == 0
+    assert frac["learned_all"] > 0.3 and frac["learned_all"] > 2.0 * frac["untrained"]
+    assert r["learned"][5][0] < r["learned_all"][5][0]   # the default policy asks fewer particles

@@ -69,3 +69,16 @@ def test_bf16_backward_close_to_exact():
     for (dWe, dbe), (dWr, dbr) in zip(exact, rounded):
         assert np.linalg.norm(dWr - dWe) <= 0.05 * np.linalg.norm(dWe)
         assert np.linalg.norm(dbr - dbe) <= 0.05 * np.linalg.norm(dbe) + 1e-12
+
+
+def test_input_pair_and_half_rounding():
+    """The bfloat16 input pair carries 16 significant bits; f16 rounds to half precision."""
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-1, 1, 10000).astype(np.float32)
+    pair = M.split_bf16(x)
+    rel = np.abs(pair - x.astype(np.float64)) / np.abs(x.astype(np.float64))
+    assert rel.max() <= 2.0 ** -16
+    alone = np.abs(M.bf16(x) - x) / np.abs(x.astype(np.float64))
+    assert alone.max() > 2.0 ** -10                              # bfloat16 alone: 8 significant bits
+    assert np.array_equal(M.f16(x), x.astype(np.float16).astype(np.float64))
+    assert np.abs(M.f16(x) - x).max() <= 2.0 ** -12
