@@ -35,7 +35,7 @@ UNIT = "particle-steps/s"
 # one FP32 plane-table row per walk evaluation beyond the first (the first evaluation's row is
 # the particle's own cell, shared by the cell's particles in the cell-sorted order; so is the
 # FP64 row of the cell the plain walk concludes in, whose six distances give the weights).
-ROW_BYTES = 176          # 11 x 16 B FP32 row read per walk evaluation
+ROW_BYTES = 128          # one 128-B FP32 plane-table row (8 x 16 B) read per walk evaluation
 LOCATE_PER_PARTICLE = 53 + 61
 GATHER_PER_PARTICLE = 8 + 64 + 93
 
@@ -343,8 +343,8 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
         # particles' state and the remaining evaluations
         return {
             "center_to_corner": 24 * nodes_per_step,
-            "advect_locate": 86 * n_avg + 1 * n_avg + 176 * max(evals_per_step - n_avg - pending_evals, 0.0),
-            "guess_walk": 57 * pending + 176 * pending_evals,
+            "advect_locate": 86 * n_avg + 1 * n_avg + ROW_BYTES * max(evals_per_step - n_avg - pending_evals, 0.0),
+            "guess_walk": 57 * pending + ROW_BYTES * pending_evals,
             "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
             "wait_corner": 0,
             "gather_interpolate": 121 * n_avg + 12 * Nn,
@@ -353,7 +353,7 @@ def algorithmic_bytes(form: str, n_avg: float, evals_per_step: float, nodes_per_
     if form == "fp32":
         return {
             "center_to_corner": 24 * nodes_per_step,
-            "advect_locate": 86 * n_avg + 176 * max(evals_per_step - n_avg, 0.0),
+            "advect_locate": 86 * n_avg + ROW_BYTES * max(evals_per_step - n_avg, 0.0),
             "sort_by_cell": 24 * n_avg + 12 * (Nc + 2),
             "wait_corner": 0,
             "gather_interpolate": 121 * n_avg + 12 * Nn,

@@ -22,6 +22,9 @@ using fdfx::add;
 using fdfx::mul;
 using fdfx::sub;
 
+// One 128-B FP32 row per cell (the layout and the error bound are in fdf_walk.cuh): the first
+// vertex c0 as a float pair, thr32, the absolute slack for the FP64 arithmetic of the table, then
+// per face n32 = fl32(n) and e32 = fl32(n . (fc - c0)).
 __global__ void k_build_table32(const double *__restrict__ planes, const double *__restrict__ coor, GridDims g,
                                 float *__restrict__ table) {
   const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -40,22 +43,26 @@ __global__ void k_build_table32(const double *__restrict__ planes, const double 
     c0[q] = add((double)h, (double)l);   // exact: the pair's value
   }
   const double thr = row[36];
-  // rounded up with a little headroom: thr32 * (1 - 2^-24) >= thr, which the error bound uses;
+  // rounded up with a little headroom: thr32 * (1 - 2^-24)^2 >= thr, which the error bound uses;
   // a degenerate cell carries the sign bit
   float thr32 = __double2float_ru(mul(thr, 1.0 + 0x1p-22));
   if (fdfx::ubits(row[37]) != 0ULL) thr32 = -fabsf(thr32) - 1.0f;
   t[3] = thr32;
-  t[7] = 0.0f;
+  double sigma = 0.0;   // max over faces of sum_i |fc_i - c0_i| |n_i|
   for (int f = 0; f < 6; ++f) {
     const double *p = row + 6 * f;
-    float *o = t + 8 + 6 * f;
-    o[0] = __double2float_rn(sub(p[0], c0[0]));
-    o[1] = __double2float_rn(sub(p[1], c0[1]));
-    o[2] = __double2float_rn(sub(p[2], c0[2]));
-    o[3] = __double2float_rn(p[3]);
-    o[4] = __double2float_rn(p[4]);
-    o[5] = __double2float_rn(p[5]);
+    const double dx = sub(p[0], c0[0]), dy = sub(p[1], c0[1]), dz = sub(p[2], c0[2]);
+    const double e = add(add(mul(dx, p[3]), mul(dy, p[4])), mul(dz, p[5]));
+    const double sg = add(add(mul(fabs(dx), fabs(p[3])), mul(fabs(dy), fabs(p[4]))), mul(fabs(dz), fabs(p[5])));
+    sigma = sg > sigma ? sg : sigma;
+    float *o = t + 8 + 4 * f;
+    o[0] = __double2float_rn(p[3]);
+    o[1] = __double2float_rn(p[4]);
+    o[2] = __double2float_rn(p[5]);
+    o[3] = __double2float_rn(e);
   }
+  // the FP64 roundings of e and of the reference's own distance, 32 eps sigma (rounded up)
+  t[7] = __double2float_ru(mul(sigma, 0x1p-48));
 }
 
 // (hi, lo) float pair held in a double slot of the swarm arrays
@@ -254,11 +261,8 @@ __global__ void k_compact_pending(const unsigned int *__restrict__ pf, int n_cap
 // P1).  Whatever the guess, the cells, weights and statuses are the reference walk's; a good
 // guess turns the walk's dependent row loads into L1 hits.  Grid-stride over the list with a
 // warp-uniform trip count; path_hits counts the evaluations whose row was prefetched.
-__device__ __forceinline__ void prefetch_row_l1(const float *row) {
-  const char *p = reinterpret_cast<const char *>(row);
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 88));
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 4 * FDF_ROW32 - 4));
+__device__ __forceinline__ void prefetch_row_l1(const float *row) {   // a row is one 128-B line
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(row));
 }
 
 __global__ void __launch_bounds__(FDF_GUESS_THREADS, FDF_GUESS_MIN_BLOCKS) k_locate32_path(SwarmBuf b, GridDims g, const float *__restrict__ table,

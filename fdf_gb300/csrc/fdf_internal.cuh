@@ -19,7 +19,7 @@
 #include <cuda_runtime.h>
 
 #define FDF_ROW 38            // doubles per plane-table row (36 plane values + thr + flag)
-#define FDF_ROW32 44          // floats per precision-form row (c0 pair, thr32, a zero, 36 face values)
+#define FDF_ROW32 32          // floats per FP32 plane-table row: 128 B (c0 pair, thr32, slack, 6 x (n32, e32))
 #define FDF_MAX_TRAVERSAL 1000
 #define FDF_DISTANCE_THRESHOLD 1e-11
 #define FDF_INTERP_DIST_TOL 1e-14

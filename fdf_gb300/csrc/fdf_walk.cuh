@@ -5,16 +5,24 @@
 //
 // Each face class the walk needs -- d < 0, d == 0 (|d| < thr), d > 0 -- is decided from an
 // FP32 signed distance when that is provably the FP64 class for the position, and from the
-// exact FP64 distance (the FP64 plane table, the reference's arithmetic) otherwise.  With
-// c0 = c0h + c0l the cell's first vertex as a float pair (exact), fcr = fl32(fc - c0),
-// pr = fl32(fl32(ph - c0h) + fl32(pl - c0l)), n32 = fl32(n) and d32 = (fcr - pr) . n32 (FP32,
-// fused), every rounding is bounded by u32 = 2^-24 times the magnitudes involved:
-//     |pr_i - (p_i - c0_i)| <= u32 (2 B_i + 2 u32 (|ph_i| + |c0h_i|)),  B_i = |p_i - c0_i|
-//     |d32 - d64| <= 7.001 u32 S,   S = sum_i (A_i + B_i + u32 (|ph_i| + |c0h_i|)) |n_i|
-// with A_i = |fc_i - c0_i| (d64 is the reference's FP64 value; its own error is
-// ~1e-16 S).  The kernel uses E = 12 u32 S32 (S32, the FP32 estimate of S, is within
-// 8 u32 of S) and M = fl32(E + thr32) with thr32 >= thr (1 + 2^-22) rounded up, and
-// classifies
+// exact FP64 distance (the FP64 plane table, the reference's arithmetic) otherwise.
+//
+// FP32 distance.  With c0 = c0h + c0l the cell's first vertex as a float pair (exact),
+// P = p - c0, E = n . (fc - c0) and d = (fc - p) . n = E - n . P, the row holds n32 = fl32(n)
+// and e32 = fl32(E64) (E64: E in FP64), and the kernel computes
+//     pr_i = fl32(fl32(ph_i - c0h_i) + fl32(pl_i - c0l_i)),  d32 = e32 - (n32 . pr)
+// (the dot product as an FMA chain, then one subtraction).  With B_i = |P_i|,
+// ex_i = u (|ph_i| + |c0h_i|), u = 2^-24, eps = 2^-53 and A_i = |fc_i - c0_i|, the roundings
+// are bounded by
+//     |pr_i - P_i| <= 2u B_i + 2u ex_i                     (the pair subtraction)
+//     |e32 - E| <= u |E| + 6 eps sum_i A_i |n_i|            (E64, then fl32)
+//     dot product 3u, n32 u, the final subtraction u |d|, the reference's own d64 within
+//     5 eps sum_i (A_i + B_i) |n_i| of d,
+// which add up to
+//     |d32 - d64| <= u S (1 + 12u) + 23 eps sigma,   S = 2 |e32| + 7 sum_i |n32_i| (|pr_i| + ex_i)
+// with sigma = max over faces of sum_i A_i |n_i|.  The row carries slack >= 32 eps sigma
+// (rounded up) and thr32 >= thr (1 + 2^-22) (rounded up), and the kernel classifies with
+// M = fl32(4u S32 + fl32(thr32 + slack)) (S32: S in FP32, within 8u of S)
 //     d32 > M -> d64 >= thr (positive);  d32 < -M -> d64 <= -thr (negative);
 // anything else (including NaN) falls back to the exact FP64 distance of that face.
 // The cells, statuses and walk paths are therefore the reference's for the position.
@@ -22,12 +30,12 @@
 //
 // Positions.  The precision forms hold each coordinate as a float pair (hi, lo) whose exact
 // sum is the position.  The plain form walks its FP64 position x through its split
-// (hi = fl32(x), lo = fl32(x - hi), within 2^-48 |x| of x): that offset is below u32 times
-// the u32 |ph| part of S, well inside the bound's slack (12 against 7.001 + 1), and the
-// undecided faces are computed from x itself (EXACT), so every class is x's own.
+// (hi = fl32(x), lo = fl32(x - hi), within 2^-48 |x| <= u ex of x): that offset adds at most
+// u sum_i |n_i| ex_i to the error, well inside the 7 sum_i |n32_i| ex_i of S, and the undecided
+// faces are computed from x itself (EXACT), so every class is x's own.
 //
-// Per-cell FP32 row (176 B, 11 x 16 B): c0h (3 x f32), thr32 (f32, negative for a degenerate
-// cell), c0l (3 x f32), a zero, then per face LEFT..BACK: fcr (3 x f32), n32 (3 x f32).
+// Per-cell FP32 row (128 B, one cache line, 8 x 16 B): c0h (3 x f32), thr32 (f32, negative for
+// a degenerate cell), c0l (3 x f32), slack (f32), then per face LEFT..BACK: n32 (3 x f32), e32.
 #pragma once
 #include "fdf_internal.cuh"
 #include "fdf_exact.cuh"
@@ -86,30 +94,24 @@ __device__ __forceinline__ void eval_cell32(const float *__restrict__ table, con
   e.zero = false;
   e.degenerate = (__float_as_uint(h0.w) >> 31) != 0u;
   if (e.degenerate) return;
-  const float thr32 = h0.w;
+  float4 fr[6];   // per face: n32 (x, y, z), e32 (w); six 16-B loads
+#pragma unroll
+  for (int q = 0; q < 6; ++q) fr[q] = __ldg(row + 2 + q);
   const float prx = __fadd_rn(__fsub_rn(px.x, h0.x), __fsub_rn(px.y, h1.x));
   const float pry = __fadd_rn(__fsub_rn(py.x, h0.y), __fsub_rn(py.y, h1.y));
   const float prz = __fadd_rn(__fsub_rn(pz.x, h0.z), __fsub_rn(pz.y, h1.z));
-  // the split term u32 (|ph| + |c0h|) of the bound, per component
-  const float ex = __fmul_rn(__fadd_rn(sx, fabsf(h0.x)), 5.9604644775390625e-8f);
-  const float ey = __fmul_rn(__fadd_rn(sy, fabsf(h0.y)), 5.9604644775390625e-8f);
-  const float ez = __fmul_rn(__fadd_rn(sz, fabsf(h0.z)), 5.9604644775390625e-8f);
-  float fr[36];   // per face: fcr (3), n32 (3); nine 16-B loads
-#pragma unroll
-  for (int q = 0; q < 9; ++q) {
-    const float4 v = __ldg(row + 2 + q);
-    fr[4 * q] = v.x; fr[4 * q + 1] = v.y; fr[4 * q + 2] = v.z; fr[4 * q + 3] = v.w;
-  }
+  // |pr_i| + ex_i, ex_i = u (|ph_i| + |c0h_i|): the split term of the bound
+  const float ax = __fmaf_rn(__fadd_rn(sx, fabsf(h0.x)), 5.9604644775390625e-8f, fabsf(prx));
+  const float ay = __fmaf_rn(__fadd_rn(sy, fabsf(h0.y)), 5.9604644775390625e-8f, fabsf(pry));
+  const float az = __fmaf_rn(__fadd_rn(sz, fabsf(h0.z)), 5.9604644775390625e-8f, fabsf(prz));
+  const float base = __fadd_rn(h0.w, h1.w);   // thr32 + slack
 #pragma unroll
   for (int f = 0; f < 6; ++f) {
-    const float fx = fr[6 * f], fy = fr[6 * f + 1], fz = fr[6 * f + 2];
-    const float nx = fr[6 * f + 3], ny = fr[6 * f + 4], nz = fr[6 * f + 5];
-    const float tx = __fsub_rn(fx, prx), ty = __fsub_rn(fy, pry), tz = __fsub_rn(fz, prz);
-    const float d32 = __fmaf_rn(tz, nz, __fmaf_rn(ty, ny, __fmul_rn(tx, nx)));
-    const float S = __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fz), fabsf(prz)), ez), fabsf(nz),
-                              __fmaf_rn(__fadd_rn(__fadd_rn(fabsf(fy), fabsf(pry)), ey), fabsf(ny),
-                                        __fmul_rn(__fadd_rn(__fadd_rn(fabsf(fx), fabsf(prx)), ex), fabsf(nx))));
-    const float M = __fadd_rn(__fmul_rn(S, 12.0f * 5.9604644775390625e-8f), thr32);
+    const float nx = fr[f].x, ny = fr[f].y, nz = fr[f].z, ef = fr[f].w;
+    const float d32 = __fsub_rn(ef, __fmaf_rn(nz, prz, __fmaf_rn(ny, pry, __fmul_rn(nx, prx))));
+    const float S = __fmaf_rn(7.0f, __fmaf_rn(fabsf(nz), az, __fmaf_rn(fabsf(ny), ay, __fmul_rn(fabsf(nx), ax))),
+                              __fadd_rn(fabsf(ef), fabsf(ef)));
+    const float M = __fmaf_rn(S, 4.0f * 5.9604644775390625e-8f, base);
     if (d32 > M) {
       e.dv[f] = d32;
     } else if (d32 < -M) {
