@@ -762,14 +762,16 @@ def run_gpu(args, rank, ws, local, dist):
         if momentum_on(wl):
             mom = (pinned_like(np.zeros((KM, JM, IM + 1, 3))), pinned_like(np.zeros((KM, JM + 1, IM, 3))),
                    pinned_like(np.zeros((KM + 1, JM, IM, 3))))
-        from fdf_gb300.context import TRANSFER_IN_PLACE, TRANSFER_STAGED, _ptr
+        from fdf_gb300.context import TRANSFER_AUTO, TRANSFER_IN_PLACE, TRANSFER_STAGED, _ptr
         lib, h = ctx.lib, ctx.h
         import ctypes
         got = ctypes.c_int64()
 
-        def e2e_steps(route: int, k: int):
-            """k steps through the C ABI with the host arrays: set, step, get (swarm and fields)."""
-            ctx.set_transfer_route(route)
+        def e2e_steps(route, k: int):
+            """k steps through the C ABI with the host arrays: set, step, get (swarm and fields);
+            route None keeps the context's route (and what AUTO has measured)."""
+            if route is not None:
+                ctx.set_transfer_route(route)
             split = {"set_swarm": 0.0, "step": 0.0, "get_swarm": 0.0, "get_fields": 0.0}
             ps, n_cur, moved = 0, live[0], 0
             barrier(dist)
@@ -805,19 +807,26 @@ def run_gpu(args, rank, ws, local, dist):
 
         live = [n0]
         k_e2e = max(3, min(args.steps, 10))
-        # the library's default route (copy engines through the staging buffer) is the headline;
-        # the in-place route (layout kernels reading and writing the pinned arrays over the host
-        # link) is timed beside it in the same process
-        v_st, ms_st, gbs_st = e2e_steps(TRANSFER_STAGED, k_e2e)
+        # the library's default route (AUTO: per direction, the route it measured faster on this
+        # machine during an untimed first step) is the headline; the staged route (copy engines
+        # through the staging buffer) and the in-place route (layout kernels reading and writing
+        # the pinned arrays over the host link) are timed beside it in the same process
+        e2e_steps(TRANSFER_AUTO, 1)
+        chosen = ctx.transfer_routes()
+        v_st, ms_st, gbs_st = e2e_steps(None, k_e2e)
+        v_s2, ms_s2, gbs_s2 = e2e_steps(TRANSFER_STAGED, max(3, k_e2e // 2))
         v_ip, ms_ip, gbs_ip = e2e_steps(TRANSFER_IN_PLACE, max(3, k_e2e // 2))
-        ctx.set_transfer_route(TRANSFER_STAGED)
+        ctx.set_transfer_route(TRANSFER_AUTO)
+        names = {TRANSFER_STAGED: "staged", TRANSFER_IN_PLACE: "in place", -1: "staged (not measured)"}
         link = host_link_gbs(local)
         e2e = {"value": v_st, "unit": UNIT, "h2d_bytes_per_step": int(120 * n0),
                "d2h_bytes_per_step": int(120 * n0 + 16 * Nn + 8 * Nf + (24 * Nf if mom is not None else 0)),
-               "steps": k_e2e, "route": "staged (copy engines, the library default)",
+               "steps": k_e2e,
+               "route": f"auto (the library default): upload {names[chosen[0]]}, download {names[chosen[1]]}",
                "path": "fdf_SetSwarm + fdf_AdvanceStep + fdf_GetSwarm/GetScatteredFields/GetFaceDeposits, "
                        "pinned host DMSwarm-layout arrays",
                "ms_per_step": ms_st, "transfer_gbs": gbs_st,
+               "staged_route": {"value": v_s2, "ms_per_step": ms_s2, "transfer_gbs": gbs_s2},
                "in_place_route": {"value": v_ip, "ms_per_step": ms_ip, "transfer_gbs": gbs_ip},
                "host_link_gbs": link}
 

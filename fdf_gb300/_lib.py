@@ -47,6 +47,7 @@ _SIGS = {
     "fdf_Contra2CartDevice": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fdf_SetForm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_SetTransferRoute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fdf_GetTransferRoutes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "fdf_SetTimeStep": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_SetParticleVolume": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "fdf_ReserveParticles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64]),

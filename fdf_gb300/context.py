@@ -23,7 +23,7 @@ ERR_NAMES = {55: "PETSC_ERR_MEM", 56: "PETSC_ERR_SUP", 62: "PETSC_ERR_ARG_WRONG"
              97: "PETSC_ERR_GPU"}
 NEEDS_LOCATION, ACTIVE_AND_LOCATED, MIGRATING_OUT, LOST, UNINITIALIZED = 0, 1, 2, 3, 4
 FORM_PLAIN_FP64, FORM_FP32, FORM_LEARNED_FP32 = 0, 1, 2
-TRANSFER_STAGED, TRANSFER_IN_PLACE = 0, 1
+TRANSFER_STAGED, TRANSFER_IN_PLACE, TRANSFER_AUTO = 0, 1, 2
 LOCATOR_BF16, LOCATOR_F16 = 0, 1
 LOCATOR_NPARAM = 33923
 
@@ -179,8 +179,15 @@ class PicContext:
         self._check(self.lib.fdf_Contra2CartDevice(self.h, ctypes.c_void_p(ucont.data_ptr())))
 
     def set_transfer_route(self, route: int):
-        """TRANSFER_STAGED (copy engines through a staging buffer, the default) or TRANSFER_IN_PLACE."""
+        """TRANSFER_AUTO (the default: per direction, the route measured faster on this machine),
+        TRANSFER_STAGED (copy engines through a staging buffer) or TRANSFER_IN_PLACE."""
         self._check(self.lib.fdf_SetTransferRoute(self.h, int(route)))
+
+    def transfer_routes(self) -> tuple[int, int]:
+        """(upload, download) routes in use; -1 where AUTO has not measured yet."""
+        up, down = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.fdf_GetTransferRoutes(self.h, ctypes.byref(up), ctypes.byref(down)))
+        return up.value, down.value
 
     def set_form(self, form: int):
         """FORM_PLAIN_FP64 (bit-exact), FORM_FP32 (precision form) or FORM_LEARNED_FP32 (precision

@@ -84,7 +84,7 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox); cfree(ctx->mom); cfree(ctx->mom32);
   eulerian_free(ctx);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
-  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->spid);
   cfree(ctx->cell_start); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
   locator_free(ctx);
   for (auto &gx : ctx->step_graph)
@@ -221,9 +221,17 @@ int fdf_SetUcat(FdfContext *ctx, const double *ucat, int node_sized) {
 
 int fdf_SetTransferRoute(FdfContext *ctx, int route) {
   if (!ctx) return FDF_ERR_ARG_NULL;
-  if (route != FDF_TRANSFER_STAGED && route != FDF_TRANSFER_IN_PLACE)
+  if (route != FDF_TRANSFER_STAGED && route != FDF_TRANSFER_IN_PLACE && route != FDF_TRANSFER_AUTO)
     return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_SetTransferRoute: unknown route");
   ctx->xfer_route = route;
+  ctx->route_up = ctx->route_down = -1;   // AUTO measures again
+  return FDF_SUCCESS;
+}
+
+int fdf_GetTransferRoutes(FdfContext *ctx, int *upload, int *download) {
+  if (!ctx || !upload || !download) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_GetTransferRoutes: null argument");
+  *upload = ctx->xfer_route == FDF_TRANSFER_AUTO ? ctx->route_up : ctx->xfer_route;
+  *download = ctx->xfer_route == FDF_TRANSFER_AUTO ? ctx->route_down : ctx->xfer_route;
   return FDF_SUCCESS;
 }
 
@@ -267,13 +275,15 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   ctx->buf[1] = SwarmBuf{};
   ctx->staging_bytes = 0;
   ctx->gen++;
-  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->staging);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->spid);
+  cfree(ctx->staging);
   int cap = (int)(capacity < 256 ? 256 : capacity);   // never zero: the sort always has scratch
   size_t per = swarm_bytes_per_buf(cap);
   CU(dev_alloc(&ctx->swarm_mem, 2 * per));
   CU(dev_alloc(&ctx->keys, 4ull * cap));
   CU(dev_alloc(&ctx->perm, 4ull * cap));
   CU(dev_alloc(&ctx->rank, 4ull * cap));
+  CU(dev_alloc(&ctx->spid, 8ull * cap));
   CU(dev_alloc(&ctx->staging, (size_t)cap * 120 + 1024));
   carve_swarm((char *)ctx->swarm_mem, cap, ctx->buf[0]);
   carve_swarm((char *)ctx->swarm_mem + per, cap, ctx->buf[1]);
@@ -320,6 +330,55 @@ static int64_t transfer_chunk(int64_t n) {
   return std::max<int64_t>(int64_t(1) << 22, (n + FDF_XFER_CHUNKS - 1) / FDF_XFER_CHUNKS);
 }
 
+// The AUTO route's measurement: a warm-up of XFER_WARM particles by each route, then a slice of
+// xfer_slice(n) particles by each, timed with events; the rest of the call and later calls of
+// that direction take the faster.  Offsets stay multiples of XFER_WARM, so the in-place kernels'
+// 16-byte accesses stay aligned.  Calls of fewer than 4 XFER_SLICE_MIN particles are not timed.
+constexpr int64_t XFER_WARM = 2048, XFER_SLICE_MIN = int64_t(1) << 20, XFER_SLICE_MAX = int64_t(1) << 22;
+static int64_t xfer_slice(int64_t n) {
+  if (n < 4 * XFER_SLICE_MIN) return 0;
+  return std::min(XFER_SLICE_MAX, n / 4) / XFER_WARM * XFER_WARM;
+}
+
+// Times two ranges of one transfer direction: run(0, o, m) by the staged route, run(1, o, m) in
+// place; returns the faster route (FDF_TRANSFER_*) and leaves `done` particles transferred.
+extern "C++" {
+namespace {
+template <typename Run>
+int calibrate_route(FdfContext *ctx, int64_t m, Run run, int64_t &done, cudaError_t &err) {
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int best = FDF_TRANSFER_STAGED;
+  for (auto &e : ev)
+    if (err == cudaSuccess) err = cudaEventCreate(&e);
+  if (err == cudaSuccess) err = run(0, 0, XFER_WARM);
+  if (err == cudaSuccess) err = run(1, XFER_WARM, XFER_WARM);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->side);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+  const int64_t o = 2 * XFER_WARM;
+  if (err == cudaSuccess) err = cudaEventRecord(ev[0], ctx->stream);
+  if (err == cudaSuccess) err = run(0, o, m);
+  if (err == cudaSuccess) err = cudaEventRecord(ev[1], ctx->side);    // the staged route ends on either
+  if (err == cudaSuccess) err = cudaEventRecord(ev[2], ctx->stream);   // stream: time to the later one
+  if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->side);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+  float t_staged = 0.f, t_a = 0.f, t_in = 0.f;
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&t_staged, ev[0], ev[1]);
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&t_a, ev[0], ev[2]);
+  t_staged = std::max(t_staged, t_a);
+  if (err == cudaSuccess) err = cudaEventRecord(ev[0], ctx->stream);
+  if (err == cudaSuccess) err = run(1, o + m, m);
+  if (err == cudaSuccess) err = cudaEventRecord(ev[3], ctx->stream);
+  if (err == cudaSuccess) err = cudaEventSynchronize(ev[3]);
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&t_in, ev[0], ev[3]);
+  if (err == cudaSuccess && t_in < t_staged) best = FDF_TRANSFER_IN_PLACE;
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  done = o + 2 * m;
+  return best;
+}
+}  // namespace
+}  // extern "C++"
+
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity, const double *weight,
                  const double *P, const int64_t *cell_id, const int64_t *pid, const int64_t *status) {
   if (!ctx) return FDF_ERR_ARG_NULL;
@@ -337,38 +396,63 @@ int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const doubl
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
   const void *arrays[7] = {position, velocity, weight, P, cell_id, pid, status};
   void *views[7];
-  if (n > 0 && ctx->xfer_route == FDF_TRANSFER_IN_PLACE && host_views(arrays, views)) {
-    ctx->cur = 0;
-    launch_swarm_from_host(views, (int)n, ctx->g, ctx->buf[0], form_is32(ctx->form), ctx->stream);
-    CHECK_LAUNCH();
-    ctx->launches += 1;
-  } else if (n > 0) {
-    ctx->cur = 0;
-    // the side stream starts after everything already queued on the context stream
-    CU(cudaEventRecord(ctx->ev_xfer, ctx->stream));
-    CU(cudaStreamWaitEvent(ctx->side, ctx->ev_xfer, 0));
-    const int64_t chunk = transfer_chunk(n);
-    for (int64_t o = 0; o < n; o += chunk) {
-      const int64_t m = std::min(chunk, n - o);
-      CU(cudaMemcpyAsync(d_pos + 3 * o, position + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaMemcpyAsync(d_vel + 3 * o, velocity + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaMemcpyAsync(d_wgt + 3 * o, weight + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaMemcpyAsync(d_P + o, P + o, 8ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaMemcpyAsync(d_cell + 3 * o, cell_id + 3 * o, 24ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaMemcpyAsync(d_pid + o, pid + o, 8ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaMemcpyAsync(d_st + o, status + o, 8ull * m, cudaMemcpyHostToDevice, ctx->side));
-      CU(cudaEventRecord(ctx->ev_xfer, ctx->side));
-      CU(cudaStreamWaitEvent(ctx->stream, ctx->ev_xfer, 0));
-      const SwarmBuf b = shifted(ctx->buf[0], o);
-      if (form_is32(ctx->form))
-        launch_swarm_from_aos32(d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o, d_pid + o,
-                                d_st + o, (int)m, ctx->g, b, ctx->stream);
-      else
-        launch_swarm_from_aos(d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o, d_pid + o,
-                              d_st + o, (int)m, ctx->g, b, ctx->stream);
-      CHECK_LAUNCH();
+  const bool f32 = form_is32(ctx->form);
+  // particles [o, o + m) by the staged (route 0) or the in-place route (1)
+  auto run = [&](int route, int64_t o, int64_t m) -> cudaError_t {
+    if (m <= 0) return cudaSuccess;
+    if (route == 1) {
+      const void *v[7];
+      const int bs[7] = {3, 3, 3, 1, 3, 1, 1};
+      for (int q = 0; q < 7; ++q) v[q] = static_cast<const double *>(views[q]) + bs[q] * o;
+      launch_swarm_from_host(v, (int)m, ctx->g, shifted(ctx->buf[0], o), f32, ctx->stream);
       ctx->launches += 1;
+      return cudaGetLastError();
     }
+    // the side stream starts after everything already queued on the context stream
+    cudaError_t e = cudaEventRecord(ctx->ev_xfer, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->side, ctx->ev_xfer, 0);
+    const int64_t chunk = transfer_chunk(n);
+    for (int64_t c = o; c < o + m && e == cudaSuccess; c += chunk) {
+      const int64_t k = std::min(chunk, o + m - c);
+      const cudaMemcpyKind h2d = cudaMemcpyHostToDevice;
+      e = cudaMemcpyAsync(d_pos + 3 * c, position + 3 * c, 24ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_vel + 3 * c, velocity + 3 * c, 24ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_wgt + 3 * c, weight + 3 * c, 24ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_P + c, P + c, 8ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_cell + 3 * c, cell_id + 3 * c, 24ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_pid + c, pid + c, 8ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(d_st + c, status + c, 8ull * k, h2d, ctx->side);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_xfer, ctx->side);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_xfer, 0);
+      if (e != cudaSuccess) break;
+      const SwarmBuf b = shifted(ctx->buf[0], c);
+      if (f32)
+        launch_swarm_from_aos32(d_pos + 3 * c, d_vel + 3 * c, d_wgt + 3 * c, d_P + c, d_cell + 3 * c, d_pid + c,
+                                d_st + c, (int)k, ctx->g, b, ctx->stream);
+      else
+        launch_swarm_from_aos(d_pos + 3 * c, d_vel + 3 * c, d_wgt + 3 * c, d_P + c, d_cell + 3 * c, d_pid + c,
+                              d_st + c, (int)k, ctx->g, b, ctx->stream);
+      ctx->launches += 1;
+      e = cudaGetLastError();
+    }
+    return e;
+  };
+  ctx->cur = 0;
+  if (n > 0) {
+    const bool pinned = ctx->xfer_route != FDF_TRANSFER_STAGED && host_views(arrays, views);
+    int route = FDF_TRANSFER_STAGED;
+    int64_t done = 0;
+    cudaError_t e = cudaSuccess;
+    if (pinned && ctx->xfer_route == FDF_TRANSFER_IN_PLACE) {
+      route = FDF_TRANSFER_IN_PLACE;
+    } else if (pinned && ctx->route_up >= 0) {
+      route = ctx->route_up;
+    } else if (pinned && xfer_slice(n) > 0) {
+      route = calibrate_route(ctx, xfer_slice(n), run, done, e);
+      if (e == cudaSuccess) ctx->route_up = route;
+    }
+    if (e == cudaSuccess) e = run(route == FDF_TRANSFER_IN_PLACE ? 1 : 0, done, n - done);
+    if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_SetSwarm: ") + cudaGetErrorString(e));
   }
   DevCounters c{};
   c.n = (int)n;
@@ -436,37 +520,61 @@ int fdf_GetSwarm(FdfContext *ctx, int64_t n_max, int64_t *n_out, double *positio
   long long *d_cell = (long long *)(d_P + n), *d_pid = d_cell + 3 * n, *d_st = d_pid + n;
   const void *arrays[7] = {position, velocity, weight, P, cell_id, pid, status};
   void *views[7];
-  if (ctx->xfer_route == FDF_TRANSFER_IN_PLACE && host_views(arrays, views)) {
-    launch_swarm_to_host(ctx->buf[ctx->cur], (int)n, ctx->g, views, form_is32(ctx->swarm_form), ctx->stream);
-    CHECK_LAUNCH();
-    ctx->launches += 1;
-    CU(cudaStreamSynchronize(ctx->stream));
-    return FDF_SUCCESS;
+  const bool f32 = form_is32(ctx->swarm_form);
+  const SwarmBuf &src = ctx->buf[ctx->cur];
+  // particles [o, o + m) by the staged (route 0) or the in-place route (1)
+  auto run = [&](int route, int64_t o, int64_t m) -> cudaError_t {
+    if (m <= 0) return cudaSuccess;
+    if (route == 1) {
+      void *v[7];
+      const int bs[7] = {3, 3, 3, 1, 3, 1, 1};
+      for (int q = 0; q < 7; ++q) v[q] = static_cast<double *>(views[q]) + bs[q] * o;
+      launch_swarm_to_host(shifted(src, o), (int)m, ctx->g, v, f32, ctx->stream);
+      ctx->launches += 1;
+      return cudaGetLastError();
+    }
+    const int64_t chunk = transfer_chunk(n);
+    cudaError_t e = cudaSuccess;
+    for (int64_t c = o; c < o + m && e == cudaSuccess; c += chunk) {
+      const int64_t k = std::min(chunk, o + m - c);
+      const SwarmBuf b = shifted(src, c);
+      if (f32)
+        launch_swarm_to_aos32(b, (int)k, ctx->g, d_pos + 3 * c, d_vel + 3 * c, d_wgt + 3 * c, d_P + c,
+                              d_cell + 3 * c, d_pid + c, d_st + c, ctx->stream);
+      else
+        launch_swarm_to_aos(b, (int)k, ctx->g, d_pos + 3 * c, d_vel + 3 * c, d_wgt + 3 * c, d_P + c, d_cell + 3 * c,
+                            d_pid + c, d_st + c, ctx->stream);
+      ctx->launches += 1;
+      e = cudaGetLastError();
+      const cudaMemcpyKind d2h = cudaMemcpyDeviceToHost;
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_xfer, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->side, ctx->ev_xfer, 0);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(position + 3 * c, d_pos + 3 * c, 24ull * k, d2h, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(velocity + 3 * c, d_vel + 3 * c, 24ull * k, d2h, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(weight + 3 * c, d_wgt + 3 * c, 24ull * k, d2h, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(P + c, d_P + c, 8ull * k, d2h, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(cell_id + 3 * c, d_cell + 3 * c, 24ull * k, d2h, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(pid + c, d_pid + c, 8ull * k, d2h, ctx->side);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(status + c, d_st + c, 8ull * k, d2h, ctx->side);
+    }
+    return e;
+  };
+  const bool pinned = ctx->xfer_route != FDF_TRANSFER_STAGED && host_views(arrays, views);
+  int route = FDF_TRANSFER_STAGED;
+  int64_t done = 0;
+  cudaError_t e = cudaSuccess;
+  if (pinned && ctx->xfer_route == FDF_TRANSFER_IN_PLACE) {
+    route = FDF_TRANSFER_IN_PLACE;
+  } else if (pinned && ctx->route_down >= 0) {
+    route = ctx->route_down;
+  } else if (pinned && xfer_slice(n) > 0) {
+    route = calibrate_route(ctx, xfer_slice(n), run, done, e);
+    if (e == cudaSuccess) ctx->route_down = route;
   }
-  const int64_t chunk = transfer_chunk(n);
-  for (int64_t o = 0; o < n; o += chunk) {
-    const int64_t m = std::min(chunk, n - o);
-    const SwarmBuf b = shifted(ctx->buf[ctx->cur], o);
-    if (form_is32(ctx->swarm_form))
-      launch_swarm_to_aos32(b, (int)m, ctx->g, d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o,
-                            d_pid + o, d_st + o, ctx->stream);
-    else
-      launch_swarm_to_aos(b, (int)m, ctx->g, d_pos + 3 * o, d_vel + 3 * o, d_wgt + 3 * o, d_P + o, d_cell + 3 * o,
-                          d_pid + o, d_st + o, ctx->stream);
-    CHECK_LAUNCH();
-    ctx->launches += 1;
-    CU(cudaEventRecord(ctx->ev_xfer, ctx->stream));
-    CU(cudaStreamWaitEvent(ctx->side, ctx->ev_xfer, 0));
-    CU(cudaMemcpyAsync(position + 3 * o, d_pos + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
-    CU(cudaMemcpyAsync(velocity + 3 * o, d_vel + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
-    CU(cudaMemcpyAsync(weight + 3 * o, d_wgt + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
-    CU(cudaMemcpyAsync(P + o, d_P + o, 8ull * m, cudaMemcpyDeviceToHost, ctx->side));
-    CU(cudaMemcpyAsync(cell_id + 3 * o, d_cell + 3 * o, 24ull * m, cudaMemcpyDeviceToHost, ctx->side));
-    CU(cudaMemcpyAsync(pid + o, d_pid + o, 8ull * m, cudaMemcpyDeviceToHost, ctx->side));
-    CU(cudaMemcpyAsync(status + o, d_st + o, 8ull * m, cudaMemcpyDeviceToHost, ctx->side));
-  }
-  CU(cudaStreamSynchronize(ctx->side));
-  CU(cudaStreamSynchronize(ctx->stream));
+  if (e == cudaSuccess) e = run(route == FDF_TRANSFER_IN_PLACE ? 1 : 0, done, n - done);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->side);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, FDF_ERR_GPU, std::string("fdf_GetSwarm: ") + cudaGetErrorString(e));
   return FDF_SUCCESS;
 }
 
@@ -601,8 +709,8 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
     CU(cudaEventRecord(ctx->ev_corner, ctx->side));
   }
   launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start,
-                       ctx->perm, s);
-  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
+                       ctx->perm, s, src.pid, ctx->spid);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s, ctx->spid);
   size_t e2 = prof ? record_event(ctx, s) : 0;
   if (!locate_only) CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
   size_t e3 = prof ? record_event(ctx, s) : 0;
@@ -681,8 +789,9 @@ int resort(FdfContext *ctx, int remove_lost, int remove_oob, int64_t *removed_lo
   launch_resort_keys(src, ctx->cap, g, f32 ? 1 : 0, remove_lost, remove_oob, ctx->bbox, ctx->fbox, ctx->cnt,
                      ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, s);
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
-  launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, 1, ctx->cell_start, ctx->perm, s);
-  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
+  launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, 1, ctx->cell_start, ctx->perm, s,
+                       src.pid, ctx->spid);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s, ctx->spid);
   if (f32)
     launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s, GATHER_COPY);
   else

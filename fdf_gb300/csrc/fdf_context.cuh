@@ -57,13 +57,15 @@ struct FdfContext {
   int cur = 0;
   void *swarm_mem = nullptr;
   unsigned int *keys = nullptr, *perm = nullptr;   // [cap]: cell key per slot, sorted slot -> previous slot
+  long long *spid = nullptr;                       // [cap]: PID at its sorted position (the sort's scratch)
   unsigned int *rank = nullptr;                    // [cap]: rank of the slot's particle within its new cell
   unsigned int *cell_start = nullptr;              // [Nc+2]: histogram, then its exclusive scan
   unsigned int *scan_sums = nullptr;
   DevCounters *cnt = nullptr;
   void *staging = nullptr;
   size_t staging_bytes = 0;
-  int xfer_route = FDF_TRANSFER_STAGED;   // fdf_SetTransferRoute
+  int xfer_route = FDF_TRANSFER_AUTO;     // fdf_SetTransferRoute
+  int route_up = -1, route_down = -1;     // AUTO: the route measured faster per direction (-1: not yet)
   unsigned int sentinel = 0;
   bool swarm_set = false;
   bool layout_ok = false;   // the held particles are sorted by (cell, PID) and cell_start matches them

@@ -126,17 +126,24 @@ int fdf_SetTimeStep(FdfContext *ctx, double dt);                 /* user->dt    
 int fdf_SetParticleVolume(FdfContext *ctx, double volume);       /* face deposit V_p    */
 
 /* ---- swarm transfer (DMSwarm fields, ParticleSwarm.c:64-96, [n][bs] layout) ----
- * Route (fdf_SetTransferRoute): STAGED (default) copies the arrays with the copy engines, in
- * particle chunks, through a device staging buffer, the layout conversion of one chunk
- * overlapping the copies of the next; IN_PLACE has the layout kernels read (fdf_SetSwarm) or
- * write (fdf_GetSwarm) the arrays over the host link when all seven arrays of a call are
- * page-locked host memory (cudaHostAlloc / cudaHostRegister) and 16-byte aligned, and falls
- * back to STAGED otherwise.  How fast kernels reach host memory depends on the machine (the
- * copy engines ran at the link's rate on every GB300 tried, kernel accesses at a quarter of it
- * on one), hence the default.  The results are the same either way. */
+ * Route (fdf_SetTransferRoute): STAGED copies the arrays with the copy engines, in particle
+ * chunks, through a device staging buffer, the layout conversion of one chunk overlapping the
+ * copies of the next; IN_PLACE has the layout kernels read (fdf_SetSwarm) or write
+ * (fdf_GetSwarm) the arrays over the host link when all seven arrays of a call are page-locked
+ * host memory (cudaHostAlloc / cudaHostRegister) and 16-byte aligned, and falls back to STAGED
+ * otherwise.  Which is faster depends on the machine (on the GB300s tried, the copy engines ran
+ * at the link's rate on one and kernel accesses at a quarter of it; on two others the in-place
+ * route was 19-39 % faster).  AUTO (default), per direction: the first call with page-locked
+ * arrays and at least 4M particles moves two slices of its particles (up to 4M each) by each
+ * route, timed with events, and that call's remaining particles and every later call of that
+ * direction take the faster route; smaller calls and other arrays go STAGED.  The results are
+ * the same by either route.  fdf_GetTransferRoutes reports the routes chosen (-1: AUTO has not
+ * measured that direction yet); fdf_SetTransferRoute(AUTO) measures again. */
 #define FDF_TRANSFER_STAGED 0
 #define FDF_TRANSFER_IN_PLACE 1
+#define FDF_TRANSFER_AUTO 2
 int fdf_SetTransferRoute(FdfContext *ctx, int route);
+int fdf_GetTransferRoutes(FdfContext *ctx, int *upload, int *download);
 int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity);
 int fdf_SetSwarm(FdfContext *ctx, int64_t n, const double *position, const double *velocity,
                  const double *weight, const double *P, const int64_t *cell_id, const int64_t *pid,

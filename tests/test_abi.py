@@ -37,6 +37,21 @@ def test_python_binding_covers_the_header():
     assert set(declared_functions()) == set(_lib.exported_symbols())
 
 
+def test_python_constants_match_the_header():
+    """The Python mirror's form, route and locator constants are the header's #defines."""
+    from fdf_gb300 import context as C
+    defines = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        for name, val in re.findall(r"^#define\s+FDF_(\w+)\s+(-?\d+)\s*$", open(h).read(), flags=re.M):
+            defines[name] = int(val)
+    pairs = {"FORM_PLAIN_FP64": C.FORM_PLAIN_FP64, "FORM_FP32": C.FORM_FP32, "FORM_LEARNED_FP32": C.FORM_LEARNED_FP32,
+             "TRANSFER_STAGED": C.TRANSFER_STAGED, "TRANSFER_IN_PLACE": C.TRANSFER_IN_PLACE,
+             "TRANSFER_AUTO": C.TRANSFER_AUTO, "LOCATOR_BF16": C.LOCATOR_BF16, "LOCATOR_F16": C.LOCATOR_F16,
+             "LOCATOR_NPARAM": C.LOCATOR_NPARAM}
+    for name, value in pairs.items():
+        assert defines[name] == value, name
+
+
 def test_context_create_fails_loudly_without_gpu():
     try:
         import torch

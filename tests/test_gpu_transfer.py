@@ -66,7 +66,7 @@ def _pinned(a, offset=0):
     return out, t
 
 
-def _roundtrip(form, s, pinned, offset=0, launches=None, route=None):
+def _roundtrip(form, s, pinned, offset=0, launches=None, route=None, routes=None):
     wl = W.config_sinusoidal(IM=8, JM=8, KM=16, n=10, cfl=1.0, steps=1)
     keep = []
     ins = []
@@ -97,6 +97,8 @@ def _roundtrip(form, s, pinned, offset=0, launches=None, route=None):
         got = ctypes.c_int64()
         ctx._check(ctx.lib.fdf_GetSwarm(ctx.h, s.n, ctypes.byref(got), *[_ptr(a) for a in outs]))
         assert got.value == s.n
+        if routes is not None:
+            routes.append(ctx.transfer_routes())
     return [np.array(a) for a in outs]
 
 
@@ -104,20 +106,25 @@ def _roundtrip(form, s, pinned, offset=0, launches=None, route=None):
 def test_page_locked_arrays_in_place(require_gpu, form):
     """With the in-place route, page-locked, 16-byte aligned arrays are read and written in place
     by the layout kernels; the swarm is the staged route's bit for bit (and an unaligned
-    page-locked set takes the staged route).  By default (the staged route) page-locked arrays are
-    copied by the copy engines like any other.  4500003 particles: a ragged last tile, and two
-    chunks on the staged route."""
+    page-locked set takes the staged route).  By default (AUTO) the first page-locked transfer of
+    each direction times both routes on slices of its particles and finishes with the faster,
+    again bit for bit.  4500003 particles: a ragged last tile, and two chunks on the staged
+    route."""
     n = 4_500_003
     s = _swarm(n, (8, 8, 16), np.random.default_rng(4))
     s.cell[s.cell[:, 0] < 0] = -1
-    counts = []
-    ref = _roundtrip(form, s, pinned=False, launches=counts)
+    counts, routes = [], []
+    ref = _roundtrip(form, s, pinned=False, launches=counts, routes=routes)
     direct = _roundtrip(form, s, pinned=True, launches=counts, route=TRANSFER_IN_PLACE)
     skewed = _roundtrip(form, s, pinned=True, offset=8, launches=counts, route=TRANSFER_IN_PLACE)
-    default = _roundtrip(form, s, pinned=True, launches=counts)
+    default = _roundtrip(form, s, pinned=True, launches=counts, routes=routes)
     staged = _roundtrip(form, s, pinned=True, launches=counts, route=TRANSFER_STAGED)
-    # staged: one layout kernel per chunk; in place: one for the swarm
-    assert counts == [2, 1, 2, 2, 2]
+    # staged: one layout kernel per chunk; in place: one for the swarm; AUTO: a warm-up and a
+    # timed slice by each route, then the rest by the faster (one kernel either way)
+    assert counts == [2, 1, 2, 5, 2]
+    assert routes[0] == (-1, -1)                                  # unpinned: nothing measured
+    assert all(r in (TRANSFER_STAGED, TRANSFER_IN_PLACE) for r in routes[1])
+    print(f"[transfer] AUTO chose upload {routes[1][0]}, download {routes[1][1]} (0 staged, 1 in place)")
     for f, a, b, c, d, e in zip(FIELDS, ref, direct, skewed, default, staged):
         for x in (b, c, d, e):
             assert np.array_equal(a.view(np.uint8), x.view(np.uint8)), f
