@@ -84,7 +84,7 @@ int fdf_ContextDestroy(FdfContext *ctx) {
   cfree(ctx->fi32); cfree(ctx->fj32); cfree(ctx->fk32); cfree(ctx->fbox); cfree(ctx->mom); cfree(ctx->mom32);
   eulerian_free(ctx);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
-  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->spid);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank);
   cfree(ctx->cell_start); cfree(ctx->scan_sums); cfree(ctx->cnt); cfree(ctx->staging);
   locator_free(ctx);
   for (auto &gx : ctx->step_graph)
@@ -275,15 +275,13 @@ int fdf_ReserveParticles(FdfContext *ctx, int64_t capacity) {
   ctx->buf[1] = SwarmBuf{};
   ctx->staging_bytes = 0;
   ctx->gen++;
-  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->spid);
-  cfree(ctx->staging);
+  cfree(ctx->swarm_mem); cfree(ctx->keys); cfree(ctx->perm); cfree(ctx->rank); cfree(ctx->staging);
   int cap = (int)(capacity < 256 ? 256 : capacity);   // never zero: the sort always has scratch
   size_t per = swarm_bytes_per_buf(cap);
   CU(dev_alloc(&ctx->swarm_mem, 2 * per));
   CU(dev_alloc(&ctx->keys, 4ull * cap));
   CU(dev_alloc(&ctx->perm, 4ull * cap));
   CU(dev_alloc(&ctx->rank, 4ull * cap));
-  CU(dev_alloc(&ctx->spid, 8ull * cap));
   CU(dev_alloc(&ctx->staging, (size_t)cap * 120 + 1024));
   carve_swarm((char *)ctx->swarm_mem, cap, ctx->buf[0]);
   carve_swarm((char *)ctx->swarm_mem + per, cap, ctx->buf[1]);
@@ -709,8 +707,8 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
     CU(cudaEventRecord(ctx->ev_corner, ctx->side));
   }
   launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start,
-                       ctx->perm, s, src.pid, ctx->spid);
-  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s, ctx->spid);
+                       ctx->perm, s);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
   size_t e2 = prof ? record_event(ctx, s) : 0;
   if (!locate_only) CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
   size_t e3 = prof ? record_event(ctx, s) : 0;
@@ -789,9 +787,8 @@ int resort(FdfContext *ctx, int remove_lost, int remove_oob, int64_t *removed_lo
   launch_resort_keys(src, ctx->cap, g, f32 ? 1 : 0, remove_lost, remove_oob, ctx->bbox, ctx->fbox, ctx->cnt,
                      ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, s);
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
-  launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, 1, ctx->cell_start, ctx->perm, s,
-                       src.pid, ctx->spid);
-  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s, ctx->spid);
+  launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, 1, ctx->cell_start, ctx->perm, s);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
   if (f32)
     launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s, GATHER_COPY);
   else

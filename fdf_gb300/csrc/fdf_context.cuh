@@ -57,7 +57,6 @@ struct FdfContext {
   int cur = 0;
   void *swarm_mem = nullptr;
   unsigned int *keys = nullptr, *perm = nullptr;   // [cap]: cell key per slot, sorted slot -> previous slot
-  long long *spid = nullptr;                       // [cap]: PID at its sorted position (the sort's scratch)
   unsigned int *rank = nullptr;                    // [cap]: rank of the slot's particle within its new cell
   unsigned int *cell_start = nullptr;              // [Nc+2]: histogram, then its exclusive scan
   unsigned int *scan_sums = nullptr;

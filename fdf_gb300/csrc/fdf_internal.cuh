@@ -192,14 +192,12 @@ size_t scan_scratch_words(long long count);
 long long scan_max_count();
 void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums, cudaStream_t s);
 // perm[cell_start[key] + rank[s]] = s for every kept particle (keys and ranks from the locate
-// kernels' histogram); with spid, also spid[same position] = pid[s].
+// kernels' histogram).
 void launch_scatter_slots(const unsigned int *keys, const unsigned int *rank, int n_cap, const DevCounters *cnt,
                           unsigned int sentinel, int keep_lost, const unsigned int *cell_start, unsigned int *perm,
-                          cudaStream_t s, const long long *pid = nullptr, long long *spid = nullptr);
-// Orders every cell's slots by (PID, previous slot), or by previous slot when pid is null; spid
-// (optional): the PIDs as launch_scatter_slots placed them, read in place of pid[perm[.]].
+                          cudaStream_t s);
 void launch_order_segments(const unsigned int *cell_start, int nseg, const long long *pid, unsigned int *perm,
-                           cudaStream_t s, const long long *spid = nullptr);
+                           cudaStream_t s);
 void cell_sort_on_scratch(const int *cell, long long n, long long ncells, unsigned int *perm,
                           unsigned int *cell_start, unsigned int *cursor, unsigned int *sums, cudaStream_t s);
 

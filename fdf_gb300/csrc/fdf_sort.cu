@@ -115,25 +115,19 @@ __global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__res
                                                       const unsigned int *__restrict__ rank, const DevCounters *cnt,
                                                       unsigned int sentinel, int keep_lost,
                                                       const unsigned int *__restrict__ cell_start,
-                                                      unsigned int *__restrict__ perm,
-                                                      const long long *__restrict__ pid,
-                                                      long long *__restrict__ spid) {
+                                                      unsigned int *__restrict__ perm) {
   const int n = cnt->n_sorted;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const unsigned int key = keys[s];   // sentinel: a LOST particle kept at the end; above: removed
   if (key > sentinel || (key == sentinel && !keep_lost)) return;
-  const unsigned int dst = cell_start[key] + rank[s];
-  perm[dst] = (unsigned int)s;
-  if (spid) spid[dst] = pid[s];   // read in order here, so the ordering pass reads it in place
+  perm[cell_start[key] + rank[s]] = (unsigned int)s;
 }
 
 // Orders every cell's slots by (PID, previous slot) -- or by previous slot alone when
 // pid is null.  Segments are short (a few particles per cell on average): up to 8 entries
 // are checked and, when out of order, sorted in registers by a 19-comparator sorting
-// network; longer ones are insertion-sorted in place in global memory.  With spid (the PIDs
-// at their unordered sorted positions) a short segment reads its keys contiguously instead of
-// through perm, which turns the dependent gathers into loads the warp issues together.
+// network; longer ones are insertion-sorted in place in global memory.
 constexpr int SEG_NET = 8;
 
 __device__ __forceinline__ bool key_gt(long long ka, unsigned int va, long long kb, unsigned int vb) {
@@ -142,8 +136,7 @@ __device__ __forceinline__ bool key_gt(long long ka, unsigned int va, long long 
 
 __global__ void __launch_bounds__(256, FDF_ORDER_MIN_BLOCKS) k_order_segments(const unsigned int *__restrict__ cell_start, int nseg,
                                                        const long long *__restrict__ pid,
-                                                       unsigned int *__restrict__ perm,
-                                                       const long long *__restrict__ spid) {
+                                                       unsigned int *__restrict__ perm) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nseg) return;
   const unsigned int s0 = cell_start[c], s1 = cell_start[c + 1];
@@ -160,7 +153,7 @@ __global__ void __launch_bounds__(256, FDF_ORDER_MIN_BLOCKS) k_order_segments(co
       ix[q] = 0xffffffffu;
       if (q < (int)L) {
         ix[q] = perm[s0 + q];
-        kp[q] = spid ? spid[s0 + q] : pid ? pid[ix[q]] : (long long)ix[q];
+        kp[q] = pid ? pid[ix[q]] : (long long)ix[q];
         if (q > 0 && key_gt(kp[q - 1], ix[q - 1], kp[q], ix[q])) sorted = false;
       }
     }
@@ -248,19 +241,18 @@ void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums,
 
 void launch_scatter_slots(const unsigned int *keys, const unsigned int *rank, int n_cap, const DevCounters *cnt,
                           unsigned int sentinel, int keep_lost, const unsigned int *cell_start, unsigned int *perm,
-                          cudaStream_t s, const long long *pid, long long *spid) {
+                          cudaStream_t s) {
   int th = 256;
   int blocks = (n_cap + th - 1) / th;
   if (blocks == 0) blocks = 1;
-  k_scatter_slots<<<blocks, th, 0, s>>>(keys, rank, cnt, sentinel, keep_lost, cell_start, perm, pid,
-                                        pid ? spid : nullptr);
+  k_scatter_slots<<<blocks, th, 0, s>>>(keys, rank, cnt, sentinel, keep_lost, cell_start, perm);
 }
 
 void launch_order_segments(const unsigned int *cell_start, int nseg, const long long *pid, unsigned int *perm,
-                           cudaStream_t s, const long long *spid) {
+                           cudaStream_t s) {
   int th = 256;
   int blocks = (nseg + th - 1) / th;
-  k_order_segments<<<blocks, th, 0, s>>>(cell_start, nseg, pid, perm, pid ? spid : nullptr);
+  k_order_segments<<<blocks, th, 0, s>>>(cell_start, nseg, pid, perm);
 }
 
 // Stable counting sort of particle slots by cell id, on caller-provided scratch:
