@@ -281,14 +281,19 @@ MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, on
 # units the stage processed then: live particles, or guessed particles for the network and
 # the walk from the guess.
 TRAFFIC = {
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (8.665e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (0.597e9, "guesses", 12.92e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (3.941e9, "guesses", 12.92e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (7.757e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (0.596e9, "guesses", 12.92e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (2.063e9, "guesses", 12.92e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "sort_by_cell"): (1.870e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.906e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (8.314e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "deposit"): (1.345e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (7.623e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "sort_by_cell"): (1.870e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.906e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "advect_locate"): (14.193e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "gather_interpolate"): (10.884e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "deposit"): (1.345e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "advect_locate"): (13.444e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "gather_interpolate"): (10.885e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "deposit"): (2.651e9, "particles", 63.81e6),
 }
 
 

@@ -154,8 +154,13 @@ inline cudaError_t dev_alloc(T **p, size_t bytes) {
 }
 
 
+// Bytes of one swarm buffer, a multiple of 256: the second buffer of the pair starts at this
+// offset, and its arrays keep the 256-B alignment of the first's (the deposit's bulk copies need
+// 16-B aligned sources).
 inline size_t swarm_bytes_per_buf(int cap) {
-  return (size_t)cap * (10 * sizeof(double) + 7 * sizeof(float) + sizeof(long long) + sizeof(int) + 1) + 24 * 256;
+  const size_t b =
+      (size_t)cap * (10 * sizeof(double) + 7 * sizeof(float) + sizeof(long long) + sizeof(int) + 1) + 24 * 256;
+  return (b + 255) / 256 * 256;
 }
 
 inline void carve_swarm(char *p, int cap, SwarmBuf &b) {
