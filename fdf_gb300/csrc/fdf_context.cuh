@@ -14,8 +14,7 @@ struct LocatorState {
   bool has_params = false;
   float *params = nullptr;            // [MLP_NPARAM] FP32 master weights
   float *grads = nullptr, *adam_m = nullptr, *adam_v = nullptr;
-  __nv_bfloat16 *params_bf = nullptr; // bfloat16 copy the training GEMMs read
-  __nv_bfloat16 *w1x = nullptr;       // [128][6] W1 repeated for the inputs' (hi, lo) pairs
+  unsigned char *train_img = nullptr; // bfloat16 image of the weights the training step reads
   unsigned char *tc_img = nullptr;    // inference weights as the tcgen05 kernel's shared-memory image
   int infer_bf16 = 1;                 // inference operands: bfloat16 (1) or half precision (0)
   float *bias = nullptr;

@@ -7,10 +7,10 @@
 //   samples   n points seeded like the volumetric initialisation (random cell, random
 //             logical coordinates), each located by the plain FP64 walk from its generating
 //             cell; the located (position, cell) pairs become (xhat, target) in FP32
-//   step t    minibatch by counter hash -> forward (4 tcgen05 GEMMs, bias + SiLU) ->
-//             loss and dloss/dy -> backward (dW by split-K GEMMs reduced in fixed order,
-//             dH by GEMMs, SiLU', bias sums) -> Adam on the FP32 master weights ->
-//             bfloat16 copy for the next step
+//   step t    two launches: k_train_tc (one CTA per 128-sample tile of the minibatch drawn by
+//             counter hash: forward, loss and backward on tcgen05, the tile's gradient
+//             partials) and k_train_update (partials added in tile order, Adam on the FP32
+//             master weights, their bfloat16 image rewritten for the next step)
 //   finally   weights packed into the tcgen05 inference kernel's shared-memory image
 #include "fdf_context.cuh"
 
@@ -20,38 +20,18 @@
 
 namespace {
 
+// Training scratch for batches of up to B samples: the tiles' gradient partials and losses (and the
+// batch's loss), the
+// samples of an explicit batch (fdf_LocatorGradients) and the tensor-core time-out word.
 struct TrainScratch {
-  __nv_bfloat16 *X, *H[4], *Gb, *Gb4;   // X [B][6]: the inputs' bfloat16 pairs
-  float *T, *C, *Z[4], *dH, *G, *Y, *G4, *loss_part, *partials;
-  float *dW1x;                          // [128][6] gradient of W1x = [W1 | W1]
-  unsigned int *err;                    // the GEMMs' tensor-core time-out bit
-  int splits;
+  float *part, *loss_part, *xs, *ts;
+  unsigned int *err;
 };
 
-int splits_for(int B) {
-  int sp = B / 256;
-  if (sp < 1) sp = 1;
-  if (sp > 64) sp = 64;
-  return sp;
-}
-
 size_t scratch_bytes(int B) {
-  const size_t r = 256;
-  auto up = [&](size_t b) { return (b + r - 1) / r * r; };
-  const size_t bh = (size_t)B * MLP_H;
-  size_t t = 0;
-  t += up(2 * 6 * (size_t)B);                      // X
-  t += 3 * up(2 * bh);                             // H1..H3
-  t += up(2 * bh) + up(2 * 3 * (size_t)B);         // Gb, Gb4
-  t += up(4 * 3 * (size_t)B);                      // T
-  t += up(4 * bh);                                 // C
-  t += 3 * up(4 * bh);                             // Z1..Z3
-  t += 2 * up(4 * bh);                             // dH, G
-  t += 2 * up(4 * 3 * (size_t)B);                  // Y, G4
-  t += up(4 * ((size_t)B / 256 + 2));              // loss partials
-  t += up(4 * (size_t)splits_for(B) * MLP_H * MLP_H);
-  t += up(4 * MLP_H * 6) + up(4);                  // dW1x, err
-  return t;
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t tiles = (size_t)mlp_train_tiles(B);
+  return up(4 * tiles * MLP_PART_STRIDE) + up(4 * (tiles + 1)) + 2 * up(12 * (size_t)B) + up(4);
 }
 
 TrainScratch carve_scratch(void *base, int B) {
@@ -61,42 +41,28 @@ TrainScratch carve_scratch(void *base, int B) {
     p += (bytes + 255) / 256 * 256;
     return (void *)r;
   };
-  const size_t bh = (size_t)B * MLP_H;
+  const size_t tiles = (size_t)mlp_train_tiles(B);
   TrainScratch s{};
-  s.X = (__nv_bfloat16 *)take(2 * 6 * (size_t)B);
-  s.H[0] = s.X;
-  for (int l = 1; l < 4; ++l) s.H[l] = (__nv_bfloat16 *)take(2 * bh);
-  s.Gb = (__nv_bfloat16 *)take(2 * bh);
-  s.Gb4 = (__nv_bfloat16 *)take(2 * 3 * (size_t)B);
-  s.T = (float *)take(4 * 3 * (size_t)B);
-  s.C = (float *)take(4 * bh);
-  s.Z[0] = nullptr;
-  for (int l = 1; l < 4; ++l) s.Z[l] = (float *)take(4 * bh);
-  s.dH = (float *)take(4 * bh);
-  s.G = (float *)take(4 * bh);
-  s.Y = (float *)take(4 * 3 * (size_t)B);
-  s.G4 = (float *)take(4 * 3 * (size_t)B);
-  s.loss_part = (float *)take(4 * ((size_t)B / 256 + 2));
-  s.splits = splits_for(B);
-  s.partials = (float *)take(4 * (size_t)s.splits * MLP_H * MLP_H);
-  s.dW1x = (float *)take(4 * MLP_H * 6);
+  s.part = (float *)take(4 * tiles * MLP_PART_STRIDE);
+  s.loss_part = (float *)take(4 * (tiles + 1));   // the tiles' losses, then the batch's
+  s.xs = (float *)take(12 * (size_t)B);
+  s.ts = (float *)take(12 * (size_t)B);
   s.err = (unsigned int *)take(4);
   return s;
 }
 
 int alloc_params(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
-  if (L.params && L.grads && L.adam_m && L.adam_v && L.params_bf && L.w1x && L.bias && L.tc_img) return FDF_SUCCESS;
+  if (L.params && L.grads && L.adam_m && L.adam_v && L.train_img && L.bias && L.tc_img) return FDF_SUCCESS;
   // all or none: a partial set left by a failed allocation is freed and made again
   L.has_params = false;
-  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf); cfree(L.w1x);
+  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.train_img);
   cfree(L.bias); cfree(L.tc_img);
   CU(dev_alloc(&L.params, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.grads, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.adam_m, 4ull * MLP_NPARAM));
   CU(dev_alloc(&L.adam_v, 4ull * MLP_NPARAM));
-  CU(dev_alloc(&L.params_bf, 2ull * MLP_NPARAM));
-  CU(dev_alloc(&L.w1x, 2ull * MLP_H * 6));
+  CU(dev_alloc(&L.train_img, MLP_IMG_BYTES));
   CU(dev_alloc(&L.bias, 4ull * MLP_BIAS_WORDS));
   CU(dev_alloc(&L.tc_img, mlp_tc_image_bytes()));
   return FDF_SUCCESS;
@@ -121,68 +87,26 @@ void set_norm(FdfContext *ctx) {
   }
 }
 
-// Makes the bfloat16 copies of the weights the training GEMMs read.
-void training_weights(FdfContext *ctx, cudaStream_t s) {
-  LocatorState &L = ctx->loc;
-  mlp_to_bf16(L.params, L.params_bf, MLP_NPARAM, s);
-  mlp_split_w1(L.params_bf + MLP_OFF_W1, L.w1x, s);
-  ctx->launches += 2;
-}
-
-// The training copies and the inference packing.
+// The weights' images: bfloat16 for training, the inference kernel's operand type and biases.
 void refresh_weights(FdfContext *ctx, cudaStream_t s) {
   LocatorState &L = ctx->loc;
-  training_weights(ctx, s);
+  mlp_pack_tc(L.params, L.train_img, 1, s);
   mlp_pack_bias(L.params, L.bias, s);
   mlp_pack_tc(L.params, L.tc_img, L.infer_bf16, s);
-  ctx->launches += 2;
+  ctx->launches += 3;
 }
 
-// Loss and gradients (into L.grads) of the batch in scratch (X, T), current weights.
-void forward_backward(FdfContext *ctx, const TrainScratch &S, int B, float *loss_out, cudaStream_t s) {
-  LocatorState &L = ctx->loc;
-  const __nv_bfloat16 *Wb[4] = {L.w1x, L.params_bf + MLP_OFF_W2, L.params_bf + MLP_OFF_W3,
-                                L.params_bf + MLP_OFF_W4};
-  const float *bvec[4] = {L.params + MLP_OFF_B1, L.params + MLP_OFF_B2, L.params + MLP_OFF_B3, L.params + MLP_OFF_B4};
-  float *dW[4] = {S.dW1x, L.grads + MLP_OFF_W2, L.grads + MLP_OFF_W3, L.grads + MLP_OFF_W4};
-  float *db[4] = {L.grads + MLP_OFF_B1, L.grads + MLP_OFF_B2, L.grads + MLP_OFF_B3, L.grads + MLP_OFF_B4};
-  const int fin[4] = {6, MLP_H, MLP_H, MLP_H};   // layer 1 reads the inputs' (hi, lo) pairs against W1x
-  // forward: C = H_{l} W_l^T (A = H [B][fin], B(k, n) = W[n][k])
-  for (int l = 0; l < 3; ++l) {
-    mlp_gemm(S.H[l], fin[l], 1, Wb[l], 1, fin[l], S.C, MLP_H, 1, B, MLP_H, fin[l], 1, nullptr, S.err, s);
-    mlp_bias_silu(S.C, bvec[l], B, MLP_H, S.Z[l + 1], S.H[l + 1], s);
-  }
-  mlp_gemm(S.H[3], MLP_H, 1, Wb[3], 1, MLP_H, S.C, 3, 1, B, 3, MLP_H, 1, nullptr, S.err, s);
-  float sc[3];
+// Output scale of the loss: errors are measured in cells per axis.
+void loss_scale(const FdfContext *ctx, float sc[3]) {
   const int N[3] = {ctx->g.IM, ctx->g.JM, ctx->g.KM};
   for (int d = 0; d < 3; ++d) sc[d] = 0.5f * (float)N[d];
-  mlp_out_loss(S.C, bvec[3], S.T, B, sc, S.Y, S.G4, S.Gb4, S.loss_part, s);
-  mlp_sum_partials(S.loss_part, (B + 255) / 256, loss_out, s);
-  // backward, layer 4 then 3, 2, 1: g = dloss/dz_l (FP32 G, bfloat16 Gb)
-  const __nv_bfloat16 *gb = S.Gb4;
-  const float *g = S.G4;
-  int nout = 3;
-  for (int l = 3; l >= 0; --l) {
-    // dW_l [nout][fin] = sum_b gb[b][o] h_l[b][i]: A(m = o, k = b) = gb[b*nout + o], B(k = b, n = i) = h[b*fin + i]
-    mlp_gemm(gb, 1, nout, S.H[l], fin[l], 1, dW[l], fin[l], 1, nout, fin[l], B, S.splits, S.partials, S.err, s);
-    mlp_colsum(g, B, nout, db[l], s);
-    if (l == 0) break;
-    // dH_l [B][fin] = gb @ W_l: A(m = b, k = o) = gb[b*nout + o], B(k = o, n = i) = W[o*fin + i]
-    mlp_gemm(gb, nout, 1, Wb[l], fin[l], 1, S.dH, MLP_H, 1, B, MLP_H, nout, 1, nullptr, S.err, s);
-    mlp_silu_bwd(S.dH, S.Z[l], (long long)B * MLP_H, S.G, S.Gb, s);
-    gb = S.Gb;
-    g = S.G;
-    nout = MLP_H;
-  }
-  mlp_fold_w1(S.dW1x, L.grads + MLP_OFF_W1, s);
-  ctx->launches += 2 * 3 + 1 + 2 + 4 * 2 + 3 * 2 + 4 * (S.splits > 1 ? 1 : 0) + 1;
 }
 
 }  // namespace
 
 void locator_free(FdfContext *ctx) {
   LocatorState &L = ctx->loc;
-  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.params_bf); cfree(L.w1x);
+  cfree(L.params); cfree(L.grads); cfree(L.adam_m); cfree(L.adam_v); cfree(L.train_img);
   cfree(L.bias); cfree(L.tc_img); cfree(L.pending); cfree(L.guess); cfree(L.scratch); cfree(L.pflag);
   cfree(L.scan_sums);
   L.pending_cap = 0;
@@ -275,13 +199,19 @@ int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target
   if (r) return r;
   TrainScratch S = carve_scratch(ctx->loc.scratch, ctx->loc.batch_cap);
   cudaStream_t s = ctx->stream;
-  // xhat goes through the G buffer (FP32) into X (its bfloat16 pairs)
-  CU(cudaMemcpyAsync(S.G, xhat, 12ull * B, cudaMemcpyHostToDevice, s));
-  CU(cudaMemcpyAsync(S.T, target, 12ull * B, cudaMemcpyHostToDevice, s));
+  LocatorState &L = ctx->loc;
+  CU(cudaMemcpyAsync(S.xs, xhat, 12ull * B, cudaMemcpyHostToDevice, s));
+  CU(cudaMemcpyAsync(S.ts, target, 12ull * B, cudaMemcpyHostToDevice, s));
   CU(cudaMemsetAsync(S.err, 0, 4, s));
-  mlp_split_inputs(S.G, B, S.X, s);
-  float *d_loss = S.loss_part + (B + 255) / 256;
-  forward_backward(ctx, S, B, d_loss, s);
+  float sc[3];
+  loss_scale(ctx, sc);
+  float *d_loss = S.loss_part + mlp_train_tiles(B);
+  CU(cudaMemsetAsync(d_loss, 0, 4, s));
+  mlp_pack_tc(L.params, L.train_img, 1, s);
+  mlp_train_step(L.train_img, L.params, S.xs, S.ts, B, 0, 0, 0, B, sc, S.part, S.loss_part, S.err, s);
+  mlp_train_update(S.part, mlp_train_tiles(B), S.loss_part, L.params, L.grads, nullptr, nullptr, L.train_img, d_loss,
+                   0, 0.f, 1.f, 1.f, s);
+  ctx->launches += 3;
   CHECK_LAUNCH();
   unsigned int errw = 0;
   CU(cudaMemcpyAsync(grads, ctx->loc.grads, 4ull * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
@@ -374,15 +304,20 @@ int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t 
   TrainScratch S = carve_scratch(L.scratch, L.batch_cap);
   CUT(cudaMalloc((void **)&hist_loss, 4ull * (steps > 0 ? steps : 1)));
   CUT(cudaMemsetAsync(S.err, 0, 4, s));
+  float sc[3];
+  loss_scale(ctx, sc);
+  const int tiles = mlp_train_tiles(B);
+  mlp_pack_tc(L.params, L.train_img, 1, s);
+  ctx->launches += 1;
   const double pi = 3.14159265358979323846;
   for (long long t = 0; t < steps; ++t) {
-    mlp_gather_batch(xs, ts, m, seed ^ 0x5DEECE66DULL, t, B, S.X, S.T, s);
-    forward_backward(ctx, S, B, hist_loss + t, s);
+    mlp_train_step(L.train_img, L.params, xs, ts, m, seed ^ 0x5DEECE66DULL, t, 1, B, sc, S.part, S.loss_part, S.err,
+                   s);
     const double lr_t = lr * (0.02 + 0.98 * 0.5 * (1.0 + std::cos(pi * (double)t / (double)steps)));
     L.adam_t += 1;
     const double c1 = 1.0 - std::pow(0.9, (double)L.adam_t), c2 = 1.0 - std::pow(0.999, (double)L.adam_t);
-    mlp_adam(L.params, L.grads, L.adam_m, L.adam_v, MLP_NPARAM, (float)lr_t, (float)c1, (float)c2, s);
-    training_weights(ctx, s);
+    mlp_train_update(S.part, tiles, S.loss_part, L.params, L.grads, L.adam_m, L.adam_v, L.train_img, hist_loss + t, 1,
+                     (float)lr_t, (float)c1, (float)c2, s);
     ctx->launches += 2;
     if ((t & 255) == 255) CUT(cudaGetLastError());
   }

@@ -22,32 +22,25 @@
 
 #define MLP_BIAS_WORDS 392      // b1/2 | b2/2 | b3/2 | b4 (387 used; hidden biases halved for the SiLU epilogue)
 
+// The weights' shared-memory image (16-bit, K-major core-matrix layout of fdf_tc.cuh), shared by
+// inference and training: W1 [128][16] (K padded from 3; the bfloat16 image repeats W1 in
+// columns 3-5 for the inputs' low parts), W2 and W3 [128][128], W4 [16][128] (N padded from 3).
+#define MLP_IMG_W1 0
+#define MLP_IMG_W2 4096
+#define MLP_IMG_W3 36864
+#define MLP_IMG_W4 69632
+#define MLP_IMG_BYTES 73728
+
+// Per-tile gradient partials of the fused training step: one row of MLP_PART_STRIDE floats per
+// 128-sample tile, in the parameter layout.
+#define MLP_PART_STRIDE 33936
+
 // Input normalisation xhat = (x - centre) * inv_half, in FP32.
 struct MlpNorm {
   float centre[3];
   float inv_half[3];
 };
 
-// Training building blocks (all on stream s, deterministic).  mlp_gemm runs on tcgen05 and sets
-// ERRBIT_TC_TIMEOUT in *err if a tensor-core wait runs out.  X rows are the inputs' bfloat16
-// pairs [hi x, y, z, lo x, y, z] (mlp_split_inputs), multiplied by W1x = [W1 | W1]
-// (mlp_split_w1); mlp_fold_w1 adds the two column groups of the W1x gradient.
-void mlp_gemm(const __nv_bfloat16 *A, long long sam, long long sak, const __nv_bfloat16 *B, long long sbk,
-              long long sbn, float *C, long long scm, long long scn, int M, int N, int K, int splits,
-              float *partials, unsigned int *err, cudaStream_t s);
-void mlp_gather_batch(const float *xs, const float *ts, long long n_samples, unsigned long long seed, long long step,
-                      int B, __nv_bfloat16 *X, float *T, cudaStream_t s);
-void mlp_split_inputs(const float *xs, int B, __nv_bfloat16 *X, cudaStream_t s);
-void mlp_split_w1(const __nv_bfloat16 *w1, __nv_bfloat16 *w1x, cudaStream_t s);
-void mlp_fold_w1(const float *dw1x, float *dw1, cudaStream_t s);
-void mlp_bias_silu(const float *C, const float *b, int B, int N, float *Z, __nv_bfloat16 *H, cudaStream_t s);
-void mlp_out_loss(const float *C4, const float *b4, const float *T, int B, const float sc[3], float *Y, float *G,
-                  __nv_bfloat16 *Gb, float *loss_part, cudaStream_t s);
-void mlp_silu_bwd(const float *dH, const float *Z, long long total, float *G, __nv_bfloat16 *Gb, cudaStream_t s);
-void mlp_colsum(const float *G, int B, int N, float *db, cudaStream_t s);
-void mlp_adam(float *w, const float *g, float *m, float *v, int n, float lr, float c1, float c2, cudaStream_t s);
-void mlp_to_bf16(const float *in, __nv_bfloat16 *out, int n, cudaStream_t s);
-void mlp_sum_partials(const float *part, int n, float *out, cudaStream_t s);
 void mlp_pack_bias(const float *params, float *bias, cudaStream_t s);
 
 // Training samples from located points: xs = normalised FP32 position, ts = cell-centre target.
@@ -56,6 +49,21 @@ void mlp_make_samples(const double *x, const double *y, const double *z, const i
                       const unsigned int *keep, long long n, MlpNorm norm, GridDims g, float *xs, float *ts,
                       cudaStream_t s);
 void mlp_flag_located(const int *cell, const unsigned char *status, long long n, unsigned int *flag, cudaStream_t s);
+
+// Fused training step on tcgen05 (fdf_mlp.cu): the loss and gradients of a batch of B samples,
+// one CTA per 128-sample tile.  Sample b of the batch is xs/ts row mix64(seed, step, b) mod n
+// (hashed != 0, the training minibatch) or row b (hashed == 0).  wimg is the bfloat16 image of
+// the current weights, params the FP32 parameters (the biases are read from there).  Each tile
+// writes its gradient partials to part [tiles][MLP_PART_STRIDE] and its share of the loss to
+// loss_part [tiles].  mlp_train_update then adds the partials in tile order into grads (and the
+// loss into *loss_out), and with adam != 0 takes the Adam step on params and rewrites wimg.
+void mlp_train_step(const unsigned char *wimg, const float *params, const float *xs, const float *ts,
+                    long long n_samples, unsigned long long seed, long long step, int hashed, int B,
+                    const float sc[3], float *part, float *loss_part, unsigned int *err, cudaStream_t s);
+void mlp_train_update(const float *part, int tiles, const float *loss_part, float *params, float *grads, float *m,
+                      float *v, unsigned char *wimg, float *loss_out, int adam, float lr, float c1, float c2,
+                      cudaStream_t s);
+inline int mlp_train_tiles(int B) { return (B + 127) / 128; }
 
 // Initial weights: W uniform in +-1/sqrt(fan_in) from the splitmix64 streams (seed, 100 + layer),
 // biases zero (host).

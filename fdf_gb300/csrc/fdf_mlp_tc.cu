@@ -37,11 +37,11 @@ constexpr int TC_PIPES = 4;                  // warpgroups per CTA, one tile pip
 constexpr int TC_THREADS = 128 * TC_PIPES;
 constexpr int TC_TMEM_COLS = 128 * TC_PIPES; // FP32 accumulator columns, 128 per pipeline
 // shared memory map (bytes)
-constexpr int SM_W1 = 0;                     // [128][16]  4096
-constexpr int SM_W2 = SM_W1 + 4096;          // [128][128] 32768
-constexpr int SM_W3 = SM_W2 + 32768;         // [128][128] 32768
-constexpr int SM_W4 = SM_W3 + 32768;         // [16][128]  4096
-constexpr int SM_PIPE = SM_W4 + 4096;        // per pipeline: A1 [128][16] 4096, A [128][128] 32768
+constexpr int SM_W1 = MLP_IMG_W1;            // [128][16]  4096
+constexpr int SM_W2 = MLP_IMG_W2;            // [128][128] 32768
+constexpr int SM_W3 = MLP_IMG_W3;            // [128][128] 32768
+constexpr int SM_W4 = MLP_IMG_W4;            // [16][128]  4096
+constexpr int SM_PIPE = MLP_IMG_BYTES;       // per pipeline: A1 [128][16] 4096, A [128][128] 32768
 constexpr int PIPE_BYTES = 4096 + 32768;
 constexpr int SM_BIAS = SM_PIPE + TC_PIPES * PIPE_BYTES;   // 392 floats
 constexpr int SM_HB2 = SM_BIAS + 1568;       // the hidden half-biases as 192 16-bit pairs

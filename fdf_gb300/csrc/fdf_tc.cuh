@@ -31,6 +31,15 @@ __host__ __device__ constexpr unsigned make_idesc(int M, int N, bool bf16) {
   return (1u << 4) | (bf16 ? (1u << 7) | (1u << 10) : 0u) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
 }
 
+// The same with either operand read MN-major (transposed): a matrix stored K-major as rows r,
+// columns c (element (r, c) at op_off(r, c, sbo)) is, read MN-major, the operand whose M (or N)
+// index is c and whose K index is r.  Its descriptor then takes the leading byte offset sbo
+// (between 8-row groups of r, its K direction) and the stride byte offset 128 (between
+// 8-element groups of c); one K step of 16 is 2 sbo bytes.
+__host__ __device__ constexpr unsigned make_idesc_t(int M, int N, bool bf16, bool a_mn, bool b_mn) {
+  return make_idesc(M, N, bf16) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+
 __device__ __forceinline__ void mma_f16(unsigned tmem_d, unsigned long long adesc, unsigned long long bdesc,
                                         unsigned idesc, unsigned accumulate) {
   asm volatile(

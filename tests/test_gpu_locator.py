@@ -56,13 +56,13 @@ def test_init_matches_oracle(small):
     assert np.array_equal(ctx.locator_get_params(), flat(M.init_params(seed=3)))
 
 
-def test_gradients_match_oracle(small):
+@pytest.mark.parametrize("B", [512, 300])   # whole 128-sample tiles, and a last tile partly empty
+def test_gradients_match_oracle(small, B):
     ctx, wl = small
     dims = wl.dims
     rng = np.random.default_rng(11)
     params = [(W_, (0.2 * rng.standard_normal(b.shape)).astype(np.float32)) for W_, b in M.init_params(seed=4)]
     ctx.locator_set_params(flat(params))
-    B = 512
     xhat = rng.uniform(-1, 1, size=(B, 3)).astype(np.float32)
     cells = np.stack([rng.integers(0, d, size=B) for d in dims], axis=1)
     t = M.targets(cells, dims).astype(np.float32)
