@@ -22,10 +22,13 @@
 
 namespace {
 
-// SiLU and its derivative in FP32 (training).
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + expf(-z)); }
+// SiLU and its derivative in FP32 (training): s = sigmoid(z) from the fast exponential and
+// division intrinsics (s -> 0 as z -> -inf: 1 / (1 + inf) is 0), SiLU = z s,
+// SiLU' = s (1 + z (1 - s)).
+__device__ __forceinline__ float sigmoid_f(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigmoid_f(z); }
 __device__ __forceinline__ float silu_grad(float z) {
-  const float s = 1.0f / (1.0f + expf(-z));
+  const float s = sigmoid_f(z);
   return s * (1.0f + z * (1.0f - s));
 }
 
@@ -85,15 +88,15 @@ __global__ void k_pack_bias(const float *__restrict__ params, float *__restrict_
 // operands, FP32 accumulators, FP32 bias add, SiLU and SiLU' in FP32); H1 and H2 are recomputed
 // from C1 and C2 for the backward instead of being kept.
 //
-// Sample row r of the tile is TMEM lane r; its two threads (warps w and w + 4 share the lane
-// quarter of w % 4) take accumulator columns 0-63 and 64-127.  The tile's gradient partials
+// Sample row r of the tile is TMEM lane r; its four threads (warps w, w + 4, w + 8, w + 12 share
+// the lane quarter of w % 4) take accumulator columns 0-31, 32-63, 64-95 and 96-127.  The tile's gradient partials
 // (dW of its rows, bias sums, loss) go to part [tile][MLP_PART_STRIDE] in the parameter layout;
 // k_train_update adds them in tile order, so the result does not depend on scheduling.
 //
 // Tensor memory: C1 columns 0-127, C2 128-255, C3 256-383, working accumulator 384-511; the
 // dH of a layer lands in the columns of the C it no longer needs.  Every wait is bounded: past
 // the limit the CTA records ERRBIT_TC_TIMEOUT, frees its tensor memory and returns.
-constexpr int TT_THREADS = 256;
+constexpr int TT_THREADS = 512;
 constexpr unsigned TT_SM_X = MLP_IMG_BYTES;          // [128][16]  inputs' bfloat16 pairs
 constexpr unsigned TT_SM_H = TT_SM_X + 4096;         // [128][128] activations of one layer
 constexpr unsigned TT_SM_G = TT_SM_H + 32768;        // [128][128] gradient of a hidden layer's output
@@ -151,7 +154,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
   using namespace fdftc;
   extern __shared__ __align__(1024) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2;
+  const int quarter = warp & 3, cg = warp >> 2;   // lane quarter, column group
   const int row = 32 * quarter + lane;                       // sample row = TMEM lane
   const unsigned lane_base = (unsigned)(32 * quarter) << 16;
   const long long tile = blockIdx.x;
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
                                                                                        : MLP_OFF_B4 + q - 384];
   }
   float tgt[3] = {0.f, 0.f, 0.f};
-  if (half == 0) {   // the sample: X row [hi x, y, z, lo x, y, z, 0, ...], its target in registers
+  if (cg == 0) {   // the sample: X row [hi x, y, z, lo x, y, z, 0, ...], its target in registers
     float x[3] = {0.f, 0.f, 0.f};
     if (valid) {
       long long si = b;
@@ -238,8 +241,8 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
   // hidden-layer epilogue: H = bf16(SiLU(C + b)) into the activation buffer
   auto epi_hidden = [&](unsigned cc, const float *bl) {
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      const int col = 64 * half + 16 * c;
+    for (int c = 0; c < 2; ++c) {
+      const int col = 32 * cg + 16 * c;
       float v[16];
       tmem_ld16(tl + cc + (unsigned)col, v);
       unsigned w[8];
@@ -253,8 +256,8 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
   // the warp's column sums of G into red[quarter][column]
   auto epi_back = [&](unsigned dc, unsigned cc, const float *bl) {
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      const int col = 64 * half + 16 * c;
+    for (int c = 0; c < 2; ++c) {
+      const int col = 32 * cg + 16 * c;
       float dv[16], zv[16];
       tmem_ld16(tl + dc + (unsigned)col, dv);
       tmem_ld16(tl + cc + (unsigned)col, zv);
@@ -270,11 +273,11 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
       if ((lane & 1) == 0) red[quarter * 128 + col + colsum16_column(lane)] = cs;
     }
   };
-  // this thread's 64 columns of a 128 x 128 dW in the working columns, as row `row` of W
+  // this thread's 32 columns of a 128 x 128 dW in the working columns, as row `row` of W
   auto store_dw = [&](int off) {
 #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-      const int col = 64 * half + 16 * c;
+    for (int c = 0; c < 2; ++c) {
+      const int col = 32 * cg + 16 * c;
       float v[16];
       tmem_ld16(tl + TT_D + (unsigned)col, v);
       float4 *dst = reinterpret_cast<float4 *>(prt + off + row * 128 + col);
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
     }
     if (!(ok = wait_mma())) break;
     // ---- output: y = C4 + b4, the loss and its gradient G4 = dloss/dy (FP32; bfloat16 operand)
-    if (half == 0) {
+    if (cg == 0) {
       float v[16];
       tmem_ld16(tl + TT_D, v);
       const float sc[3] = {sx, sy, sz};
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
     if (tid < 3) prt[MLP_OFF_B4 + tid] = ((red[tid] + red[128 + tid]) + red[256 + tid]) + red[384 + tid];
     if (tid == 3) loss_part[tile] = (((lsum[0] + lsum[1]) + lsum[2]) + lsum[3]) / (3.0f * (float)B);
     if (!(ok = wait_mma())) break;
-    if (half == 0) {
+    if (cg == 0) {
       float v[16];
       tmem_ld16(tl + TT_D, v);
 #pragma unroll
@@ -423,7 +426,7 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
     }
     store_db(MLP_OFF_B1);
     if (!(ok = wait_mma())) break;
-    if (half == 0) {
+    if (cg == 0) {
       float v[16];
       tmem_ld16(tl + TT_D, v);
 #pragma unroll
