@@ -277,18 +277,20 @@ LOCATOR_TYPES = {"bf16": 0, "f16": 1}
 MLP_FLOPS = 2 * (3 * 128 + 128 * 128 + 128 * 128 + 128 * 3)   # per particle, one inference
 
 # DRAM bytes (read + write) per launch of a stage's kernels, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) on this workload at full size, with the
-# units the stage processed then: live particles, or guessed particles for the network and
-# the walk from the guess.
+# (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on this workload at full size, with
+# the units the stage processed then: live particles, or guessed particles for the network and
+# the walk from the guess.  The precision forms' sort stage: scan and slot scatter as captured
+# with the PID-ordered sort, plus the ordering kernel captured since it orders by previous slot
+# (0.364 GB instead of 1.02 GB per launch).
 TRAFFIC = {
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "advect_locate"): (7.757e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "learned_guess"): (0.596e9, "guesses", 12.92e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "guess_walk"): (2.063e9, "guesses", 12.92e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "sort_by_cell"): (1.870e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "sort_by_cell"): (1.213e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "gather_interpolate"): (7.906e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "learned_fp32", "deposit"): (1.345e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "advect_locate"): (7.623e9, "particles", 63.81e6),
-    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "sort_by_cell"): (1.870e9, "particles", 63.81e6),
+    ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "sort_by_cell"): (1.213e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "gather_interpolate"): (7.906e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "fp32", "deposit"): (1.345e9, "particles", 63.81e6),
     ("bent_pipe_96x96x1536_n64000000_cfl4", "plain_fp64", "advect_locate"): (13.444e9, "particles", 63.81e6),

@@ -708,7 +708,9 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
   }
   launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, drop ? 0 : 1, ctx->cell_start,
                        ctx->perm, s);
-  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
+  // the plain form orders each cell by PID (the oracle's summation order); the precision forms
+  // keep each cell's particles in their previous order (no gather of the PIDs)
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), f32 ? nullptr : src.pid, ctx->perm, s);
   size_t e2 = prof ? record_event(ctx, s) : 0;
   if (!locate_only) CU(cudaStreamWaitEvent(s, ctx->ev_corner, 0));
   size_t e3 = prof ? record_event(ctx, s) : 0;
@@ -771,8 +773,9 @@ int run_pipeline(FdfContext *ctx, int advect, int drop, FdfStepInfo *info, bool 
   return FDF_SUCCESS;
 }
 
-// Re-sorts the held particles by (cell, PID) into the other buffer, dropping the LOST and/or
-// the out-of-bounds ones; cell_start then matches the held particles.
+// Re-sorts the held particles by cell -- within a cell by PID in the plain form, in their
+// previous order in the precision forms -- into the other buffer, dropping the LOST and/or the
+// out-of-bounds ones; cell_start then matches the held particles.
 int resort(FdfContext *ctx, int remove_lost, int remove_oob, int64_t *removed_lost, int64_t *removed_oob) {
   if (!ctx->has_grid) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no grid: call fdf_SetGrid first");
   if (!ctx->swarm_set) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "no swarm: call fdf_SetSwarm first");
@@ -788,7 +791,7 @@ int resort(FdfContext *ctx, int remove_lost, int remove_oob, int64_t *removed_lo
                      ctx->keys, ctx->rank, ctx->cell_start, ctx->sentinel, s);
   exclusive_scan_u32(ctx->cell_start, g.Nc + 2, ctx->scan_sums, s);
   launch_scatter_slots(ctx->keys, ctx->rank, ctx->cap, ctx->cnt, ctx->sentinel, 1, ctx->cell_start, ctx->perm, s);
-  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), src.pid, ctx->perm, s);
+  launch_order_segments(ctx->cell_start, (int)(g.Nc + 1), f32 ? nullptr : src.pid, ctx->perm, s);
   if (f32)
     launch_gather_interp32(src, dst, ctx->cap, g, ctx->corner32, ctx->perm, ctx->cell_start, ctx->cnt, s, GATHER_COPY);
   else

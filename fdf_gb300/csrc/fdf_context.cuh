@@ -66,7 +66,7 @@ struct FdfContext {
   int route_up = -1, route_down = -1;     // AUTO: the route measured faster per direction (-1: not yet)
   unsigned int sentinel = 0;
   bool swarm_set = false;
-  bool layout_ok = false;   // the held particles are sorted by (cell, PID) and cell_start matches them
+  bool layout_ok = false;   // the held particles are sorted by cell and cell_start matches them
   int swarm_form = FDF_FORM_PLAIN_FP64;   // form the swarm's device arrays are held in
   int out_form = FDF_FORM_PLAIN_FP64;     // form of the last deposits
   bool out_momentum = false;              // the last deposits include the momentum

@@ -332,7 +332,7 @@ __global__ void k_advect32(SwarmBuf b, float dt32, DevCounters *cnt) {
   st_pair(b.z, s, pair_add(ld_pair(b.z, s), __fmul_rn(b.wf[s], dt32)));
 }
 
-// Sort keys of the particles held (a re-sort by (cell, PID)), dropping the LOST ones
+// Sort keys of the particles held (a re-sort by cell), dropping the LOST ones
 // (CheckAndRemoveLostParticles, ParticleMotion.c:532-625) and/or the ones outside the
 // bounding box (CheckAndRemoveOutOfBoundsParticles, :283-383; the FP32 form decides as the
 // step does).  Kept particles without a cell go to the LOST bucket at the end; the removed

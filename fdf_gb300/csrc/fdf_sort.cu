@@ -7,11 +7,13 @@
 //      particles the initial setup keeps, and removed particles get no slot;
 //   3. each particle takes slot cell_start[key] + its rank within its cell, which the
 //      histogram atomic of step 1 returned;
-//   4. each cell's slots are then ordered by (PID, previous slot), so the final
-//      order -- and every later sum -- is the same on every run, whatever order
-//      the atomics took, and does not depend on the history of the swarm.
-// Sorted order is therefore (cell, PID): the order the oracle uses for the face
-// deposits, which makes those sums comparable bit for bit.
+//   4. each cell's slots are then ordered by (PID, previous slot) in the plain form, so
+//      the final order -- and every later sum -- is the same on every run, whatever
+//      order the atomics took, and does not depend on the history of the swarm: sorted
+//      order is (cell, PID), the order the oracle uses for the face deposits, which makes
+//      those sums comparable bit for bit.  The precision forms order each cell's slots by
+//      previous slot alone (a stable counting sort: the same on every run for the same
+//      input, and no gather of the PIDs), as does the standalone sort.
 #include "fdf_internal.cuh"
 
 namespace {

@@ -237,8 +237,9 @@ int fdf_InterpolatePoints(FdfContext *ctx, int64_t n, const int64_t *cell, const
  * upper rank from the lower rank's partial sums, so the ranks' results together are the one-rank
  * results bit for bit (plain form). */
 /* The held particles whose cell has k outside [k_lo, k_hi) leave the context into the host arrays
- * (DMSwarm layout, in (cell, PID) order: cells below the slab, then above); particles without a
- * cell stay.  *n = the number extracted (FDF_ERR_ARG_OUTOFRANGE, nothing moved, if > n_max). */
+ * (DMSwarm layout, in the held order -- by cell, within a cell by PID in the plain form: cells
+ * below the slab, then above); particles without a cell stay.  *n = the number extracted
+ * (FDF_ERR_ARG_OUTOFRANGE, nothing moved, if > n_max). */
 int fdf_ExtractParticles(FdfContext *ctx, int64_t k_lo, int64_t k_hi, int64_t n_max, int64_t *n, double *position,
                          double *velocity, double *weight, double *P, int64_t *cell_id, int64_t *pid, int64_t *status);
 /* Particles from another rank join the held swarm with their cells, weights and statuses (the

@@ -175,7 +175,8 @@ def _ksum(vals):
 
 def test_fp32_deposit_matches_host_restatement(ctx):
     """The FP32 deposit (warp-staged kernel) against the same float32 arithmetic on the host:
-    particles in the swarm's (cell, PID) order, each face summing its lower cell's a V/3 then
+    particles in the swarm's held order (by cell; within a cell, the precision form keeps the
+    previous order), each face summing its lower cell's a V/3 then
     its own cell's (1 - a) V/3 with Neumaier compensation; count and P average per cell.  Every
     value must be bit-identical."""
     wl = W.config_sinusoidal(IM=32, JM=6, KM=12, n=20_000, cfl=1.0, steps=3)   # 33 nodes per row: a warp starts at i = IM
