@@ -75,6 +75,7 @@ _SIGS = {
     "fdf_SetProfiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fdf_TestFailDeviceAllocations": (ctypes.c_int, [ctypes.c_int64]),
     "fdf_TestLocatorWaitTimeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    "fdf_TestLocatorTrainTimeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     "fdf_GetCounters": (ctypes.c_int, [ctypes.c_void_p, c_int64_p, c_int64_p, c_int64_p]),
     "fdf_GetStageTimes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
     "fdf_LocatorInit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),

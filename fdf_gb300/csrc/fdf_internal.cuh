@@ -129,10 +129,12 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #define FDF_LOC_THREADS 128
 #endif
 // Resident blocks per SM the FP32 locate kernels are compiled for.  The walk is bound by load
-// latency, so 1024 resident threads (64 registers, a few spilled to L1) beat 768 (80, none
-// spilled): 3.9 against 4.8 ms per 64M-particle step; 1280 (48 registers) spills too much.
+// latency, so resident threads beat spills up to a point: with 176-B plane-table rows 1024
+// threads (64 registers) beat 768 (80): 3.9 against 4.8 ms per 64M-particle step, and 1280 (48
+// registers) spilled too much; with the 128-B rows 1152 threads (56 registers, a few more spills)
+// take 3.17 against 3.22 ms for the FP32 walk.
 #ifndef FDF_LOC_MIN_BLOCKS
-#define FDF_LOC_MIN_BLOCKS (1024 / FDF_LOC_THREADS)
+#define FDF_LOC_MIN_BLOCKS (1152 / FDF_LOC_THREADS)
 #endif
 // Resident blocks per SM of the plain walk (its steps decided from the FP32 table; per
 // 64M-particle step 1024 resident threads take 7.6 ms against 8.6 ms at 768 and 8.4 ms at 1280
@@ -144,9 +146,10 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 #ifndef FDF_ORDER_MIN_BLOCKS
 #define FDF_ORDER_MIN_BLOCKS 8
 #endif
-// Resident 256-thread blocks per SM the learned form's walk from P1 is compiled for.
+// Resident 256-thread blocks per SM the learned form's walk from P1 is compiled for (4: 64
+// registers, 0.701 ms per 64M-particle step against 0.712 ms at 3 with 80 registers).
 #ifndef FDF_GUESS_MIN_BLOCKS
-#define FDF_GUESS_MIN_BLOCKS 3
+#define FDF_GUESS_MIN_BLOCKS 4
 #endif
 // Threads per block of the learned form's walk from P1.
 #ifndef FDF_GUESS_THREADS

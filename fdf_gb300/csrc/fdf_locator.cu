@@ -188,9 +188,12 @@ int fdf_LocatorGetNormalization(FdfContext *ctx, float *centre, float *inv_half)
   return FDF_SUCCESS;
 }
 
-int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target, int64_t batch, float *grads,
-                         float *loss) {
-  if (!ctx || !xhat || !target || !grads || !loss) return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorGradients: null argument");
+// fdf_LocatorGradients, and with stall_test the time-out test of fdf_TestLocatorTrainTimeout
+// (the training kernel alone, no MMA issued; grads and loss unused).
+static int locator_gradients(FdfContext *ctx, const float *xhat, const float *target, int64_t batch, float *grads,
+                             float *loss, int stall_test) {
+  if (!ctx || !xhat || !target || (!stall_test && (!grads || !loss)))
+    return fail(ctx, FDF_ERR_ARG_NULL, "fdf_LocatorGradients: null argument");
   if (batch < 1 || batch > 65536) return fail(ctx, FDF_ERR_ARG_OUTOFRANGE, "fdf_LocatorGradients: batch in [1, 65536]");
   if (!ctx->loc.has_params) return fail(ctx, FDF_ERR_ARG_WRONGSTATE, "fdf_LocatorGradients: no locator");
   CU(cudaSetDevice(ctx->device));
@@ -208,18 +211,32 @@ int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target
   float *d_loss = S.loss_part + mlp_train_tiles(B);
   CU(cudaMemsetAsync(d_loss, 0, 4, s));
   mlp_pack_tc(L.params, L.train_img, 1, s);
-  mlp_train_step(L.train_img, L.params, S.xs, S.ts, B, 0, 0, 0, B, sc, S.part, S.loss_part, S.err, s);
-  mlp_train_update(S.part, mlp_train_tiles(B), S.loss_part, L.params, L.grads, nullptr, nullptr, L.train_img, d_loss,
-                   0, 0.f, 1.f, 1.f, s);
-  ctx->launches += 3;
+  mlp_train_step(L.train_img, L.params, S.xs, S.ts, B, 0, 0, 0, B, sc, S.part, S.loss_part, S.err, s, stall_test);
+  ctx->launches += 2;
+  if (!stall_test) {
+    mlp_train_update(S.part, mlp_train_tiles(B), S.loss_part, L.params, L.grads, nullptr, nullptr, L.train_img,
+                     d_loss, 0, 0.f, 1.f, 1.f, s);
+    ctx->launches += 1;
+  }
   CHECK_LAUNCH();
   unsigned int errw = 0;
-  CU(cudaMemcpyAsync(grads, ctx->loc.grads, 4ull * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
-  CU(cudaMemcpyAsync(loss, d_loss, 4, cudaMemcpyDeviceToHost, s));
+  if (!stall_test) {
+    CU(cudaMemcpyAsync(grads, ctx->loc.grads, 4ull * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(loss, d_loss, 4, cudaMemcpyDeviceToHost, s));
+  }
   CU(cudaMemcpyAsync(&errw, S.err, 4, cudaMemcpyDeviceToHost, s));
   CU(cudaStreamSynchronize(s));
   if (errw & ERRBIT_TC_TIMEOUT) return fail(ctx, FDF_ERR_GPU, "fdf_LocatorGradients: tensor-core wait timed out");
   return FDF_SUCCESS;
+}
+
+int fdf_LocatorGradients(FdfContext *ctx, const float *xhat, const float *target, int64_t batch, float *grads,
+                         float *loss) {
+  return locator_gradients(ctx, xhat, target, batch, grads, loss, 0);
+}
+
+int fdf_TestLocatorTrainTimeout(FdfContext *ctx, const float *xhat, const float *target, int64_t batch) {
+  return locator_gradients(ctx, xhat, target, batch, nullptr, nullptr, 1);
 }
 
 int fdf_LocatorTrain(FdfContext *ctx, int64_t n_samples, uint64_t seed, int64_t steps, int64_t batch, double lr,

@@ -150,7 +150,8 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
     k_train_tc(const unsigned char *__restrict__ wimg, const float *__restrict__ params, const float *__restrict__ xs,
                const float *__restrict__ ts, long long n_samples, unsigned long long seed, long long step,
                int hashed, int B, float sx, float sy, float sz, float *__restrict__ part,
-               float *__restrict__ loss_part, unsigned int *__restrict__ err, unsigned long long wait_limit) {
+               float *__restrict__ loss_part, unsigned int *__restrict__ err, unsigned long long wait_limit,
+               int stall_test) {
   using namespace fdftc;
   extern __shared__ __align__(1024) unsigned char smem[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -298,8 +299,8 @@ __global__ void __launch_bounds__(TT_THREADS, 1)
   do {
     // ---- forward: C1 = X W1x^T, then C2, C3, and the output
     sync_issue();
-    if (tid == 0) {
-      fence_after_sync();
+    if (tid == 0 && !stall_test) {   // stall_test (tests of the time-out path only): nothing is
+      fence_after_sync();            // issued or committed, so the first wait runs out
       gemm_kk(tmem + TT_C1, aX, 256, sb + MLP_IMG_W1, 256, id_h, 1);
       mma_commit(bar);
     }
@@ -504,7 +505,8 @@ void mlp_make_samples(const double *x, const double *y, const double *z, const i
 
 void mlp_train_step(const unsigned char *wimg, const float *params, const float *xs, const float *ts,
                     long long n_samples, unsigned long long seed, long long step, int hashed, int B,
-                    const float sc[3], float *part, float *loss_part, unsigned int *err, cudaStream_t s) {
+                    const float sc[3], float *part, float *loss_part, unsigned int *err, cudaStream_t s,
+                    int stall_test) {
   static int attr_device = -1;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -513,7 +515,8 @@ void mlp_train_step(const unsigned char *wimg, const float *params, const float 
     attr_device = dev;
   }
   k_train_tc<<<(unsigned)mlp_train_tiles(B), TT_THREADS, TT_SM_LAUNCH, s>>>(
-      wimg, params, xs, ts, n_samples, seed, step, hashed, B, sc[0], sc[1], sc[2], part, loss_part, err, GT_WAIT_LIMIT);
+      wimg, params, xs, ts, n_samples, seed, step, hashed, B, sc[0], sc[1], sc[2], part, loss_part, err,
+      stall_test ? 1024ull : GT_WAIT_LIMIT, stall_test);
 }
 void mlp_train_update(const float *part, int tiles, const float *loss_part, float *params, float *grads, float *m,
                       float *v, unsigned char *wimg, float *loss_out, int adam, float lr, float c1, float c2,

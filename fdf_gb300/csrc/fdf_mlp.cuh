@@ -56,10 +56,13 @@ void mlp_flag_located(const int *cell, const unsigned char *status, long long n,
 // the current weights, params the FP32 parameters (the biases are read from there).  Each tile
 // writes its gradient partials to part [tiles][MLP_PART_STRIDE] and its share of the loss to
 // loss_part [tiles].  mlp_train_update then adds the partials in tile order into grads (and the
-// loss into *loss_out), and with adam != 0 takes the Adam step on params and rewrites wimg.
+// loss into *loss_out), and with adam != 0 takes the Adam step on params and rewrites wimg.  A
+// timed-out tensor-core wait sets ERRBIT_TC_TIMEOUT in *err; stall_test != 0 is for tests of that
+// path: no MMA is issued, so each CTA's first bounded wait (1024 polls) runs out.
 void mlp_train_step(const unsigned char *wimg, const float *params, const float *xs, const float *ts,
                     long long n_samples, unsigned long long seed, long long step, int hashed, int B,
-                    const float sc[3], float *part, float *loss_part, unsigned int *err, cudaStream_t s);
+                    const float sc[3], float *part, float *loss_part, unsigned int *err, cudaStream_t s,
+                    int stall_test = 0);
 void mlp_train_update(const float *part, int tiles, const float *loss_part, float *params, float *grads, float *m,
                       float *v, unsigned char *wimg, float *loss_out, int adam, float lr, float c1, float c2,
                       cudaStream_t s);

@@ -379,6 +379,12 @@ int fdf_TestFailDeviceAllocations(int64_t after);
  * FDF_ERR_GPU as a real time-out would.  Nothing is left in flight: the next call works.
  * No counterpart in the reference. */
 int fdf_TestLocatorWaitTimeout(FdfContext *ctx, const double *position, int64_t n);
+/* Time-out path of the locator's fused training kernel: fdf_LocatorGradients' training launch on
+ * the batch xhat, target [batch][3] with no MMA issued, so that each CTA's first bounded mbarrier
+ * wait (1024 polls) runs out; the CTAs free their tensor memory and return, and the call returns
+ * FDF_ERR_GPU as a real time-out would.  Nothing is left in flight and the weights are untouched:
+ * the next call works.  No counterpart in the reference. */
+int fdf_TestLocatorTrainTimeout(FdfContext *ctx, const float *xhat, const float *target, int64_t batch);
 
 #ifdef __cplusplus
 }

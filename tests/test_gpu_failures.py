@@ -146,6 +146,29 @@ def test_tensor_core_wait_runs_out(require_gpu):
     assert np.array_equal(cells0, cells1) and np.array_equal(y0, y1)
 
 
+def test_training_tensor_core_wait_runs_out(require_gpu):
+    """The fused training kernel's bounded wait, made to run out with no MMA in flight: the call
+    reports the time-out, the weights are untouched, and the next gradient call equals the one
+    before it."""
+    wl = W.config_bent_pipe(8, 6, 16, n=2000, cfl=1.0)
+    rng = np.random.default_rng(5)
+    B = 300
+    xhat = np.ascontiguousarray(rng.uniform(-1, 1, size=(B, 3)).astype(np.float32))
+    tgt = np.ascontiguousarray(rng.uniform(-1, 1, size=(B, 3)).astype(np.float32))
+    with PicContext(0) as ctx:
+        ctx.set_grid(wl.coor)
+        ctx.locator_init(seed=3)
+        p0 = ctx.locator_get_params()
+        g0, l0 = ctx.locator_gradients(xhat, tgt)
+        rc = ctx.lib.fdf_TestLocatorTrainTimeout(ctx.h, ctypes.c_void_p(xhat.ctypes.data),
+                                                 ctypes.c_void_p(tgt.ctypes.data), B)
+        assert rc == ERR_GPU
+        assert b"timed out" in ctx.lib.fdf_GetLastError(ctx.h)
+        g1, l1 = ctx.locator_gradients(xhat, tgt)   # nothing left in flight: the next call works
+        assert np.array_equal(p0, ctx.locator_get_params())
+    assert np.array_equal(g0, g1) and l0 == l1
+
+
 def test_locate_points_out_of_range_start_cells(require_gpu):
     wl = W.config_sinusoidal(IM=10, JM=8, KM=20, n=10, cfl=1.0, steps=1)
     g = O.Grid(wl.coor)
