@@ -124,9 +124,11 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 }
 
 // Threads per block of the advect + locate kernels.  A block keeps its SM slot until its
-// slowest walk ends, so smaller blocks waste fewer warp slots on the walk-length tail.
+// slowest walk ends, so smaller blocks waste fewer warp slots on the walk-length tail (FP32 walk
+// per 64M-particle step at 1152 resident threads: 3.15 ms in 64-thread blocks, 3.17 in 128, 3.18
+// in 96, 3.42 in 256).
 #ifndef FDF_LOC_THREADS
-#define FDF_LOC_THREADS 128
+#define FDF_LOC_THREADS 64
 #endif
 // Resident blocks per SM the FP32 locate kernels are compiled for.  The walk is bound by load
 // latency, so resident threads beat spills up to a point: with 176-B plane-table rows 1024
@@ -142,6 +144,10 @@ __device__ __forceinline__ void node_ijk(const GridDims &g, unsigned int q, int 
 // 1.59 -> 1.24 ms for the 64M-particle sort stage).
 #ifndef FDF_PLAIN_MIN_BLOCKS
 #define FDF_PLAIN_MIN_BLOCKS 8
+#endif
+// Threads per block of the plain walk (with FDF_PLAIN_MIN_BLOCKS: 1024 resident threads).
+#ifndef FDF_PLAIN_THREADS
+#define FDF_PLAIN_THREADS 128
 #endif
 #ifndef FDF_ORDER_MIN_BLOCKS
 #define FDF_ORDER_MIN_BLOCKS 8

@@ -42,7 +42,7 @@ using fdfx::add;
 using fdfx::sub;
 using fdfx::mul;
 
-__global__ void __launch_bounds__(FDF_LOC_THREADS, FDF_PLAIN_MIN_BLOCKS)
+__global__ void __launch_bounds__(FDF_PLAIN_THREADS, FDF_PLAIN_MIN_BLOCKS)
     k_locate(SwarmBuf b, GridDims g, const float *__restrict__ table, const double *__restrict__ planes, double dt,
                int advect, int reset_first, const double *__restrict__ bbox, int drop_removed, DevCounters *cnt,
                unsigned int *__restrict__ keys, unsigned int *__restrict__ rank, unsigned int *__restrict__ count,
@@ -155,7 +155,7 @@ void launch_locate(const SwarmBuf &b, int n_cap, GridDims g, const float *table,
                    int advect, const double *bbox, int drop_removed, DevCounters *cnt, unsigned int *keys,
                    unsigned int *rank, unsigned int *count, unsigned int sentinel, cudaStream_t s) {
   // advect and drop_removed are both set by the fused step, which also resets statuses first
-  constexpr int th = FDF_LOC_THREADS;
+  constexpr int th = FDF_PLAIN_THREADS;
   const unsigned int blocks = n_cap > 0 ? (unsigned int)((n_cap + th - 1) / th) : 1u;
   k_locate<<<blocks, th, 0, s>>>(b, g, table, planes, dt, advect, drop_removed, bbox, drop_removed, cnt,
                                                 keys, rank, count, sentinel);
