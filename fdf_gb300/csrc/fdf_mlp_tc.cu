@@ -8,8 +8,9 @@
 // arithmetic and store the activations as the next layer's A operand.  One CTA per SM holds
 // the weights once and runs four independent tile pipelines (one per warpgroup, each with its
 // own activation buffers, mbarrier and 128 TMEM columns), so the tensor core serves one
-// pipeline's MMAs while the others run their epilogues; each pipeline prefetches its next
-// tile's positions while the current tile computes.
+// pipeline's MMAs while the others run their epilogues.  Each epilogue reads the accumulator 32
+// columns at a time with the next 32 in flight, and each pipeline loads its next tile's particle
+// indices and positions one layer before it uses them, so neither latency stalls the chain.
 //
 // Input layer.  A bfloat16 coordinate carries 8 significant bits, coarser than a cell of a
 // long grid (1536 cells over the normalised range [-1, 1] are 0.0013 wide; bfloat16's spacing
@@ -115,14 +116,6 @@ __global__ void k_pack_tc(const float *__restrict__ params, unsigned char *__res
   reinterpret_cast<unsigned short *>(img)[q] = bits;
 }
 
-__device__ __forceinline__ float load_coord(const double *a, unsigned int r, int pairs) {
-  if (pairs) {
-    const float2 pr = *reinterpret_cast<const float2 *>(a + r);
-    return pr.x + pr.y;
-  }
-  return (float)a[r];
-}
-
 template <bool BF16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_mlp_guess_tc(const unsigned char *__restrict__ wimg, const float *__restrict__ bias_g, MlpNorm norm,
@@ -189,39 +182,63 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     fence_after_sync();
     return !bad;
   };
-  // bias + SiLU of the 128 accumulator columns (b: half-biases), stored as the next layer's A operand
-  // (the next chunk's TMEM load is in flight while a chunk is converted)
-  auto chunk = [&](const unsigned (&r)[16], const unsigned *b, int c) {
-    unsigned w[8];
+  // bias + SiLU of the 128 accumulator columns (b: half-biases), stored as the next layer's A operand,
+  // 32 columns at a time (the next 32 columns' TMEM load is in flight while a chunk is converted)
+  auto chunk = [&](const unsigned (&r)[32], const unsigned *b, int c) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      w[q] = silu2<BF16>(pack2<BF16>(__uint_as_float(r[2 * q]), __uint_as_float(r[2 * q + 1])), b[8 * c + q]);
-    *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4 *>(as + op_off(row, 16 * c + 8, 2048)) = make_uint4(w[4], w[5], w[6], w[7]);
+    for (int h = 0; h < 4; ++h) {
+      unsigned w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int pq = 4 * h + q;   // column pair within the chunk
+        w[q] = silu2<BF16>(pack2<BF16>(__uint_as_float(r[2 * pq]), __uint_as_float(r[2 * pq + 1])), b[16 * c + pq]);
+      }
+      *reinterpret_cast<uint4 *>(as + op_off(row, 32 * c + 8 * h, 2048)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
   };
   auto epilogue = [&](const unsigned *b) {
-    unsigned ra[16], rb[16];
-    tmem_ld16_issue(tmem + lane_base, ra);
-    tmem_wait_ld(ra);
-#pragma unroll 1
-    for (int c = 0; c < 8; c += 2) {
-      tmem_ld16_issue(tmem + lane_base + (unsigned)(16 * (c + 1)), rb);
-      chunk(ra, b, c);
-      tmem_wait_ld(rb);
-      if (c + 2 < 8) tmem_ld16_issue(tmem + lane_base + (unsigned)(16 * (c + 2)), ra);
-      chunk(rb, b, c + 1);
-      if (c + 2 < 8) tmem_wait_ld(ra);
+    unsigned ra[32], rb[32];
+    tmem_ld32_issue(tmem + lane_base, ra);
+    tmem_wait_ld32(ra);
+    tmem_ld32_issue(tmem + lane_base + 32u, rb);
+    chunk(ra, b, 0);
+    tmem_wait_ld32(rb);
+    tmem_ld32_issue(tmem + lane_base + 64u, ra);
+    chunk(rb, b, 1);
+    tmem_wait_ld32(ra);
+    tmem_ld32_issue(tmem + lane_base + 96u, rb);
+    chunk(ra, b, 2);
+    tmem_wait_ld32(rb);
+    chunk(rb, b, 3);
+  };
+  // the next tile's inputs in two steps whose loads are consumed one layer later: its particle
+  // index, then the raw 8-byte coordinates (an FP64 value, or a float pair (hi, lo))
+  constexpr unsigned NO_ROW = 0xffffffffu;
+  auto fetch_index = [&](long long tile) -> unsigned {
+    const long long r = tile * TC_ROWS + row;
+    if (tile >= ntiles || r >= n) return NO_ROW;
+    return list ? list[r] : (unsigned int)r;
+  };
+  auto fetch_raw = [&](unsigned p, unsigned long long (&raw)[3]) {
+    raw[0] = raw[1] = raw[2] = 0ull;
+    if (p != NO_ROW) {
+      raw[0] = reinterpret_cast<const unsigned long long *>(px)[p];
+      raw[1] = reinterpret_cast<const unsigned long long *>(py)[p];
+      raw[2] = reinterpret_cast<const unsigned long long *>(pz)[p];
     }
   };
-  auto load_inputs = [&](long long tile, float &x, float &y, float &z) {
-    const long long r = tile * TC_ROWS + row;
-    x = 0.f; y = 0.f; z = 0.f;
-    if (tile < ntiles && r < n) {
-      const unsigned int p = list ? list[r] : (unsigned int)r;
-      x = (load_coord(px, p, pairs) - norm.centre[0]) * norm.inv_half[0];
-      y = (load_coord(py, p, pairs) - norm.centre[1]) * norm.inv_half[1];
-      z = (load_coord(pz, p, pairs) - norm.centre[2]) * norm.inv_half[2];
+  auto to_inputs = [&](unsigned p, const unsigned long long (&raw)[3], float &x, float &y, float &z) {
+    float c[3] = {0.f, 0.f, 0.f};
+    if (p != NO_ROW) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float v = pairs ? __int_as_float((int)(unsigned)(raw[d] & 0xffffffffull)) +
+                                    __int_as_float((int)(unsigned)(raw[d] >> 32))
+                              : (float)__longlong_as_double((long long)raw[d]);
+        c[d] = (v - norm.centre[d]) * norm.inv_half[d];
+      }
     }
+    x = c[0]; y = c[1]; z = c[2];
   };
   // the MMAs of one layer, issued by the pipeline's first thread after its threads' stores
   auto issue = [&](int layer) {
@@ -245,7 +262,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   };
 
   float cx, cy, cz;
-  load_inputs(tile0, cx, cy, cz);
+  {
+    unsigned long long raw[3];
+    const unsigned p0 = fetch_index(tile0);
+    fetch_raw(p0, raw);
+    to_inputs(p0, raw, cx, cy, cz);
+  }
 #pragma unroll 1
   for (long long tile = tile0; tile < ntiles; tile += tstride) {
     const long long r = tile * TC_ROWS + row;
@@ -261,10 +283,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // stall_test (tests of the time-out path only): nothing is issued or committed, so the wait
     // below runs out with no MMA in flight
     if (!stall_test) issue(0);
-    load_inputs(tile + tstride, cx, cy, cz);   // the next tile's positions, while this one computes
+    const unsigned np = fetch_index(tile + tstride);   // the next tile's rows, while this one computes
     if (!wait_mma()) { timed_out = true; break; }
     epilogue(hb2);
     issue(1);
+    unsigned long long nraw[3];
+    fetch_raw(np, nraw);
     if (!wait_mma()) { timed_out = true; break; }
     epilogue(hb2 + 64);
     issue(2);
@@ -289,6 +313,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         guess[r] = (idx[2] * g.JM + idx[1]) * g.IM + idx[0];
       }
     }
+    to_inputs(np, nraw, cx, cy, cz);
     fence_before_sync();   // this tile's TMEM reads finish before the next tile's MMAs (ordered by issue(0))
   }
   if (timed_out && row == 0) atomicOr(err, (unsigned)ERRBIT_TC_TIMEOUT);
