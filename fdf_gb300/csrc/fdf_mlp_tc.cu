@@ -172,11 +172,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   auto pipe_sync = [&]() { asm volatile("bar.sync %0, 128;\n" ::"r"(pipe_bar) : "memory"); };
   // waits for the MMAs this pipeline committed last; its 128 threads agree on a time-out
+  // (only the pipeline's first warp polls: the others wait at the named barrier, which issues
+  // nothing, so the other pipelines' epilogues keep the schedulers)
   auto wait_mma = [&]() -> bool {
-    bool done = false;
-    for (unsigned long long it = 0; it < wait_limit && !done; ++it) done = mbar_try_wait(bar_addr, phase);
+    if (row < 32) {
+      bool done = false;
+      for (unsigned long long it = 0; it < wait_limit && !done; ++it) done = mbar_try_wait(bar_addr, phase);
+      if (!done) tflag[pipe] = 1u;
+    }
     phase ^= 1u;
-    if (!done) tflag[pipe] = 1u;
     pipe_sync();
     const bool bad = tflag[pipe] != 0u;
     fence_after_sync();
