@@ -749,7 +749,7 @@ def run_gpu(args, rank, ws, local, dist):
                       **({"learned_locator": r["learned"]} if r["learned"] else {})}
                   for f, r in results.items()}
     identity = None
-    if "learned_fp32" in forms and args.identity_steps > 0:
+    if "learned_fp32" in forms and args.identity_steps > 0 and ws == 1:   # a check, not a measurement
         identity = learned_identity(ctx, wl, args, args.identity_steps)
     prepare(ctx, wl, forms[0], args)
     ctx.initial_setup()
