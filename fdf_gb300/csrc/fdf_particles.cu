@@ -457,9 +457,7 @@ void launch_gather_interp(const SwarmBuf &src, const SwarmBuf &dst, int n_cap, G
 void launch_deposit(const SwarmBuf &b, GridDims g, const unsigned int *cell_start, double volume, double *count,
                     double *avg, double *fi, double *fj, double *fk, double *mi, double *mj, double *mk,
                     cudaStream_t s) {
-  int th = 256;
-  long long blocks = (g.Nn + th - 1) / th;
-  double third = volume / 3.0;
+  const double third = volume / 3.0;
   if (mi)
     k_deposit_mom_staged<<<(unsigned)((g.Nn + DEPM_WARPS * 32 - 1) / (DEPM_WARPS * 32)), DEPM_WARPS * 32, 0, s>>>(
         b, g, cell_start, third, count, avg, fi, fj, fk, mi, mj, mk);
