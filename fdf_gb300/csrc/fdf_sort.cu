@@ -112,18 +112,39 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(unsigned int *__res
 }
 
 // Slot of every kept particle: cell_start[key] + its rank among the particles of the same
-// key, which the locate kernels took from their histogram atomics.
+// key, which the locate kernels took from their histogram atomics.  Each thread handles
+// FDF_SCATTER_ITEMS particles (strided by the block, so every load stays coalesced) and issues
+// all their loads before their stores: the cell_start gather depends on the key, so a thread
+// with one particle waits two load latencies for one store (sort stage per 64M-particle step:
+// 0.78 ms with one particle per thread, 0.66 with 2, 0.61 with 4, 0.63 with 8).
+#ifndef FDF_SCATTER_ITEMS
+#define FDF_SCATTER_ITEMS 4
+#endif
 __global__ void __launch_bounds__(256) k_scatter_slots(const unsigned int *__restrict__ keys,
                                                       const unsigned int *__restrict__ rank, const DevCounters *cnt,
                                                       unsigned int sentinel, int keep_lost,
                                                       const unsigned int *__restrict__ cell_start,
                                                       unsigned int *__restrict__ perm) {
-  const int n = cnt->n_sorted;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const unsigned int key = keys[s];   // sentinel: a LOST particle kept at the end; above: removed
-  if (key > sentinel || (key == sentinel && !keep_lost)) return;
-  perm[cell_start[key] + rank[s]] = (unsigned int)s;
+  constexpr int IT = FDF_SCATTER_ITEMS;
+  const long long n = cnt->n_sorted;
+  const long long base = (long long)blockIdx.x * IT * blockDim.x + threadIdx.x;
+  unsigned int key[IT], start[IT], rk[IT];
+  bool keep[IT];
+#pragma unroll
+  for (int q = 0; q < IT; ++q) {
+    const long long s = base + (long long)q * blockDim.x;
+    key[q] = s < n ? keys[s] : 0xffffffffu;   // sentinel: a LOST particle kept at the end; above: removed
+    keep[q] = key[q] < sentinel || (key[q] == sentinel && keep_lost);
+  }
+#pragma unroll
+  for (int q = 0; q < IT; ++q) {
+    const long long s = base + (long long)q * blockDim.x;
+    start[q] = keep[q] ? cell_start[key[q]] : 0u;
+    rk[q] = keep[q] ? rank[s] : 0u;
+  }
+#pragma unroll
+  for (int q = 0; q < IT; ++q)
+    if (keep[q]) perm[start[q] + rk[q]] = (unsigned int)(base + (long long)q * blockDim.x);
 }
 
 // Orders every cell's slots by (PID, previous slot) -- or by previous slot alone when
@@ -244,8 +265,8 @@ void exclusive_scan_u32(unsigned int *data, long long count, unsigned int *sums,
 void launch_scatter_slots(const unsigned int *keys, const unsigned int *rank, int n_cap, const DevCounters *cnt,
                           unsigned int sentinel, int keep_lost, const unsigned int *cell_start, unsigned int *perm,
                           cudaStream_t s) {
-  int th = 256;
-  int blocks = (n_cap + th - 1) / th;
+  const int th = 256, per_block = th * FDF_SCATTER_ITEMS;
+  int blocks = (n_cap + per_block - 1) / per_block;
   if (blocks == 0) blocks = 1;
   k_scatter_slots<<<blocks, th, 0, s>>>(keys, rank, cnt, sentinel, keep_lost, cell_start, perm);
 }
