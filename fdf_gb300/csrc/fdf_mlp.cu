@@ -106,8 +106,8 @@ constexpr unsigned TT_SM_BIAS = TT_SM_RED + 2048;    // b1 | b2 | b3 | b4 in FP3
 constexpr unsigned TT_SM_LOSS = TT_SM_BIAS + 1600;   // [4] per-warp loss sums
 constexpr unsigned TT_SM_BAR = TT_SM_LOSS + 32;      // mbarrier (8 B), TMEM base (4 B), time-out flag (4 B)
 constexpr unsigned TT_SM_END = TT_SM_BAR + 16;
-// The allocation leaves room beyond the last operand, so every descriptor's reach stays inside it,
-// and keeps one CTA per SM (the CTA takes all 512 TMEM columns).
+// The allocation, more than half an SM's shared memory, keeps one CTA per SM: the CTA takes all
+// 512 TMEM columns, so a second one would wait in its allocation.
 constexpr unsigned TT_SM_LAUNCH = 192 * 1024;
 static_assert(TT_SM_END <= TT_SM_LAUNCH && TT_SM_LAUNCH > 114 * 1024, "training step shared memory");
 constexpr unsigned TT_C1 = 0, TT_C2 = 128, TT_C3 = 256, TT_D = 384;
